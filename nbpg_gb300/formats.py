@@ -1,0 +1,97 @@
+"""Readers and writers for the NBPG on-disk formats (byte-identical to the reference).
+
+* vectors  ``.u8bin .i8bin .u4bin .i4bin .fbin``: ``[n u32][dims u32][n*dims*sizeof(T) bytes]``
+  (algorithms/utils/Point/point_range.h:18-30, disk_point_range.h:16-25).  For the
+  packed 4-bit types ``dims`` counts bytes (two codes per byte).
+* graph ``<index>.graph``: ``[N u32][R u32][deg u32 x N][neighbours of node 0, 1, ...]``
+  (algorithms/utils/Graph/graph.h:169-221 load, 339-379 save).  In memory a graph is
+  an ``(N, R+1)`` u32 array whose column 0 is the degree, as in graph.h:18-116.
+* ground truth ``.gt``: ``[nq u32][k u32][ids u32 nq*k][dists f32 nq*k]``
+  (data_tools/ANNs/data_proc/CompGT.cpp:126-133, data_tools/ANNs/base/ground_truth.h:26-46).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+EXT_DTYPE = {
+    ".u8bin": ("u8", np.uint8),
+    ".i8bin": ("i8", np.int8),
+    ".u4bin": ("u4", np.uint8),
+    ".i4bin": ("i4", np.uint8),
+    ".fbin": ("f32", np.float32),
+    ".bin": ("f32", np.float32),
+}
+
+
+def dtype_of_path(path: str) -> str:
+    for ext, (name, _) in EXT_DTYPE.items():
+        if path.endswith(ext):
+            return name
+    raise ValueError(f"unknown vector file extension: {path}")
+
+
+def read_head(path: str) -> tuple[int, int]:
+    with open(path, "rb") as f:
+        n, d = np.fromfile(f, dtype=np.uint32, count=2)
+    return int(n), int(d)
+
+
+def read_vectors(path: str, limit: int | None = None) -> np.ndarray:
+    """Load a vector file as an (n, dims) array; 4-bit files come back as packed bytes."""
+    _, np_t = EXT_DTYPE[[e for e in EXT_DTYPE if path.endswith(e)][0]]
+    with open(path, "rb") as f:
+        n, d = (int(x) for x in np.fromfile(f, dtype=np.uint32, count=2))
+        if limit is not None:
+            n = min(n, limit)
+        data = np.fromfile(f, dtype=np_t, count=n * d)
+    if data.size != n * d:
+        raise ValueError(f"{path}: truncated ({data.size} of {n * d} elements)")
+    return data.reshape(n, d)
+
+
+def write_vectors(path: str, x: np.ndarray) -> None:
+    x = np.ascontiguousarray(x)
+    with open(path, "wb") as f:
+        np.array([x.shape[0], x.shape[1]], dtype=np.uint32).tofile(f)
+        x.tofile(f)
+
+
+def read_graph(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        n, R = (int(x) for x in np.fromfile(f, dtype=np.uint32, count=2))
+        deg = np.fromfile(f, dtype=np.uint32, count=n)
+        nbrs = np.fromfile(f, dtype=np.uint32, count=int(deg.sum()))
+    if deg.size != n or nbrs.size != int(deg.sum()) or (deg > R).any():
+        raise ValueError(f"{path}: malformed graph file")
+    g = np.zeros((n, R + 1), dtype=np.uint32)
+    g[:, 0] = deg
+    mask = np.arange(R)[None, :] < deg[:, None]
+    g[:, 1:][mask] = nbrs
+    return g
+
+
+def write_graph(path: str, g: np.ndarray) -> None:
+    g = np.ascontiguousarray(g, dtype=np.uint32)
+    n, R1 = g.shape
+    deg = g[:, 0]
+    mask = np.arange(R1 - 1)[None, :] < deg[:, None]
+    with open(path, "wb") as f:
+        np.array([n, R1 - 1], dtype=np.uint32).tofile(f)
+        deg.tofile(f)
+        g[:, 1:][mask].tofile(f)
+
+
+def read_gt(path: str) -> tuple[np.ndarray, np.ndarray]:
+    with open(path, "rb") as f:
+        nq, k = (int(x) for x in np.fromfile(f, dtype=np.uint32, count=2))
+        ids = np.fromfile(f, dtype=np.uint32, count=nq * k).reshape(nq, k)
+        ds = np.fromfile(f, dtype=np.float32, count=nq * k).reshape(nq, k)
+    return ids, ds
+
+
+def write_gt(path: str, ids: np.ndarray, dists: np.ndarray) -> None:
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    with open(path, "wb") as f:
+        np.array(ids.shape, dtype=np.uint32).tofile(f)
+        ids.tofile(f)
+        np.ascontiguousarray(dists, dtype=np.float32).tofile(f)

@@ -1,0 +1,798 @@
+// CPU oracle for the NBPG hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is a plain C++/OpenMP restatement of the
+// reference's algorithms, used as the parity checker for the CUDA library and as
+// the CPU baseline that bench.py times.  Nothing in the product links it.
+//
+// Every routine cites the reference file:line it restates (paths relative to the
+// godpgf/NBPG source tree).  The semantics that matter for bit-exact parity are
+// kept exactly: int32 distance accumulation converted to float, the lossy
+// direct-mapped visited filter, the deferred candidate merge, the cut rule with
+// its float-rounded threshold, the capped sorted visited list, merge_union on an
+// unsorted first range, sort_candidates, RobustPrune with a double alpha, the
+// reverse-edge grouping/truncation, popularity propagation and isolated-node
+// repair, and CompGT's replace-max rule with its stale read.
+//
+// Pinning: tests compare this oracle with a harness that compiles the reference
+// headers in place (oracle/ref_harness.cpp) and with golden vectors generated from
+// the reference binaries (tests/golden/).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <numeric>
+#include <queue>
+#include <random>
+#include <vector>
+#include <omp.h>
+
+namespace {
+
+enum Dtype : int { DT_U8 = 0, DT_I8 = 1, DT_U4 = 2, DT_I4 = 3, DT_F32 = 4 };
+enum Metric : int { M_L2 = 0, M_IP = 1 };
+
+// ---------------------------------------------------------------------------
+// Distances: algorithms/utils/Point/point.h:27-156
+// ---------------------------------------------------------------------------
+
+// point.h:27-32 — both nibbles scaled by 16; the signed type loses its sign.
+inline void split_byte(uint8_t b, int32_t &hi, int32_t &lo)
+{
+    hi = static_cast<int32_t>(b & 0xF0);
+    lo = static_cast<int32_t>(static_cast<uint8_t>(b << 4));
+}
+
+float dist_rows(int dtype, int metric, const uint8_t *a, const uint8_t *b, uint32_t dims)
+{
+    if (dtype == DT_F32) {
+        // point.h:137-156 — float accumulation in element order.
+        const float *x = reinterpret_cast<const float *>(a);
+        const float *y = reinterpret_cast<const float *>(b);
+        float r = 0.0f;
+        if (metric == M_L2) {
+            for (uint32_t i = 0; i < dims; ++i) { float d = x[i] - y[i]; r += d * d; }
+            return r;
+        }
+        for (uint32_t i = 0; i < dims; ++i) r += x[i] * y[i];
+        return -r;
+    }
+    int32_t r = 0;
+    if (dtype == DT_U8) {  // point.h:35-54
+        if (metric == M_L2)
+            for (uint32_t i = 0; i < dims; ++i) { int32_t d = int32_t(a[i]) - int32_t(b[i]); r += d * d; }
+        else
+            for (uint32_t i = 0; i < dims; ++i) r += int32_t(a[i]) * int32_t(b[i]);
+    } else if (dtype == DT_I8) {  // point.h:56-75
+        const int8_t *x = reinterpret_cast<const int8_t *>(a);
+        const int8_t *y = reinterpret_cast<const int8_t *>(b);
+        if (metric == M_L2)
+            for (uint32_t i = 0; i < dims; ++i) { int32_t d = int32_t(x[i]) - int32_t(y[i]); r += d * d; }
+        else
+            for (uint32_t i = 0; i < dims; ++i) r += int32_t(x[i]) * int32_t(y[i]);
+    } else {  // DT_U4 / DT_I4: point.h:77-135 (identical arithmetic for both)
+        for (uint32_t i = 0; i < dims; ++i) {
+            int32_t ah, al, bh, bl;
+            split_byte(a[i], ah, al);
+            split_byte(b[i], bh, bl);
+            if (metric == M_L2) r += (ah - bh) * (ah - bh) + (al - bl) * (al - bl);
+            else r += ah * bh + al * bl;
+        }
+    }
+    return metric == M_L2 ? static_cast<float>(r) : -static_cast<float>(r);
+}
+
+inline size_t row_bytes(int dtype, uint32_t dims) { return dtype == DT_F32 ? size_t(dims) * 4 : size_t(dims); }
+
+// ---------------------------------------------------------------------------
+// Visited filter: algorithms/utils/utilities.h:31-37 (hash64_2),
+// algorithms/utils/Graph/query_params.h:223-247 (has_been_seen, table size)
+// ---------------------------------------------------------------------------
+inline uint64_t splitmix_final(uint64_t x)
+{
+    x = (x ^ (x >> 30)) * UINT64_C(0xbf58476d1ce4e5b9);
+    x = (x ^ (x >> 27)) * UINT64_C(0x94d049bb133111eb);
+    return x ^ (x >> 31);
+}
+
+uint32_t filter_slots(uint32_t L)
+{
+    int bits = std::max<int>(10, int(std::ceil(std::log2(double(uint32_t(L * L))))) - 2);
+    return 1u << bits;
+}
+
+// (id, dist) ordered by dist then id: query_params.h:97-119
+struct Node {
+    uint32_t id;
+    float d;
+};
+inline bool node_less(const Node &a, const Node &b) { return a.d < b.d || (a.d == b.d && a.id < b.id); }
+
+struct GraphView {
+    const uint32_t *rows;  // n rows of (R+1) u32: [degree, ids...] (graph.h:18-116)
+    uint32_t R;
+    uint32_t degree(uint32_t v) const { return rows[size_t(v) * (R + 1)]; }
+    uint32_t nbr(uint32_t v, uint32_t i) const { return rows[size_t(v) * (R + 1) + 1 + i]; }
+};
+
+// Per-search working set: query_params.h:131-260 (BeamSearchMemoryCell)
+struct Cell {
+    uint32_t L = 0, max_visited = 0, slots = 0;
+    std::vector<Node> frontier, new_frontier, unvisited, candidates, visited, pool;
+    std::vector<uint32_t> table, filtered;
+    size_t fs = 0, vs = 0, num_visited = 0;
+
+    void reset(uint32_t L_, uint32_t max_visited_, uint32_t R)
+    {
+        L = L_;
+        max_visited = max_visited_;
+        slots = filter_slots(L_);
+        size_t fcap = std::max<size_t>(L_, R) + 1;
+        if (frontier.size() < fcap) frontier.resize(fcap);
+        if (unvisited.size() < fcap) unvisited.resize(fcap);
+        if (new_frontier.size() < 2 * size_t(L_) + R + 1) new_frontier.resize(2 * size_t(L_) + R + 1);
+        if (candidates.size() < size_t(L_) + R + 1) candidates.resize(size_t(L_) + R + 1);
+        if (visited.size() < max_visited_ + 1) visited.resize(max_visited_ + 1);
+        if (pool.size() < max_visited_ + 1) pool.resize(max_visited_ + 1);
+        if (filtered.size() < R + 1) filtered.resize(R + 1);
+        if (table.size() < slots) table.resize(slots);
+        std::fill_n(table.begin(), slots, 0xFFFFFFFFu);
+        fs = vs = num_visited = 0;
+    }
+
+    bool seen(uint32_t a)
+    {
+        uint32_t slot = uint32_t(splitmix_final(a) & (slots - 1));
+        if (table[slot] == a) return true;
+        table[slot] = a;
+        return false;
+    }
+};
+
+// query_params.h:204-221
+template <class DistTo>
+void seed_frontier(Cell &c, const uint32_t *sp, uint32_t nsp, DistTo dist_to)
+{
+    for (uint32_t s = 0; s < nsp; ++s) {
+        c.frontier[s] = Node{sp[s], dist_to(sp[s])};
+        c.seen(sp[s]);
+    }
+    c.fs = nsp;
+    std::sort(c.frontier.begin(), c.frontier.begin() + nsp, node_less);
+    std::copy(c.frontier.begin(), c.frontier.begin() + nsp, c.unvisited.begin());
+}
+
+// Greedy beam search: algorithms/utils/Graph/beamSearch.h:43-171 with
+// Points == Q_Points (the pure quantized path used by both query and build).
+// `self` is the node being inserted (Points[a].same_as(p), beamSearch.h:79) or -1.
+template <class DistTo>
+size_t beam_search(Cell &c, const GraphView &G, DistTo dist_to, int64_t self, uint32_t k, double cut,
+                   uint64_t limit, uint32_t degree_limit)
+{
+    const uint32_t L = c.L;
+    size_t cmps = c.fs;
+    int remain = int(c.fs);
+    int offset = 0;
+    size_t cs = 0;
+    while (remain > offset && c.num_visited < limit) {
+        const Node cur = c.unvisited[offset];
+        const uint32_t ne = std::min(G.degree(cur.id), degree_limit);
+        size_t nf = 0;
+        for (uint32_t i = 0; i < ne; ++i) {
+            uint32_t a = G.nbr(cur.id, i);
+            if (c.seen(a) || int64_t(a) == self) continue;
+            c.filtered[nf++] = a;
+        }
+        for (size_t i = 0; i < nf; ++i) {
+            uint32_t a = c.filtered[i];
+            c.candidates[cs++] = Node{a, dist_to(a)};
+            ++cmps;
+        }
+        // sorted insert into the capped visited list (beamSearch.h:95-117)
+        size_t pos = size_t(std::upper_bound(c.visited.begin(), c.visited.begin() + c.vs, cur, node_less) -
+                            c.visited.begin());
+        ++c.num_visited;
+        if (c.vs < c.max_visited) ++c.vs;
+        if (pos + 1 < c.vs) std::memmove(&c.visited[pos + 1], &c.visited[pos], (c.vs - 1 - pos) * sizeof(Node));
+        if (pos < c.vs) c.visited[pos] = cur;
+
+        // deferred merge (beamSearch.h:119-125)
+        if (cs == 0 || (limit >= uint64_t(uint32_t(2 * L)) && cs < L / 8 && offset + 1 < remain)) {
+            ++offset;
+            continue;
+        }
+        offset = 0;
+        std::sort(c.candidates.begin(), c.candidates.begin() + cs, node_less);
+        size_t cu = size_t(std::unique(c.candidates.begin(), c.candidates.begin() + cs,
+                                       [](const Node &x, const Node &y) { return x.id == y.id; }) -
+                           c.candidates.begin());
+        size_t nfs = size_t(std::set_union(c.frontier.begin(), c.frontier.begin() + c.fs, c.candidates.begin(),
+                                           c.candidates.begin() + cu, c.new_frontier.begin(), node_less) -
+                            c.new_frontier.begin());
+        cs = 0;
+        nfs = std::min<size_t>(L, nfs);
+        // cut rule (beamSearch.h:140-149): threshold rounded to float through QNode
+        if (k > 0 && nfs > k) {
+            Node probe{0, float(cut * double(c.new_frontier[k].d))};
+            size_t ub = size_t(std::upper_bound(c.new_frontier.begin(), c.new_frontier.begin() + nfs, probe, node_less) -
+                               c.new_frontier.begin());
+            nfs = std::max<uint32_t>(uint32_t(ub), uint32_t(c.fs));
+        }
+        std::copy(c.new_frontier.begin(), c.new_frontier.begin() + nfs, c.frontier.begin());
+        c.fs = nfs;
+        remain = int(std::set_difference(c.frontier.begin(), c.frontier.begin() + std::min<size_t>(c.fs, L),
+                                         c.visited.begin(), c.visited.begin() + c.vs, c.unvisited.begin(), node_less) -
+                     c.unvisited.begin());
+    }
+    return cmps;
+}
+
+// ---------------------------------------------------------------------------
+// RobustPrune: algorithms/utils/Graph/prune.h:50-74 (sort_candidates),
+// prune.h:159-209 (limitedSimilarityPrune), prune.h:218-238 (rules)
+// ---------------------------------------------------------------------------
+constexpr double kEps = 1e-5;
+
+void dedupe_by_id(Node *c, size_t &n)
+{
+    std::sort(c, c + n, [](const Node &a, const Node &b) { return a.id < b.id; });
+    n = size_t(std::unique(c, c + n, [](const Node &a, const Node &b) { return a.id == b.id; }) - c);
+}
+
+// bias[d] = dir_bias_scale * log(d + 1) + 1 for degree d (prune.h:61-62); null = no bias.
+void sort_candidates(uint32_t p, const uint32_t *degrees, const double *bias, Node *c, size_t &n)
+{
+    dedupe_by_id(c, n);
+    auto key = [&](Node a) {
+        if (bias) a.d *= bias[degrees[a.id]];
+        if (a.id == p) a.d = std::numeric_limits<float>::max();
+        return a;
+    };
+    std::sort(c, c + n, [&](const Node &a, const Node &b) { return node_less(key(a), key(b)); });
+    while (n > 0 && c[n - 1].id == p) --n;
+}
+
+float cos_at_p(float d_p_star, float d_p_prime, float d_star_prime)
+{
+    const float b = std::sqrt(d_p_prime);
+    const float c = std::sqrt(d_p_star);
+    if (b == 0.f || c == 0.f) return 1.f;
+    return (d_p_prime + d_p_star - d_star_prime) / (2.f * b * c);
+}
+
+template <class PairDist>
+size_t robust_prune(uint32_t p, Node *c, size_t &n, uint32_t R, double alpha, double cos_angle, PairDist pair_dist)
+{
+    if (alpha <= kEps && cos_angle <= kEps) {
+        if (n > R) n = R;
+        return 0;
+    }
+    size_t cmps = 0, sel = 0, scan = 0;
+    const size_t start_prune_id = 1;
+    while (sel < R && scan < n) {
+        const uint32_t ps = c[scan].id;
+        ++scan;
+        if (ps == p || ps == 0xFFFFFFFFu) continue;
+        c[sel++] = c[scan - 1];
+        for (size_t i = scan; i < n; ++i) {
+            if (i < start_prune_id) continue;
+            const uint32_t pp = c[i].id;
+            if (pp == 0xFFFFFFFFu) continue;
+            ++cmps;
+            const float dsp = pair_dist(ps, pp);
+            const float dpp = c[i].d;
+            if (alpha > kEps && alpha * dsp <= dpp) c[i].id = 0xFFFFFFFFu;
+            else if (cos_angle > kEps && cos_at_p(c[scan - 1].d, dpp, dsp) > cos_angle) c[i].id = 0xFFFFFFFFu;
+        }
+    }
+    n = sel;
+    return cmps;
+}
+
+// utilities.h:128-165 — two-pointer union; the first range need not be sorted.
+size_t merge_union(const Node *a, size_t na, const Node *b, size_t nb, Node *out, size_t cap)
+{
+    size_t i = 0, j = 0, k = 0;
+    while (i < na && j < nb && k < cap) {
+        if (node_less(a[i], b[j])) out[k++] = a[i++];
+        else if (node_less(b[j], a[i])) out[k++] = b[j++];
+        else { out[k++] = a[i++]; ++j; }
+    }
+    while (i < na && k < cap) out[k++] = a[i++];
+    while (j < nb && k < cap) out[k++] = b[j++];
+    return k;
+}
+
+// ---------------------------------------------------------------------------
+// Build: algorithms/nsw.h:30-47 (batch schedule), 110-286 (batch_insert),
+// 288-324 (batch size, alpha), 329-378 (reverse-edge helpers),
+// 380-511 (batched phases), 547-663 (build_vamana); dfs.h:100-254 (repair)
+// ---------------------------------------------------------------------------
+enum class Popular { FixedMin = 1, FixedMax, Cal, Prune };
+
+struct BuildCfg {
+    int dtype, metric;
+    uint32_t dims;
+    const uint8_t *base;
+    size_t row;
+    uint64_t n;
+    uint32_t R, L, VL, top_degree, num_split, num_passes;
+    uint64_t limit;
+    float dir_bias_scale;
+    float min_alpha, max_alpha, min_cos, max_cos;  // stored as float (nsw.h:88-99, 538-540)
+};
+
+struct Builder {
+    BuildCfg cfg;
+    std::vector<uint32_t> &G;  // n*(R+1)
+    std::vector<float> popular;
+    float min_pop = 0.f, max_pop = 1.f;
+    std::vector<uint32_t> stat_visited, stat_dist;
+    std::vector<double> bias;  // per-degree bias factor, empty = none
+
+    Builder(const BuildCfg &c, std::vector<uint32_t> &g) : cfg(c), G(g)
+    {
+        stat_visited.assign(c.n, 0);
+        stat_dist.assign(c.n, 0);
+        if (c.dir_bias_scale > 0) {
+            bias.resize(c.R + 1);
+            for (uint32_t d = 0; d <= c.R; ++d) bias[d] = c.dir_bias_scale * std::log(double(d) + 1.0) + 1.0;
+        }
+    }
+
+    const uint8_t *pt(uint32_t v) const { return cfg.base + size_t(v) * cfg.row; }
+    float dist(uint32_t a, uint32_t b) const { return dist_rows(cfg.dtype, cfg.metric, pt(a), pt(b), cfg.dims); }
+    uint32_t *row(uint32_t v) { return &G[size_t(v) * (cfg.R + 1)]; }
+
+    std::pair<float, float> alpha_cos(uint32_t v, Popular mode) const
+    {
+        switch (mode) {
+        case Popular::FixedMin: return {cfg.max_alpha, cfg.max_cos};
+        case Popular::Prune: {
+            float cof = (popular[v] - max_pop) / (min_pop - max_pop);
+            float a = cof * (cfg.max_alpha - cfg.min_alpha);
+            a = cfg.min_alpha + a;
+            float cm = cof * (cfg.max_cos - cfg.min_cos);
+            cm = cfg.min_cos + cm;
+            return {a, cm};
+        }
+        default: return {1.0f, cfg.min_cos};
+        }
+    }
+
+    struct Result {
+        std::vector<Node> prune, vis;
+    };
+
+    // nsw.h:122-175 (searchNghAndPrune)
+    void search_and_prune(Cell &c, uint32_t index, const std::vector<uint32_t> &sps, Popular mode,
+                          const std::vector<uint32_t> &degrees, Result &res)
+    {
+        auto [alpha, cos_angle] = alpha_cos(index, mode);
+        GraphView gv{G.data(), cfg.R};
+        c.reset(cfg.L, cfg.VL, cfg.R);
+        auto dist_to = [&](uint32_t a) { return dist(a, index); };
+        seed_frontier(c, sps.data(), uint32_t(sps.size()), dist_to);
+        size_t cmps = beam_search(c, gv, dist_to, int64_t(index), 0, 0.0, cfg.limit, cfg.R);
+        stat_dist[index] += uint32_t(cmps);
+        stat_visited[index] += uint32_t(c.num_visited);
+
+        size_t nf = 0, rp = 0;
+        const uint32_t deg = gv.degree(index);
+        for (uint32_t i = 0; i < deg; ++i) {
+            uint32_t nb = gv.nbr(index, i);
+            if (!c.seen(nb)) {
+                c.frontier[nf++] = Node{nb, dist(nb, index)};
+                ++rp;
+            }
+        }
+        size_t np = merge_union(c.frontier.data(), nf, c.visited.data(), c.vs, c.pool.data(), cfg.VL);
+        sort_candidates(index, degrees.data(), bias.empty() ? nullptr : bias.data(), c.pool.data(), np);
+        rp += robust_prune(index, c.pool.data(), np, cfg.R, double(alpha), double(cos_angle),
+                           [&](uint32_t a, uint32_t b) { return dist(a, b); });
+        stat_dist[index] += uint32_t(rp);
+        res.prune.assign(c.pool.begin(), c.pool.begin() + np);
+        res.vis.assign(c.visited.begin(), c.visited.begin() + c.vs);
+    }
+
+    // nsw.h:329-355
+    size_t fill_new_dists(uint32_t index, Node *c, size_t pre, size_t n) const
+    {
+        size_t rp = 0;
+        size_t td = cfg.top_degree == 0 ? cfg.R : cfg.top_degree;
+        size_t end = std::min(pre + td, n);
+        for (size_t j = pre; j < end; ++j) { c[j].d = dist(c[j].id, index); ++rp; }
+        if (end < n) {
+            float a = c[end - 1].d;
+            float b = dist(c[n - 1].id, index);
+            c[n - 1].d = b;
+            ++rp;
+            float delta = (a - b) / float(n - end);
+            for (size_t j = end; j < n - 1; ++j) {
+                float step = float(j - end + 1) * delta;
+                c[j].d = a + step;
+            }
+        }
+        return rp;
+    }
+
+    void batch_insert(const std::vector<uint32_t> &inserts,
+                      const std::function<void(std::vector<std::vector<uint32_t>> &, size_t, size_t)> &fill_sp,
+                      Popular mode, int threads)
+    {
+        const uint64_t n = cfg.n;
+        size_t eff = std::min<size_t>(size_t(0.02 * double(float(n))), 1000000ul);
+        if (eff == 0) eff = 1;
+        std::vector<std::vector<uint32_t>> sp(eff);
+        std::vector<Result> res(eff);
+        std::vector<Cell> cells(std::max(1, threads));
+        std::vector<uint32_t> degrees(n);
+        if (mode == Popular::Cal) popular.assign(n, 0.0f);
+
+        size_t inc = 0, count = 0;
+        const size_t m = inserts.size();
+        while (count < m) {
+            size_t floor, ceiling;
+            if (std::pow(2.0, double(inc)) <= double(eff)) {
+                floor = size_t(std::pow(2.0, double(inc))) - 1;
+                ceiling = std::min(size_t(std::pow(2.0, double(inc + 1))) - 1, m);
+                count = ceiling;
+            } else {
+                floor = count;
+                ceiling = std::min(count + eff, m);
+                count = count + (ceiling - floor);
+            }
+            const size_t bs = ceiling - floor;
+            for (size_t i = 0; i < bs; ++i) sp[i].clear();
+            fill_sp(sp, floor, ceiling);
+            if (!bias.empty())
+                for (uint64_t v = 0; v < n; ++v) degrees[v] = G[size_t(v) * (cfg.R + 1)];
+
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 8)
+            for (long long i = 0; i < (long long)bs; ++i)
+                search_and_prune(cells[omp_get_thread_num()], inserts[floor + i], sp[i], mode, degrees, res[i]);
+
+            if (mode == Popular::Cal)
+                for (size_t i = 0; i < bs; ++i)
+                    for (const Node &v : res[i].vis) popular[v.id] += 1.0f;
+
+            // forward lists (nsw.h:416-429)
+            for (size_t i = 0; i < bs; ++i) {
+                uint32_t *r = row(inserts[floor + i]);
+                r[0] = uint32_t(res[i].prune.size());
+                for (size_t j = 0; j < res[i].prune.size(); ++j) r[1 + j] = res[i].prune[j].id;
+            }
+            // reverse edges (nsw.h:431-444, merge_edges.h:53-81)
+            struct Edge {
+                uint32_t target;
+                Node src;
+            };
+            std::vector<Edge> edges;
+            for (size_t i = 0; i < bs; ++i)
+                for (const Node &e : res[i].prune) edges.push_back(Edge{e.id, Node{inserts[floor + i], e.d}});
+            std::sort(edges.begin(), edges.end(), [](const Edge &a, const Edge &b) {
+                if (a.target != b.target) return a.target < b.target;
+                return node_less(a.src, b.src);
+            });
+            std::vector<size_t> starts;
+            for (size_t i = 0; i < edges.size(); ++i)
+                if (i == 0 || edges[i].target != edges[i - 1].target) starts.push_back(i);
+            starts.push_back(edges.size());
+            // merge per target (nsw.h:463-511, merge_edges.h:98-119)
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+            for (long long g = 0; g < (long long)starts.size() - 1; ++g) {
+                size_t b = starts[g], e = std::min(starts[g + 1], b + size_t(cfg.VL));
+                uint32_t t = edges[b].target;
+                std::vector<Node> cand(cfg.VL + cfg.R);
+                size_t cs = 0;
+                for (size_t j = b; j < e; ++j) cand[cs++] = edges[j].src;
+                size_t pre = cs;
+                uint32_t *r = row(t);
+                for (uint32_t i = 0; i < r[0]; ++i) {
+                    uint32_t nb = r[1 + i];
+                    bool dup = false;
+                    for (size_t j = 0; j < cs; ++j)
+                        if (cand[j].id == nb) { dup = true; break; }
+                    if (dup || cs >= size_t(cfg.VL) + cfg.R) continue;
+                    cand[cs++].id = nb;
+                }
+                stat_dist[t] += uint32_t(fill_new_dists(t, cand.data(), pre, cs));
+                if (cs <= cfg.R) {
+                    std::sort(cand.begin(), cand.begin() + cs, node_less);
+                } else {
+                    dedupe_by_id(cand.data(), cs);
+                    std::sort(cand.begin(), cand.begin() + cs, node_less);
+                    if (cs > cfg.R) cs = cfg.R;
+                }
+                r[0] = uint32_t(cs);
+                for (size_t j = 0; j < cs; ++j) r[1 + j] = cand[j].id;
+            }
+            ++inc;
+        }
+
+        if (mode == Popular::Cal) {
+            // nsw.h:255-278 — one-hop propagation in node order, then log(x+1)
+            std::vector<float> tmp(n, 0.0f);
+            for (uint64_t i = 0; i < n; ++i) {
+                tmp[i] = popular[i];
+                const uint32_t *r = row(uint32_t(i));
+                for (uint32_t j = 0; j < r[0]; ++j) tmp[r[1 + j]] += tmp[i];
+            }
+            for (uint64_t i = 0; i < n; ++i) popular[i] = float(std::log(double(tmp[i] + 1.0f)));
+            auto mm = std::minmax_element(popular.begin(), popular.end());
+            min_pop = *mm.first;
+            max_pop = *mm.second;
+        }
+    }
+};
+
+// dfs.h:46-59
+bool add_edge_if_possible(std::vector<uint32_t> &G, uint32_t R, size_t from, size_t to)
+{
+    uint32_t *r = &G[from * (R + 1)];
+    if (r[0] >= R) return false;
+    for (uint32_t k = 0; k < r[0]; ++k)
+        if (r[1 + k] == to) return true;
+    r[1 + r[0]] = uint32_t(to);
+    r[0] += 1;
+    return true;
+}
+
+// dfs.h:63-137, 193-215, 249-253
+size_t repair_isolated(std::vector<uint32_t> &G, uint32_t R, uint64_t n, uint32_t entry)
+{
+    std::vector<int> flag(n, 0);
+    std::queue<size_t> q;
+    flag[entry] = 1;
+    q.push(entry);
+    while (!q.empty()) {
+        size_t v = q.front();
+        q.pop();
+        const uint32_t *r = &G[v * (R + 1)];
+        for (uint32_t j = 0; j < r[0]; ++j)
+            if (!flag[r[1 + j]]) { flag[r[1 + j]] = 1; q.push(r[1 + j]); }
+    }
+    size_t cnt = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (flag[i]) continue;
+        ++cnt;
+        const uint32_t *r = &G[i * (R + 1)];
+        bool done = false;
+        for (uint32_t j = 0; j < r[0] && !done; ++j)
+            if (flag[r[1 + j]] == 1 && add_edge_if_possible(G, R, r[1 + j], i)) done = true;
+        for (uint32_t j = 0; j < r[0] && !done; ++j)
+            if (add_edge_if_possible(G, R, r[1 + j], i)) done = true;
+        if (!done && flag[entry] == 1 && add_edge_if_possible(G, R, entry, i)) done = true;
+        for (size_t x = 0; x < n && !done; ++x)
+            if (flag[x] == 1 && add_edge_if_possible(G, R, x, i)) done = true;
+    }
+    return cnt;
+}
+
+}  // namespace
+
+extern "C" {
+
+float nbpg_oracle_distance(int dtype, int metric, const void *a, const void *b, uint32_t dims)
+{
+    return dist_rows(dtype, metric, static_cast<const uint8_t *>(a), static_cast<const uint8_t *>(b), dims);
+}
+
+uint64_t nbpg_oracle_hash64_2(uint64_t x) { return splitmix_final(x); }
+
+uint32_t nbpg_oracle_filter_slots(uint32_t L) { return filter_slots(L); }
+
+// Batched greedy search, one query per OpenMP iteration: beamSearch.h:257-303
+// (qsearchAll) with beam_search_rerank's pure-quantized branch (:249-254).
+// Per-query beam width Ls[i] and k ks[i]; max_visited = visited_factor * L (8 in
+// qsearchAll).  Returns 1 (and writes nothing) if any k > L or nsp > L.
+int nbpg_oracle_search(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, const uint32_t *graph,
+                       uint32_t R, const void *queries, uint32_t nq, const uint32_t *Ls, const uint32_t *ks,
+                       double cut, uint64_t limit, uint32_t degree_limit, uint32_t visited_factor, const uint32_t *sp,
+                       uint32_t nsp, uint32_t k_stride, uint32_t *out_ids, float *out_dists, uint32_t *out_count,
+                       uint32_t *out_visited, uint32_t *out_cmps, int threads)
+{
+    for (uint32_t i = 0; i < nq; ++i)
+        if (ks[i] > Ls[i] || nsp > Ls[i] || ks[i] > k_stride || Ls[i] == 0) return 1;
+    for (uint32_t s = 0; s < nsp; ++s)
+        if (sp[s] >= n) return 1;
+    const size_t rb = row_bytes(dtype, dims);
+    const uint8_t *B = static_cast<const uint8_t *>(base);
+    const uint8_t *Q = static_cast<const uint8_t *>(queries);
+    GraphView gv{graph, R};
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel num_threads(threads)
+    {
+        Cell c;
+#pragma omp for schedule(dynamic, 16)
+        for (long long qi = 0; qi < (long long)nq; ++qi) {
+            const uint8_t *q = Q + size_t(qi) * rb;
+            auto dist_to = [&](uint32_t a) { return dist_rows(dtype, metric, B + size_t(a) * rb, q, dims); };
+            c.reset(Ls[qi], visited_factor * Ls[qi], R);
+            seed_frontier(c, sp, nsp, dist_to);
+            size_t cmps = beam_search(c, gv, dist_to, -1, ks[qi], cut, limit, degree_limit);
+            size_t kk = std::min<size_t>(ks[qi], c.fs);
+            for (size_t j = 0; j < k_stride; ++j) {
+                out_ids[size_t(qi) * k_stride + j] = j < kk ? c.frontier[j].id : 0xFFFFFFFFu;
+                out_dists[size_t(qi) * k_stride + j] = j < kk ? c.frontier[j].d : std::numeric_limits<float>::infinity();
+            }
+            if (out_count) out_count[qi] = uint32_t(kk);
+            if (out_visited) out_visited[qi] = uint32_t(c.num_visited);
+            if (out_cmps) out_cmps[qi] = uint32_t(cmps);
+        }
+    }
+    return 0;
+}
+
+// sort_candidates (prune.h:50-74) followed by RobustPrune (prune.h:159-209) on one
+// candidate set of node p.  cand_ids/cand_dists are updated in place; *n is in/out.
+// degrees (per node) is only read when dir_bias_scale > 0.
+int nbpg_oracle_prune(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t p,
+                      uint32_t *cand_ids,
+                      float *cand_dists, uint32_t *cnt, uint32_t R, double alpha, double cos_angle, float dir_bias_scale,
+                      const uint32_t *degrees, uint32_t *out_cmps)
+{
+    const size_t rb = row_bytes(dtype, dims);
+    const uint8_t *B = static_cast<const uint8_t *>(base);
+    std::vector<Node> c(*cnt);
+    for (uint32_t i = 0; i < *cnt; ++i) c[i] = Node{cand_ids[i], cand_dists[i]};
+    std::vector<double> bias;
+    uint32_t maxdeg = 0;
+    if (dir_bias_scale > 0) {
+        for (uint32_t i = 0; i < *cnt; ++i) maxdeg = std::max(maxdeg, degrees[cand_ids[i]]);
+        bias.resize(maxdeg + 1);
+        for (uint32_t d = 0; d <= maxdeg; ++d) bias[d] = dir_bias_scale * std::log(double(d) + 1.0) + 1.0;
+    }
+    size_t m = *cnt;
+    sort_candidates(p, degrees, bias.empty() ? nullptr : bias.data(), c.data(), m);
+    size_t cmps = robust_prune(p, c.data(), m, R, alpha, cos_angle, [&](uint32_t a, uint32_t b) {
+        return dist_rows(dtype, metric, B + size_t(a) * rb, B + size_t(b) * rb, dims);
+    });
+    for (size_t i = 0; i < m; ++i) { cand_ids[i] = c[i].id; cand_dists[i] = c[i].d; }
+    *cnt = uint32_t(m);
+    if (out_cmps) *out_cmps = uint32_t(cmps);
+    return 0;
+}
+
+// build_vamana (nsw.h:547-663) on a graph given as n*(R+1) u32 rows (zeroed, or a
+// prior graph to continue from).  Deterministic: the random merge-pass start
+// points (nsw.h:584-599, randomInt in utilities.h:55-63) draw from
+// std::mt19937(sp_seed) instead of a random_device seed.
+int nbpg_oracle_build(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t R, uint32_t L,
+                      uint32_t VL, uint32_t top_degree, uint32_t num_split, uint32_t num_passes, uint64_t limit,
+                      float dir_bias_scale, double min_alpha, double max_alpha, double min_cos, double max_cos,
+                      int dynamic_prune, int rand_sp, int repair_isolate, uint64_t sp_seed, uint32_t *graph,
+                      uint32_t *out_stat_visited, uint32_t *out_stat_dist, uint64_t *out_isolated, int threads)
+{
+    if (n == 0 || R == 0 || L == 0) return 1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    std::vector<uint32_t> G(graph, graph + size_t(n) * (R + 1));
+    BuildCfg cfg{dtype,
+                 metric,
+                 dims,
+                 static_cast<const uint8_t *>(base),
+                 row_bytes(dtype, dims),
+                 n,
+                 R,
+                 L,
+                 VL,
+                 top_degree,
+                 num_split,
+                 num_passes,
+                 limit == 0 ? n : limit,
+                 dir_bias_scale,
+                 float(min_alpha),
+                 float(max_alpha),
+                 float(min_cos),
+                 float(max_cos)};
+    Builder b(cfg, G);
+    std::vector<uint32_t> inserts(n);
+    std::iota(inserts.begin(), inserts.end(), 0u);
+    Popular mode = Popular::FixedMax;
+    std::mt19937 sp_engine{uint32_t(sp_seed)};
+
+    if (num_split >= 1) {
+        auto fill = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+            for (size_t j = 0; j < hi - lo; ++j) sp[j].push_back(inserts[lo + j] % num_split);
+        };
+        for (int i = 0; i < 2; ++i) {
+            std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
+            b.batch_insert(inserts, fill, mode, threads);
+        }
+    }
+    auto fill_merge = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+        for (size_t j = 0; j < hi - lo; ++j)
+            for (uint32_t s = 0; s < num_split; ++s) {
+                std::uniform_int_distribution<uint32_t> u(0, uint32_t(n) - 1);
+                uint32_t rid = u(sp_engine) / num_split * num_split;
+                uint32_t v = rid + s;
+                if (v >= n) v -= num_split;
+                sp[j].push_back(v);
+            }
+    };
+    auto fill_rand = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+        for (size_t j = 0; j < hi - lo; ++j) sp[j].push_back(uint32_t(inserts.size() - inserts[lo + j] - 1));
+    };
+    auto fill_default = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+        for (size_t j = 0; j < hi - lo; ++j) sp[j].push_back(0);
+    };
+    for (int i = 0; i < int(num_passes); ++i) {
+        std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
+        if (i == int(num_passes) - 2 && dynamic_prune) mode = Popular::Cal;
+        else if (i == int(num_passes) - 1) mode = (dynamic_prune && num_passes > 1) ? Popular::Prune : Popular::FixedMin;
+        if (i != int(num_passes) - 1) {
+            if (num_split > 1) b.batch_insert(inserts, fill_merge, mode, threads);
+            else b.batch_insert(inserts, fill_default, mode, threads);
+        } else {
+            if (rand_sp) b.batch_insert(inserts, fill_rand, mode, threads);
+            else b.batch_insert(inserts, fill_default, mode, threads);
+        }
+    }
+    size_t iso = 0;
+    if (repair_isolate) iso = repair_isolated(G, R, n, 0);
+    std::copy(G.begin(), G.end(), graph);
+    if (out_stat_visited) std::copy(b.stat_visited.begin(), b.stat_visited.end(), out_stat_visited);
+    if (out_stat_dist) std::copy(b.stat_dist.begin(), b.stat_dist.end(), out_stat_dist);
+    if (out_isolated) *out_isolated = iso;
+    return 0;
+}
+
+// Brute-force kNN: CompGT.cpp:29-134.  exact == 0 replays CompGT's replace-max
+// rule, including its stale read of topk[0] (CompGT.cpp:80-95); exact != 0 keeps
+// the true (dist, id) top-k.  Output rows sorted by (dist, id).  Requires n >= k.
+int nbpg_oracle_gt(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, const void *queries,
+                   uint32_t nq, uint32_t k, int exact, uint32_t *out_ids, float *out_dists, int threads)
+{
+    if (k == 0 || n < k) return 1;
+    const size_t rb = row_bytes(dtype, dims);
+    const uint8_t *B = static_cast<const uint8_t *>(base);
+    const uint8_t *Q = static_cast<const uint8_t *>(queries);
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (long long j = 0; j < (long long)nq; ++j) {
+        const uint8_t *q = Q + size_t(j) * rb;
+        std::vector<Node> top;
+        top.reserve(k);
+        if (!exact) {
+            uint32_t toppos = 0;
+            float topdist = -std::numeric_limits<float>::max();
+            for (uint64_t i = 0; i < n; ++i) {
+                float d = dist_rows(dtype, metric, B + size_t(i) * rb, q, dims);
+                if (top.size() < k) {
+                    if (d > topdist) { topdist = d; toppos = uint32_t(top.size()); }
+                    top.push_back(Node{uint32_t(i), d});
+                } else if (d < topdist) {
+                    float nt = top[0].d;  // read before the overwrite below
+                    uint32_t np = 0;
+                    top[toppos] = Node{uint32_t(i), d};
+                    for (uint32_t l = 1; l < top.size(); ++l)
+                        if (top[l].d > nt) { nt = top[l].d; np = l; }
+                    topdist = nt;
+                    toppos = np;
+                }
+            }
+        } else {
+            // max-heap on (dist, id)
+            for (uint64_t i = 0; i < n; ++i) {
+                Node v{uint32_t(i), dist_rows(dtype, metric, B + size_t(i) * rb, q, dims)};
+                if (top.size() < k) {
+                    top.push_back(v);
+                    std::push_heap(top.begin(), top.end(), node_less);
+                } else if (node_less(v, top.front())) {
+                    std::pop_heap(top.begin(), top.end(), node_less);
+                    top.back() = v;
+                    std::push_heap(top.begin(), top.end(), node_less);
+                }
+            }
+        }
+        std::sort(top.begin(), top.end(), node_less);
+        for (uint32_t l = 0; l < k; ++l) {
+            out_ids[size_t(j) * k + l] = top[l].id;
+            out_dists[size_t(j) * k + l] = top[l].d;
+        }
+    }
+    return 0;
+}
+
+}  // extern "C"

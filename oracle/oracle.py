@@ -1,0 +1,190 @@
+"""ctypes front end for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``_build/libnbpg_oracle.so`` (the C++ restatement of the reference's
+algorithms) and, where it was built, ``_ref/libnbpg_ref.so`` (a harness compiled
+from the reference's own headers).  Both export the same C ABI with the prefixes
+``nbpg_oracle_`` and ``nbpg_ref_``.  Only tests, ``__graft_entry__.smoke`` and the
+CPU-baseline leg of ``bench.py`` use this module, always as the checker or the
+timed CPU baseline; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libnbpg_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libnbpg_ref.so")
+REF_COMPGT = os.path.join(HERE, "_ref", "CompGT")
+REF_VAMANA = os.path.join(HERE, "_ref", "Vamana")
+
+DTYPES = {"u8": 0, "i8": 1, "u4": 2, "i4": 3, "f32": 4}
+METRICS = {"l2": 0, "ip": 1}
+
+_u8p = C.c_void_p
+_u32p = C.POINTER(C.c_uint32)
+_f32p = C.POINTER(C.c_float)
+_u64p = C.POINTER(C.c_uint64)
+
+
+def build(ref_root: str | None = None) -> None:
+    """Compile the oracle (and the reference harness when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    ref_root = ref_root or "/root/reference"
+    if os.path.isdir(ref_root):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class CpuLib:
+    """One of the two CPU libraries (oracle restatement or reference harness)."""
+
+    def __init__(self, path: str, prefix: str):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        self.prefix = prefix
+        f = self._f
+        f("distance").restype = C.c_float
+        f("distance").argtypes = [C.c_int, C.c_int, _u8p, _u8p, C.c_uint32]
+        f("hash64_2").restype = C.c_uint64
+        f("hash64_2").argtypes = [C.c_uint64]
+        f("filter_slots").restype = C.c_uint32
+        f("filter_slots").argtypes = [C.c_uint32]
+        f("search").restype = C.c_int
+        f("search").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, _u32p, C.c_uint32, _u8p, C.c_uint32,
+                                _u32p, _u32p, C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, _u32p, C.c_uint32,
+                                C.c_uint32, _u32p, _f32p, _u32p, _u32p, _u32p, C.c_int]
+        f("prune").restype = C.c_int
+        f("build").restype = C.c_int
+        f("build").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                               C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.c_double, C.c_double,
+                               C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint64, _u32p, _u32p, _u32p,
+                               _u64p, C.c_int]
+        if hasattr(self.lib, prefix + "gt"):
+            f("gt").restype = C.c_int
+            f("gt").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, _u8p, C.c_uint32, C.c_uint32, C.c_int,
+                                _u32p, _f32p, C.c_int]
+
+    def _f(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    # -- primitives -------------------------------------------------------------
+    def distance(self, dtype: str, metric: str, a: np.ndarray, b: np.ndarray) -> float:
+        a = np.ascontiguousarray(a)
+        b = np.ascontiguousarray(b)
+        dims = a.shape[-1]
+        return float(self._f("distance")(DTYPES[dtype], METRICS[metric], a.ctypes.data, b.ctypes.data, dims))
+
+    def hash64_2(self, x: int) -> int:
+        return int(self._f("hash64_2")(x))
+
+    def filter_slots(self, L: int) -> int:
+        return int(self._f("filter_slots")(L))
+
+    # -- search -----------------------------------------------------------------
+    def search(self, dtype, metric, base, graph, queries, L, k, cut=1.35, limit=None, degree_limit=None,
+               visited_factor=8, start_points=(0,), threads=0):
+        """Strict greedy search; returns (ids, dists, count, visited, cmps)."""
+        base = np.ascontiguousarray(base)
+        queries = np.ascontiguousarray(queries)
+        graph = np.ascontiguousarray(graph, dtype=np.uint32)
+        n, dims = base.shape
+        R = graph.shape[1] - 1
+        nq = queries.shape[0]
+        Ls = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.uint32), (nq,)))
+        ks = np.ascontiguousarray(np.broadcast_to(np.asarray(k, dtype=np.uint32), (nq,)))
+        kst = max(1, int(ks.max()) if nq else 1)
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        ids = np.empty((nq, kst), np.uint32)
+        dists = np.empty((nq, kst), np.float32)
+        cnt = np.empty(nq, np.uint32)
+        vis = np.empty(nq, np.uint32)
+        cmps = np.empty(nq, np.uint32)
+        rc = self._f("search")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, _p(graph, _u32p), R,
+                               queries.ctypes.data, nq, _p(Ls, _u32p), _p(ks, _u32p), cut,
+                               n if limit is None else limit, R if degree_limit is None else degree_limit,
+                               visited_factor, _p(sp, _u32p), len(sp), kst, _p(ids, _u32p), _p(dists, _f32p),
+                               _p(cnt, _u32p), _p(vis, _u32p), _p(cmps, _u32p), threads)
+        if rc != 0:
+            raise ValueError(f"{self.prefix}search rejected its arguments (status {rc})")
+        return ids, dists, cnt, vis, cmps
+
+    # -- prune ------------------------------------------------------------------
+    def prune(self, dtype, metric, base, p, cand_ids, cand_dists, R, alpha, cos_angle=0.0, dir_bias_scale=0.0,
+              degrees=None):
+        base = np.ascontiguousarray(base)
+        n, dims = base.shape
+        ids = np.ascontiguousarray(cand_ids, dtype=np.uint32).copy()
+        ds = np.ascontiguousarray(cand_dists, dtype=np.float32).copy()
+        cnt = C.c_uint32(len(ids))
+        cmps = C.c_uint32(0)
+        deg = None if degrees is None else np.ascontiguousarray(degrees, dtype=np.uint32)
+        rc = self._f("prune")(C.c_int(DTYPES[dtype]), C.c_int(METRICS[metric]), C.c_uint32(dims),
+                              C.c_void_p(base.ctypes.data), C.c_uint64(n), C.c_uint32(p), _p(ids, _u32p),
+                              _p(ds, _f32p), C.byref(cnt), C.c_uint32(R), C.c_double(alpha), C.c_double(cos_angle),
+                              C.c_float(dir_bias_scale), _p(deg, _u32p), C.byref(cmps))
+        if rc != 0:
+            raise ValueError("prune failed")
+        m = cnt.value
+        return ids[:m], ds[:m], cmps.value
+
+    # -- build ------------------------------------------------------------------
+    def build_graph(self, dtype, metric, base, R, L, VL=140, top_degree=0, num_split=4, num_passes=2, limit=0,
+                    dir_bias_scale=0.0, min_alpha=1.0, max_alpha=1.1, min_cos=0.0, max_cos=0.0,
+                    dynamic_prune=False, rand_sp=False, repair_isolate=True, sp_seed=0, graph=None, threads=0):
+        base = np.ascontiguousarray(base)
+        n, dims = base.shape
+        g = np.zeros((n, R + 1), np.uint32) if graph is None else np.ascontiguousarray(graph, np.uint32).copy()
+        sv = np.zeros(n, np.uint32)
+        sd = np.zeros(n, np.uint32)
+        iso = np.zeros(1, np.uint64)
+        rc = self._f("build")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, R, L, VL, top_degree,
+                              num_split, num_passes, limit, dir_bias_scale, min_alpha, max_alpha, min_cos, max_cos,
+                              int(dynamic_prune), int(rand_sp), int(repair_isolate), sp_seed, _p(g, _u32p),
+                              _p(sv, _u32p), _p(sd, _u32p), _p(iso, _u64p), threads)
+        if rc != 0:
+            raise ValueError("build failed")
+        return g, sv, sd, int(iso[0])
+
+    # -- ground truth -----------------------------------------------------------
+    def gt(self, dtype, metric, base, queries, k=100, exact=False, threads=0):
+        base = np.ascontiguousarray(base)
+        queries = np.ascontiguousarray(queries)
+        n = base.shape[0]
+        dims = base.shape[1]
+        nq = queries.shape[0]
+        ids = np.empty((nq, k), np.uint32)
+        ds = np.empty((nq, k), np.float32)
+        rc = self._f("gt")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, queries.ctypes.data, nq, k,
+                           int(exact), _p(ids, _u32p), _p(ds, _f32p), threads)
+        if rc != 0:
+            raise ValueError("gt rejected its arguments")
+        return ids, ds
+
+
+_oracle = None
+_ref = None
+
+
+def oracle() -> CpuLib:
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        _oracle = CpuLib(ORACLE_SO, "nbpg_oracle_")
+    return _oracle
+
+
+def reference() -> CpuLib | None:
+    """The harness over the reference headers, or None where it was not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_SO):
+        _ref = CpuLib(REF_SO, "nbpg_ref_")
+    return _ref

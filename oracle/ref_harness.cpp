@@ -1,0 +1,253 @@
+// Harness over the reference's own headers (godpgf/NBPG), compiled in place from
+// the reference source tree by oracle/Makefile into oracle/_ref/libnbpg_ref.so.
+//
+// TEST INFRASTRUCTURE ONLY.  It exists to pin the CPU oracle (nbpg_oracle.cpp)
+// and to generate golden vectors; it is never shipped and never runs on a machine
+// without the reference sources.  Every exported function calls the reference's
+// templates directly and mirrors the signature of the matching nbpg_oracle_* call.
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <iostream>
+#include <limits>
+#include <random>
+#include <vector>
+#include <omp.h>
+
+#include "utils/Point/point.h"
+#include "utils/Point/point_range.h"
+#include "utils/Graph/graph.h"
+#include "utils/Graph/query_params.h"
+#include "utils/Graph/beamSearch.h"
+#include "utils/Graph/prune.h"
+#include "nsw.h"
+
+using namespace ant;
+
+namespace {
+
+template <typename T>
+PointRange<Point<T>> make_points(const void *rows, uint64_t n, uint32_t dims, int metric)
+{
+    using PR = PointRange<Point<T>>;
+    PR pr(n, typename PR::Parameters(dims, metric ? DistanceMetric::MIPS : DistanceMetric::EUCLIDEAN));
+    const size_t nb = size_t(dims) * sizeof(T);
+    for (uint64_t i = 0; i < n; ++i)
+        std::memcpy(pr[i].data(), static_cast<const uint8_t *>(rows) + i * nb, nb);
+    return pr;
+}
+
+Graph<uint32_t> make_graph(const uint32_t *rows, uint64_t n, uint32_t R)
+{
+    Graph<uint32_t> G(R, n);
+    for (uint64_t i = 0; i < n; ++i) std::memcpy(G[i].data(), rows + i * (R + 1), (R + 1) * sizeof(uint32_t));
+    return G;
+}
+
+template <typename T>
+int search_t(uint32_t dims, int metric, const void *base, uint64_t n, const uint32_t *graph, uint32_t R,
+             const void *queries, uint32_t nq, const uint32_t *Ls, const uint32_t *ks, double cut, uint64_t limit,
+             uint32_t degree_limit, uint32_t visited_factor, const uint32_t *sp, uint32_t nsp, uint32_t k_stride,
+             uint32_t *out_ids, float *out_dists, uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    auto Q = make_points<T>(queries, nq, dims, metric);
+    auto G = make_graph(graph, n, R);
+    QueryStatic stats(nq);
+    std::vector<uint32_t> spv(sp, sp + nsp);
+    // qsearchAll body (beamSearch.h:275-300), one table per query so that L may vary.
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long i = 0; i < (long long)nq; ++i) {
+        QueryParams QP(ks[i], Ls[i], cut, limit, degree_limit);
+        BeamSearchMemoryTable<uint32_t> table(1, 1, QP.beamSize, size_t(QP.beamSize) * visited_factor, G.max_degree());
+        auto cell = table.getCell(0, 0, QP.beamSize, size_t(QP.beamSize) * visited_factor);
+        cell.init_starting_points(Q[i], B, spv.data(), nsp);
+        auto res = beam_search_rerank(cell, Q[i], Q[i], G, B, B, stats, QP, uint32_t(i));
+        for (uint32_t j = 0; j < k_stride; ++j) {
+            out_ids[size_t(i) * k_stride + j] = j < res.size() ? res[j].first : 0xFFFFFFFFu;
+            out_dists[size_t(i) * k_stride + j] = j < res.size() ? res[j].second : std::numeric_limits<float>::infinity();
+        }
+        if (out_count) out_count[i] = uint32_t(res.size());
+    }
+    for (uint32_t i = 0; i < nq; ++i) {
+        if (out_visited) out_visited[i] = stats.visited[i];
+        if (out_cmps) out_cmps[i] = stats.distances[i];
+    }
+    return 0;
+}
+
+template <typename T>
+int prune_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t p, uint32_t *ids, float *dists,
+            uint32_t *cnt, uint32_t R, double alpha, double cos_angle, float dir_bias_scale, const uint32_t *degrees,
+            uint32_t *out_cmps)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    uint32_t maxdeg = 1;
+    if (degrees)
+        for (uint64_t i = 0; i < n; ++i) maxdeg = std::max(maxdeg, degrees[i]);
+    Graph<uint32_t> G(maxdeg, n);
+    if (degrees)
+        for (uint64_t i = 0; i < n; ++i) G[i].data()[0] = degrees[i];
+    std::vector<QueryNode<uint32_t>> c(*cnt);
+    for (uint32_t i = 0; i < *cnt; ++i) c[i] = QueryNode<uint32_t>(ids[i], dists[i]);
+    Prune pr(R, 1);
+    size_t m = *cnt;
+    pr.sort_candidates(p, G, c.data(), m, dir_bias_scale);
+    size_t cmps = pr.robustPrune(p, c.data(), m, B, alpha, cos_angle, 1);
+    for (size_t i = 0; i < m; ++i) { ids[i] = c[i].index; dists[i] = c[i].dist; }
+    *cnt = uint32_t(m);
+    if (out_cmps) *out_cmps = uint32_t(cmps);
+    return 0;
+}
+
+template <typename T>
+int build_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t R, uint32_t L, uint32_t VL,
+            uint32_t top_degree, uint32_t num_split, uint32_t num_passes, uint64_t limit, float dir_bias_scale,
+            double min_alpha, double max_alpha, double min_cos, double max_cos, int dynamic_prune, int rand_sp,
+            int repair_isolate, uint64_t sp_seed, uint32_t *graph, uint32_t *out_sv, uint32_t *out_sd,
+            uint64_t *out_iso)
+{
+    using PR = PointRange<Point<T>>;
+    auto QP = make_points<T>(base, n, dims, metric);
+    auto G = make_graph(graph, n, R);
+    QueryStatic stats(n);
+    if (limit == 0) limit = n;
+    size_t iso = 0;
+    if (num_split <= 1) {
+        // Deterministic in the reference: call build_vamana itself (nsw.h:547-663).
+        iso = build_vamana<PR, uint32_t>(QP, G, L, VL, top_degree, num_split, num_passes, limit, dir_bias_scale,
+                                         min_alpha, max_alpha, min_cos, max_cos, dynamic_prune, rand_sp,
+                                         repair_isolate, stats);
+    } else {
+        // build_vamana's pass loop with the merge-pass start points drawn from a seeded
+        // engine (the reference seeds it from std::random_device, nsw.h:584-599).
+        using NSWType = NSWIndex<uint32_t>;
+        using Fill = NSWType::FillStartFun;
+        auto prune = Prune(G.max_degree(), omp_get_max_threads());
+        auto nsw = NSWType(prune, L, VL, omp_get_max_threads(), G.max_degree(), NSWType::getMaxBatchSize(G),
+                           top_degree, min_alpha, max_alpha, min_cos, max_cos);
+        std::vector<uint32_t> inserts(QP.size());
+        std::iota(inserts.begin(), inserts.end(), 0);
+        NodePopular mode = NodePopular::FixedMaxPopular;
+        std::mt19937 engine{uint32_t(sp_seed)};
+        Fill fill_sp = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+            for (uint32_t j = 0; j < hi - lo; ++j) sp[j].push_back(inserts[lo + j] % num_split);
+        };
+        for (int i = 0; i < 2; ++i) {
+            std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
+            nsw.batch_insert(inserts.data(), inserts.size(), G, QP, L, limit, &stats, fill_sp, mode, dir_bias_scale,
+                             2, .02, false);
+        }
+        Fill fill_merge = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+            for (uint32_t j = 0; j < hi - lo; ++j)
+                for (uint32_t s = 0; s < num_split; ++s) {
+                    std::uniform_int_distribution<uint32_t> u(0, uint32_t(G.size()) - 1);
+                    uint32_t rid = u(engine) / num_split * num_split;
+                    uint32_t v = rid + s;
+                    if (v >= G.size()) v -= num_split;
+                    sp[j].push_back(v);
+                }
+        };
+        Fill fill_rand = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+            for (uint32_t j = 0; j < hi - lo; ++j) sp[j].push_back(uint32_t(inserts.size() - inserts[lo + j] - 1));
+        };
+        Fill fill_default = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+            for (uint32_t j = 0; j < hi - lo; ++j) sp[j].push_back(0);
+        };
+        for (int i = 0; i < int(num_passes); ++i) {
+            std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
+            if (i == int(num_passes) - 2 && dynamic_prune) mode = NodePopular::CalPopular;
+            else if (i == int(num_passes) - 1)
+                mode = (dynamic_prune && num_passes > 1) ? NodePopular::PopularPrune : NodePopular::FixedMinPopular;
+            Fill f = (i != int(num_passes) - 1) ? fill_merge : (rand_sp ? fill_rand : fill_default);
+            nsw.batch_insert(inserts.data(), inserts.size(), G, QP, L, limit, &stats, f, mode, dir_bias_scale, 2, .02,
+                             false);
+        }
+        if (repair_isolate) iso = DFS::repair_isolate_node(G, static_cast<uint32_t>(0));
+    }
+    for (uint64_t i = 0; i < n; ++i) std::memcpy(graph + i * (R + 1), G[i].data(), (R + 1) * sizeof(uint32_t));
+    if (out_sv) std::memcpy(out_sv, stats.visited.data(), n * sizeof(uint32_t));
+    if (out_sd) std::memcpy(out_sd, stats.distances.data(), n * sizeof(uint32_t));
+    if (out_iso) *out_iso = iso;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+float nbpg_ref_distance(int dtype, int metric, const void *a, const void *b, uint32_t dims)
+{
+    auto *x = const_cast<uint8_t *>(static_cast<const uint8_t *>(a));
+    auto *y = const_cast<uint8_t *>(static_cast<const uint8_t *>(b));
+    auto dm = metric ? DistanceMetric::MIPS : DistanceMetric::EUCLIDEAN;
+    switch (dtype) {
+    case 0: return Point<uint8_t>(x, Point<uint8_t>::Parameters(dims, dm)).distance(Point<uint8_t>(y, Point<uint8_t>::Parameters(dims, dm)));
+    case 1: return Point<int8_t>(x, Point<int8_t>::Parameters(dims, dm)).distance(Point<int8_t>(y, Point<int8_t>::Parameters(dims, dm)));
+    case 2: return Point<uint4_2>(x, Point<uint4_2>::Parameters(dims, dm)).distance(Point<uint4_2>(y, Point<uint4_2>::Parameters(dims, dm)));
+    case 3: return Point<int4_2>(x, Point<int4_2>::Parameters(dims, dm)).distance(Point<int4_2>(y, Point<int4_2>::Parameters(dims, dm)));
+    default: return Point<float>(x, Point<float>::Parameters(dims, dm)).distance(Point<float>(y, Point<float>::Parameters(dims, dm)));
+    }
+}
+
+uint64_t nbpg_ref_hash64_2(uint64_t x) { return hash64_2(x); }
+
+uint32_t nbpg_ref_filter_slots(uint32_t L) { return uint32_t(BeamSearchMemoryCell<uint32_t>::get_max_hash_filter_size(L)); }
+
+int nbpg_ref_search(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, const uint32_t *graph,
+                    uint32_t R, const void *queries, uint32_t nq, const uint32_t *Ls, const uint32_t *ks, double cut,
+                    uint64_t limit, uint32_t degree_limit, uint32_t visited_factor, const uint32_t *sp, uint32_t nsp,
+                    uint32_t k_stride, uint32_t *out_ids, float *out_dists, uint32_t *out_count,
+                    uint32_t *out_visited, uint32_t *out_cmps, int threads)
+{
+    if (threads > 0) omp_set_num_threads(threads);
+    for (uint32_t i = 0; i < nq; ++i)
+        if (ks[i] > Ls[i] || nsp > Ls[i] || ks[i] > k_stride) return 1;
+#define NBPG_REF_SEARCH(T)                                                                                              \
+    return search_t<T>(dims, metric, base, n, graph, R, queries, nq, Ls, ks, cut, limit, degree_limit, visited_factor, \
+                       sp, nsp, k_stride, out_ids, out_dists, out_count, out_visited, out_cmps)
+    switch (dtype) {
+    case 0: NBPG_REF_SEARCH(uint8_t);
+    case 1: NBPG_REF_SEARCH(int8_t);
+    case 2: NBPG_REF_SEARCH(uint4_2);
+    case 3: NBPG_REF_SEARCH(int4_2);
+    default: return 1;
+    }
+#undef NBPG_REF_SEARCH
+}
+
+int nbpg_ref_prune(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t p, uint32_t *ids,
+                   float *dists, uint32_t *cnt, uint32_t R, double alpha, double cos_angle, float dir_bias_scale,
+                   const uint32_t *degrees, uint32_t *out_cmps)
+{
+    switch (dtype) {
+    case 0: return prune_t<uint8_t>(dims, metric, base, n, p, ids, dists, cnt, R, alpha, cos_angle, dir_bias_scale, degrees, out_cmps);
+    case 1: return prune_t<int8_t>(dims, metric, base, n, p, ids, dists, cnt, R, alpha, cos_angle, dir_bias_scale, degrees, out_cmps);
+    case 2: return prune_t<uint4_2>(dims, metric, base, n, p, ids, dists, cnt, R, alpha, cos_angle, dir_bias_scale, degrees, out_cmps);
+    case 3: return prune_t<int4_2>(dims, metric, base, n, p, ids, dists, cnt, R, alpha, cos_angle, dir_bias_scale, degrees, out_cmps);
+    default: return 1;
+    }
+}
+
+int nbpg_ref_build(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t R, uint32_t L,
+                   uint32_t VL, uint32_t top_degree, uint32_t num_split, uint32_t num_passes, uint64_t limit,
+                   float dir_bias_scale, double min_alpha, double max_alpha, double min_cos, double max_cos,
+                   int dynamic_prune, int rand_sp, int repair_isolate, uint64_t sp_seed, uint32_t *graph,
+                   uint32_t *out_sv, uint32_t *out_sd, uint64_t *out_iso, int threads)
+{
+    if (threads > 0) omp_set_num_threads(threads);
+#define NBPG_REF_BUILD(T)                                                                                             \
+    return build_t<T>(dims, metric, base, n, R, L, VL, top_degree, num_split, num_passes, limit, dir_bias_scale,    \
+                      min_alpha, max_alpha, min_cos, max_cos, dynamic_prune, rand_sp, repair_isolate, sp_seed, graph, \
+                      out_sv, out_sd, out_iso)
+    switch (dtype) {
+    case 0: NBPG_REF_BUILD(uint8_t);
+    case 1: NBPG_REF_BUILD(int8_t);
+    case 2: NBPG_REF_BUILD(uint4_2);
+    case 3: NBPG_REF_BUILD(int4_2);
+    default: return 1;
+    }
+#undef NBPG_REF_BUILD
+}
+
+}  // extern "C"
