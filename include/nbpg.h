@@ -1,0 +1,173 @@
+/*
+ * nbpg.h — C ABI of the GB300-native NBPG hot path (libnbpg_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every call returns an nbpg_status; nothing aborts
+ * (the reference abort()s on k > L, sp > L and out-of-range ids:
+ * algorithms/utils/Graph/beamSearch.h:268-273, algorithms/nsw.h:128-132,
+ * algorithms/utils/Graph/query_params.h:185-189, algorithms/utils/Graph/graph.h:381-391).
+ *
+ * Data model (identical to the reference's files and in-memory layouts):
+ *   vectors  n rows of `dims` elements; dims counts bytes for the packed 4-bit
+ *            types (two codes per byte), as in the .u4bin/.i4bin header.
+ *   graph    n rows of (R+1) u32: [degree, neighbour ids...]
+ *            (algorithms/utils/Graph/graph.h:18-116).
+ *
+ * Threading: calls on one index handle are serialised by the caller (one CUDA
+ * stream per handle); distinct handles are independent.
+ */
+#ifndef NBPG_H
+#define NBPG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nbpg_status {
+    NBPG_OK = 0,
+    NBPG_ERR_INVALID_ARG = 1, /* k > L, start points > L, bad sizes/ids/dtype */
+    NBPG_ERR_OOM = 2,         /* device allocation failed */
+    NBPG_ERR_CUDA = 3,        /* a CUDA call failed; see nbpg_last_error() */
+    NBPG_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    NBPG_ERR_FORMAT = 5,      /* malformed graph or vector data */
+    NBPG_ERR_UNSUPPORTED = 6  /* valid request outside what this build supports */
+} nbpg_status;
+
+/* Element types: Point<uint8_t>, Point<int8_t>, Point<uint4_2>, Point<int4_2>,
+ * Point<float> (algorithms/utils/Point/point.h:10-18, 159-330). */
+typedef enum nbpg_dtype { NBPG_U8 = 0, NBPG_I8 = 1, NBPG_U4 = 2, NBPG_I4 = 3, NBPG_F32 = 4 } nbpg_dtype;
+
+/* DistanceMetric::EUCLIDEAN (squared L2) / MIPS (negative dot), point.h:20-24. */
+typedef enum nbpg_metric { NBPG_L2 = 0, NBPG_IP = 1 } nbpg_metric;
+
+/* Search kernels.  STRICT reproduces the reference's expansion order, visited
+ * filter and merge rules bit for bit. */
+typedef enum nbpg_kernel {
+    NBPG_KERNEL_BATCHED = 0, /* persistent CTAs pulling queries from a device queue */
+    NBPG_KERNEL_PLAIN = 1    /* one query per thread block */
+} nbpg_kernel;
+
+/* Human-readable text of the last error on this thread ("" if none). */
+const char *nbpg_last_error(void);
+
+/* Library version string. */
+const char *nbpg_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Index: device-resident base vectors + adjacency graph.
+ * Replaces PointRange<Point<T>> + Graph<uint32_t> as held by the Vamana driver
+ * (data_tools/ANNs/Vamana.cpp:149-195, 234-251).
+ * ------------------------------------------------------------------------- */
+typedef struct nbpg_index nbpg_index;
+
+typedef struct nbpg_index_desc {
+    uint32_t dtype;      /* nbpg_dtype (F32 is rejected: graph paths are quantised) */
+    uint32_t metric;     /* nbpg_metric */
+    uint32_t dims;       /* elements per row as in the file header */
+    uint32_t max_degree; /* R */
+    uint64_t n;          /* number of base vectors / graph nodes */
+    int32_t device;      /* CUDA device ordinal */
+} nbpg_index_desc;
+
+nbpg_status nbpg_index_create(const nbpg_index_desc *desc, nbpg_index **out);
+nbpg_status nbpg_index_destroy(nbpg_index *idx);
+
+/* Copy `count` host rows (dims elements each, packed) into rows [first, first+count). */
+nbpg_status nbpg_index_set_points(nbpg_index *idx, const void *rows, uint64_t first, uint64_t count);
+
+/* Copy `count` graph rows of (R+1) u32 (degree first) into nodes [first, first+count).
+ * Rejects degree > R or neighbour ids >= n with NBPG_ERR_FORMAT.
+ * Replaces Graph(const char*) loading (graph.h:169-221). */
+nbpg_status nbpg_index_set_graph(nbpg_index *idx, const uint32_t *rows, uint64_t first, uint64_t count);
+
+/* Copy graph rows back to the host (for Graph::save, graph.h:339-379). */
+nbpg_status nbpg_index_get_graph(const nbpg_index *idx, uint32_t *rows, uint64_t first, uint64_t count);
+
+/* ---------------------------------------------------------------------------
+ * Search.  Replaces qsearchAll (algorithms/utils/Graph/beamSearch.h:257-303) with
+ * beam_search_rerank's pure-quantised branch (:183-255) and filtered_beam_search
+ * (:43-171).  QueryParams fields (query_params.h:12-42) map 1:1.
+ * ------------------------------------------------------------------------- */
+typedef struct nbpg_search_params {
+    uint32_t k;              /* QueryParams::k — results per query, 0 < k <= L */
+    uint32_t L;              /* QueryParams::beamSize */
+    double cut;              /* QueryParams::cut (1.35 in check_nn_recall.h:213) */
+    uint64_t limit;          /* QueryParams::limit, max expansions; 0 = n */
+    uint32_t degree_limit;   /* QueryParams::degree_limit; 0 = R */
+    uint32_t visited_factor; /* visited list cap = factor * L; 0 = 8 (beamSearch.h:276-280) */
+    uint32_t kernel;         /* nbpg_kernel */
+    uint32_t warps_per_cta;  /* batched kernel CTA size in warps; 0 = autotuned */
+} nbpg_search_params;
+
+/* Per-query outputs, k_stride entries per query row: ids (UINT32_MAX padding),
+ * dists (+inf padding), number of results, nodes expanded and distance
+ * computations (QueryStatic, query_params.h:47-94).  Any output pointer except
+ * out_ids may be NULL.  Ls/ks give per-query beam width and k (NULL = params).
+ * start_points: entry nodes (the reference's get_sp; {0} in check_nn_recall.h:282-297),
+ * distinct, at most min L.
+ *
+ * nbpg_search: host buffers; copies in and out on the index stream and returns when done.
+ * nbpg_search_device: device buffers (start_points stays a host array); enqueued on
+ *   `stream` (a cudaStream_t, NULL = the index stream); returns after enqueueing. */
+nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *params,
+                        const uint32_t *Ls, const uint32_t *ks, const uint32_t *start_points, uint32_t n_start,
+                        uint32_t k_stride, uint32_t *out_ids, float *out_dists, uint32_t *out_count,
+                        uint32_t *out_visited, uint32_t *out_cmps);
+nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t nq, const nbpg_search_params *params,
+                               const uint32_t *d_Ls, const uint32_t *d_ks, const uint32_t *start_points,
+                               uint32_t n_start, uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
+                               uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps, void *stream);
+
+/* Device pointer of the index's packed base rows (row stride = nbpg_index_row_stride
+ * bytes) and of its graph rows (nbpg_index_graph_stride u32 per node). */
+nbpg_status nbpg_index_device_info(const nbpg_index *idx, void **d_points, uint32_t *row_stride,
+                                   uint32_t **d_graph, uint32_t *graph_stride);
+
+/* ---------------------------------------------------------------------------
+ * Brute-force kNN.  Replaces compute_groundtruth (data_tools/ANNs/data_proc/CompGT.cpp:29-134).
+ * mode COMPGT replays CompGT's replace-max rule, stale read included
+ * (CompGT.cpp:80-95), bit-exactly; mode EXACT returns the true (dist, id) top-k.
+ * Rows of k ids/dists sorted by (dist, id).  Requires n >= k.
+ * ------------------------------------------------------------------------- */
+typedef enum nbpg_gt_mode { NBPG_GT_COMPGT = 0, NBPG_GT_EXACT = 1 } nbpg_gt_mode;
+
+nbpg_status nbpg_gt(uint32_t dtype, uint32_t metric, uint32_t dims, const void *base, uint64_t n,
+                    const void *queries, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *out_ids,
+                    float *out_dists, int32_t device);
+
+/* ---------------------------------------------------------------------------
+ * Build.  Replaces build_vamana (algorithms/nsw.h:547-663) with NSWIndex::batch_insert
+ * (nsw.h:110-286), RobustPrune (algorithms/utils/Graph/prune.h:159-209), reverse-edge
+ * merging (merge_edges.h:23-148, nsw.h:463-511), popularity-driven alpha
+ * (nsw.h:297-324) and isolated-node repair (dfs.h:193-254).  Flags of the Vamana
+ * driver (Vamana.cpp:14-85) map 1:1.  Runs on the index's points and its current
+ * graph (zeroed on create, or a --pre_index_path graph set with nbpg_index_set_graph).
+ * The reference draws merge-pass start points from a random_device-seeded engine
+ * (algorithms/utils/utilities.h:55-63); here they come from std::mt19937(sp_seed).
+ * ------------------------------------------------------------------------- */
+typedef struct nbpg_build_params {
+    uint32_t L, VL, top_degree, num_split, num_passes;
+    uint64_t limit;       /* 0 = n */
+    float dir_bias_scale;
+    double min_alpha, max_alpha, min_cos_angle, max_cos_angle;
+    int32_t dynamic_prune, rand_sp, repair_isolate;
+    uint64_t sp_seed;
+} nbpg_build_params;
+
+typedef struct nbpg_build_stats {
+    uint64_t isolated;      /* nodes unreachable from node 0 before repair */
+    double seconds;         /* wall time of the build */
+    uint64_t batches;       /* batches run over all passes */
+} nbpg_build_stats;
+
+/* per_node_visited / per_node_dists (n entries each, may be NULL): BuildStats
+ * (QueryStatic) counters as accumulated by the reference (nsw.h:143-147,173-174). */
+nbpg_status nbpg_build(nbpg_index *idx, const nbpg_build_params *params, nbpg_build_stats *stats,
+                       uint32_t *per_node_visited, uint32_t *per_node_dists);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NBPG_H */

@@ -1,0 +1,82 @@
+// Host-side internals shared by the CUDA translation units of libnbpg_gb300.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/nbpg.h"
+
+namespace nbpg {
+
+void set_error(const std::string &msg);
+
+// Status helpers: every CUDA failure becomes NBPG_ERR_CUDA with its text recorded.
+#define NBPG_CUDA_TRY(expr)                                                                                 \
+    do {                                                                                                    \
+        cudaError_t _e = (expr);                                                                            \
+        if (_e != cudaSuccess) {                                                                            \
+            ::nbpg::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));                          \
+            return _e == cudaErrorMemoryAllocation ? NBPG_ERR_OOM : NBPG_ERR_CUDA;                          \
+        }                                                                                                   \
+    } while (0)
+
+#define NBPG_CHECK_ARG(cond, msg)                                                                           \
+    do {                                                                                                    \
+        if (!(cond)) {                                                                                      \
+            ::nbpg::set_error(msg);                                                                         \
+            return NBPG_ERR_INVALID_ARG;                                                                    \
+        }                                                                                                   \
+    } while (0)
+
+inline uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
+
+// Growable device scratch buffer owned by an index.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    nbpg_status ensure(size_t need)
+    {
+        if (need <= bytes) return NBPG_OK;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t b = need + need / 4 + 256;
+        cudaError_t e = cudaMalloc(&ptr, b);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaMalloc scratch: ") + cudaGetErrorString(e));
+            ptr = nullptr;
+            return NBPG_ERR_OOM;
+        }
+        bytes = b;
+        return NBPG_OK;
+    }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const { return static_cast<T *>(ptr); }
+};
+
+}  // namespace nbpg
+
+struct nbpg_index {
+    nbpg_index_desc desc{};
+    uint32_t row_bytes = 0;   // packed bytes per vector
+    uint32_t row_stride = 0;  // device row pitch, multiple of 16 (zero padded)
+    uint32_t gstride = 0;     // u32 per graph row on device: round_up(R+1, 4)
+    uint8_t *d_points = nullptr;
+    uint32_t *d_graph = nullptr;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    // scratch
+    nbpg::DevBuf queue, taint, sp, ghash, gvis, qbuf, obuf;
+    std::vector<uint32_t> sp_host;  // start points currently in `sp`
+    std::mutex mu;
+};

@@ -1,0 +1,289 @@
+// Host driver of the strict search: argument checks, shared-memory layout,
+// scratch, and the FLAG pass followed by the LIST re-run of tainted queries.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "search_ops.h"
+
+namespace nbpg {
+
+static const SearchOps *ops_for(uint32_t dtype)
+{
+    switch (dtype) {
+    case NBPG_U8: return &search_ops_u8;
+    case NBPG_I8: return &search_ops_i8;
+    case NBPG_U4:
+    case NBPG_I4: return &search_ops_u4;  // identical arithmetic: i4 codes lose their sign (point.h:27-32)
+    default: return nullptr;
+    }
+}
+
+SlotLayout make_slot_layout(uint32_t Lmax, uint32_t R, bool vis_smem, uint32_t Vcap, bool hash_smem, uint32_t Scap)
+{
+    SlotLayout l{};
+    l.Lcap = round_up(std::max<uint32_t>(Lmax, 1), 32);
+    l.Ccap = round_up(l.Lcap / 8 + R + 1, 32);
+    l.Rcap = round_up(std::max<uint32_t>(R, 1), 32);
+    l.Vcap = vis_smem ? round_up(Vcap, 32) : 0;
+    l.Scap = hash_smem ? Scap : 0;
+    uint32_t off = 0;
+    l.off_fr0 = off; off += l.Lcap * 8;
+    l.off_fr1 = off; off += l.Lcap * 8;
+    l.off_cand = off; off += l.Ccap * 8;
+    l.off_vis = off; off += l.Vcap * 8;
+    l.off_hash = off; off += l.Scap * 4;
+    l.off_filt = off; off += l.Rcap * 4;
+    l.off_unv = off; off += l.Lcap * 2;
+    l.off_fl0 = off; off += l.Lcap;
+    l.off_fl1 = off; off += l.Lcap;
+    l.bytes = round_up(off, 16);
+    return l;
+}
+
+// Thresholds for keeping per-query tables in shared memory.
+static constexpr uint32_t kHashSmemMax = 32768;  // bytes of visited filter per warp slot
+static constexpr uint32_t kVisSmemMax = 16384;   // bytes of visited list per warp slot
+
+struct PassCfg {
+    SlotLayout lay;
+    uint32_t warps = 1, grid = 1;
+    size_t smem = 0;
+    bool ghash = false, gvis = false;
+    uint32_t S = 0, Vcap = 0;
+};
+
+static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, bool list, bool plain, uint32_t Lmax,
+                             uint32_t vf, uint32_t want_warps, PassCfg &pc)
+{
+    const uint32_t R = idx->desc.max_degree;
+    pc.S = filter_slots_for(Lmax);
+    pc.Vcap = round_up(vf * Lmax, 32);
+    pc.ghash = !plain && pc.S * 4 > kHashSmemMax;
+    pc.gvis = list && !plain && pc.Vcap * 8 > kVisSmemMax;
+    pc.lay = make_slot_layout(Lmax, R, list && !pc.gvis, pc.Vcap, !pc.ghash, pc.S);
+    if (pc.lay.bytes > idx->smem_optin) {
+        set_error("per-query working set exceeds shared memory for this L");
+        return NBPG_ERR_UNSUPPORTED;
+    }
+    if (plain) {
+        pc.warps = 1;
+        pc.smem = pc.lay.bytes;
+        NBPG_CUDA_TRY(ops->set_attr(metric, list, true, pc.smem));
+        return NBPG_OK;
+    }
+    uint32_t fit = uint32_t(idx->smem_optin / pc.lay.bytes);
+    uint32_t w = want_warps ? want_warps : std::min<uint32_t>(16, fit);
+    w = std::max<uint32_t>(1, std::min<uint32_t>(w, std::min<uint32_t>(16, fit)));
+    pc.warps = w;
+    pc.smem = size_t(w) * pc.lay.bytes;
+    NBPG_CUDA_TRY(ops->set_attr(metric, list, false, pc.smem));
+    int blocks = 0;
+    NBPG_CUDA_TRY(ops->occ(metric, list, false, w * 32, pc.smem, &blocks));
+    if (blocks < 1) {
+        set_error("search kernel does not fit on an SM");
+        return NBPG_ERR_UNSUPPORTED;
+    }
+    pc.grid = uint32_t(blocks) * uint32_t(idx->sm_count);
+    return NBPG_OK;
+}
+
+nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t nq, const nbpg_search_params *P,
+                               const uint32_t *d_Ls, const uint32_t *d_ks, const uint32_t *sp, uint32_t nsp,
+                               uint32_t k_stride, uint32_t *d_ids, float *d_dists, uint32_t *d_count,
+                               uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st)
+{
+    NBPG_CHECK_ARG(idx && P && d_ids, "null argument");
+    NBPG_CHECK_ARG(idx->d_points && idx->d_graph, "index has no points/graph");
+    if (nq == 0) return NBPG_OK;
+    const uint32_t R = idx->desc.max_degree;
+    const uint64_t n = idx->desc.n;
+    NBPG_CHECK_ARG(P->L >= 1 && P->L <= 1024, "L must be in [1, 1024]");
+    NBPG_CHECK_ARG(P->k >= 1 && P->k <= P->L, "k must be in [1, L] (the reference aborts on k > L)");
+    NBPG_CHECK_ARG(k_stride >= P->k, "k_stride < k");
+    NBPG_CHECK_ARG(sp && nsp >= 1 && nsp <= P->L && nsp <= 256, "need 1..min(L,256) start points");
+    NBPG_CHECK_ARG(R <= 128, "max_degree above 128 is not supported");
+    NBPG_CHECK_ARG(P->kernel == NBPG_KERNEL_BATCHED || P->kernel == NBPG_KERNEL_PLAIN, "unknown kernel");
+    {
+        std::vector<uint32_t> s(sp, sp + nsp);
+        for (uint32_t v : s) NBPG_CHECK_ARG(v < n, "start point out of range");
+        std::sort(s.begin(), s.end());
+        NBPG_CHECK_ARG(std::adjacent_find(s.begin(), s.end()) == s.end(), "start points must be distinct");
+    }
+    const SearchOps *ops = ops_for(idx->desc.dtype);
+    NBPG_CHECK_ARG(ops, "unsupported dtype");
+    if (!st) st = idx->stream;
+
+    const int metric = int(idx->desc.metric);
+    const bool plain = P->kernel == NBPG_KERNEL_PLAIN;
+    const uint32_t vf = P->visited_factor ? P->visited_factor : 8;
+    // inner product: the cut rule routinely keeps <= k entries, so go straight to LIST
+    const bool flag_first = metric == M_L2;
+
+    PassCfg main{}, rerun{};
+    nbpg_status s = plan_pass(idx, ops, metric, !flag_first, plain, P->L, vf, P->warps_per_cta, main);
+    if (s != NBPG_OK) return s;
+    if (flag_first) {
+        s = plan_pass(idx, ops, metric, true, false, P->L, vf, 0, rerun);
+        if (s != NBPG_OK) return s;
+    }
+
+    // scratch: [0] queue main, [1] queue rerun, [2] error word; taint list; start points
+    if ((s = idx->queue.ensure(4 * sizeof(uint32_t))) != NBPG_OK) return s;
+    if ((s = idx->taint.ensure((size_t(nq) + 1) * sizeof(uint32_t))) != NBPG_OK) return s;
+    if ((s = idx->sp.ensure(256 * sizeof(uint32_t))) != NBPG_OK) return s;
+    size_t nslots = std::max<size_t>(main.ghash || main.gvis ? size_t(main.grid) * main.warps : 0,
+                                     rerun.ghash || rerun.gvis ? size_t(rerun.grid) * rerun.warps : 0);
+    uint32_t hslots = std::max(main.ghash ? main.S : 0u, rerun.ghash ? rerun.S : 0u);
+    uint32_t vcap = std::max(main.gvis ? main.Vcap : 0u, rerun.gvis ? rerun.Vcap : 0u);
+    if (hslots && (s = idx->ghash.ensure(nslots * hslots * sizeof(uint32_t))) != NBPG_OK) return s;
+    if (vcap && (s = idx->gvis.ensure(nslots * vcap * sizeof(uint64_t))) != NBPG_OK) return s;
+
+    uint32_t *q = idx->queue.as<uint32_t>();
+    NBPG_CUDA_TRY(cudaMemsetAsync(q, 0, 4 * sizeof(uint32_t), st));
+    NBPG_CUDA_TRY(cudaMemsetAsync(idx->taint.ptr, 0, sizeof(uint32_t), st));
+    if (idx->sp_host.size() != nsp || !std::equal(sp, sp + nsp, idx->sp_host.begin())) {
+        NBPG_CUDA_TRY(cudaMemcpyAsync(idx->sp.ptr, sp, nsp * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+        idx->sp_host.assign(sp, sp + nsp);
+    }
+
+    SearchArgs a{};
+    a.base = idx->d_points;
+    a.row_stride = idx->row_stride;
+    a.vecs = idx->row_stride / 16;
+    a.lpr = 1;
+    while (a.lpr < a.vecs && a.lpr < 32) a.lpr <<= 1;
+    a.vpl = (a.vecs + a.lpr - 1) / a.lpr;
+    NBPG_CHECK_ARG(a.vpl <= 2, "rows above 1024 bytes are not supported");
+    a.graph = idx->d_graph;
+    a.gstride = idx->gstride;
+    a.R = R;
+    a.n = n;
+    a.queries = static_cast<const uint8_t *>(d_queries);
+    a.nq = nq;
+    a.Ls = d_Ls;
+    a.ks = d_ks;
+    a.L_all = P->L;
+    a.k_all = P->k;
+    a.cut = P->cut;
+    a.limit = P->limit ? P->limit : n;
+    a.degree_limit = P->degree_limit ? std::min(P->degree_limit, R) : R;
+    a.visited_factor = vf;
+    a.sp = idx->sp.as<uint32_t>();
+    a.nsp = nsp;
+    a.k_stride = k_stride;
+    a.out_ids = d_ids;
+    a.out_dists = d_dists;
+    a.out_count = d_count;
+    a.out_visited = d_visited;
+    a.out_cmps = d_cmps;
+    a.err = q + 2;
+    a.prefetch = plain ? 0 : 2;
+
+    // main pass
+    SearchArgs m = a;
+    m.queue = q;
+    m.taint = flag_first ? idx->taint.as<uint32_t>() : nullptr;
+    m.lay = main.lay;
+    m.g_hash = main.ghash ? idx->ghash.as<uint32_t>() : nullptr;
+    m.g_hash_slots = main.ghash ? hslots : 0;
+    m.g_vis = main.gvis ? idx->gvis.as<uint64_t>() : nullptr;
+    m.g_vis_cap = main.gvis ? vcap : 0;
+    ops->launch(metric, !flag_first, plain, plain ? nq : main.grid, main.warps, main.smem, m, st);
+    NBPG_CUDA_TRY(cudaGetLastError());
+
+    if (flag_first) {
+        SearchArgs r = a;
+        r.queue = q + 1;
+        r.only = idx->taint.as<uint32_t>();
+        r.lay = rerun.lay;
+        r.g_hash = rerun.ghash ? idx->ghash.as<uint32_t>() : nullptr;
+        r.g_hash_slots = rerun.ghash ? hslots : 0;
+        r.g_vis = rerun.gvis ? idx->gvis.as<uint64_t>() : nullptr;
+        r.g_vis_cap = rerun.gvis ? vcap : 0;
+        r.prefetch = 0;
+        ops->launch(metric, true, false, rerun.grid, rerun.warps, rerun.smem, r, st);
+        NBPG_CUDA_TRY(cudaGetLastError());
+    }
+    return NBPG_OK;
+}
+
+}  // namespace nbpg
+
+using namespace nbpg;
+
+extern "C" nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                          const nbpg_search_params *params, const uint32_t *d_Ls,
+                                          const uint32_t *d_ks, const uint32_t *start_points, uint32_t n_start,
+                                          uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
+                                          uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps,
+                                          void *stream)
+{
+    if (!idx) { set_error("null index"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(idx->mu);
+    cudaSetDevice(idx->desc.device);
+    return search_device_impl(idx, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride, d_out_ids,
+                              d_out_dists, d_out_count, d_out_visited, d_out_cmps, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *P,
+                                   const uint32_t *Ls, const uint32_t *ks, const uint32_t *start_points,
+                                   uint32_t n_start, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
+                                   uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps)
+{
+    if (!idx || !P || !queries || !out_ids) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(idx->mu);
+    cudaSetDevice(idx->desc.device);
+    if (nq == 0) return NBPG_OK;
+    nbpg_search_params p = *P;
+    if (Ls || ks) {
+        uint32_t Lmax = 0;
+        for (uint32_t i = 0; i < nq; ++i) {
+            uint32_t L = Ls ? Ls[i] : P->L, k = ks ? ks[i] : P->k;
+            NBPG_CHECK_ARG(L >= 1 && k >= 1 && k <= L, "per-query k must be in [1, L] (the reference aborts on k > L)");
+            NBPG_CHECK_ARG(k <= k_stride, "per-query k above k_stride");
+            NBPG_CHECK_ARG(n_start <= L, "more start points than a query's L");
+            Lmax = std::max(Lmax, L);
+        }
+        p.L = Lmax;
+        p.k = 1;
+    }
+    cudaStream_t st = idx->stream;
+    const size_t qbytes = size_t(nq) * idx->row_stride;
+    const size_t per_q = size_t(k_stride) * 8 + 5 * 4;
+    nbpg_status s;
+    if ((s = idx->qbuf.ensure(qbytes)) != NBPG_OK) return s;
+    if ((s = idx->obuf.ensure(size_t(nq) * per_q + 64)) != NBPG_OK) return s;
+    uint8_t *dq = idx->qbuf.as<uint8_t>();
+    NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, qbytes, st));
+    NBPG_CUDA_TRY(cudaMemcpy2DAsync(dq, idx->row_stride, queries, idx->row_bytes, idx->row_bytes, nq,
+                                    cudaMemcpyHostToDevice, st));
+    uint8_t *o = idx->obuf.as<uint8_t>();
+    uint32_t *d_ids = reinterpret_cast<uint32_t *>(o);
+    float *d_d = reinterpret_cast<float *>(o + size_t(nq) * k_stride * 4);
+    uint32_t *d_c = reinterpret_cast<uint32_t *>(o + size_t(nq) * k_stride * 8);
+    uint32_t *d_v = d_c + nq, *d_m = d_v + nq, *d_L = d_m + nq, *d_k = d_L + nq;
+    if (Ls) NBPG_CUDA_TRY(cudaMemcpyAsync(d_L, Ls, nq * 4, cudaMemcpyHostToDevice, st));
+    else if (ks) { std::vector<uint32_t> t(nq, P->L); NBPG_CUDA_TRY(cudaMemcpyAsync(d_L, t.data(), nq * 4, cudaMemcpyHostToDevice, st)); NBPG_CUDA_TRY(cudaStreamSynchronize(st)); }
+    if (ks) NBPG_CUDA_TRY(cudaMemcpyAsync(d_k, ks, nq * 4, cudaMemcpyHostToDevice, st));
+    else if (Ls) { std::vector<uint32_t> t(nq, P->k); NBPG_CUDA_TRY(cudaMemcpyAsync(d_k, t.data(), nq * 4, cudaMemcpyHostToDevice, st)); NBPG_CUDA_TRY(cudaStreamSynchronize(st)); }
+    const bool per = Ls || ks;
+    s = search_device_impl(idx, dq, nq, &p, per ? d_L : nullptr, per ? d_k : nullptr, start_points, n_start, k_stride,
+                           d_ids, d_d, d_c, d_v, d_m, st);
+    if (s != NBPG_OK) return s;
+    uint32_t err = 0;
+    NBPG_CUDA_TRY(cudaMemcpyAsync(out_ids, d_ids, size_t(nq) * k_stride * 4, cudaMemcpyDeviceToHost, st));
+    if (out_dists) NBPG_CUDA_TRY(cudaMemcpyAsync(out_dists, d_d, size_t(nq) * k_stride * 4, cudaMemcpyDeviceToHost, st));
+    if (out_count) NBPG_CUDA_TRY(cudaMemcpyAsync(out_count, d_c, nq * 4, cudaMemcpyDeviceToHost, st));
+    if (out_visited) NBPG_CUDA_TRY(cudaMemcpyAsync(out_visited, d_v, nq * 4, cudaMemcpyDeviceToHost, st));
+    if (out_cmps) NBPG_CUDA_TRY(cudaMemcpyAsync(out_cmps, d_m, nq * 4, cudaMemcpyDeviceToHost, st));
+    NBPG_CUDA_TRY(cudaMemcpyAsync(&err, idx->queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+    NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err) {
+        set_error("a query was rejected on the device (k > L or L above the planned maximum)");
+        return NBPG_ERR_INVALID_ARG;
+    }
+    return NBPG_OK;
+}

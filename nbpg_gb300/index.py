@@ -1,0 +1,161 @@
+"""Host-side mirror of the reference's search/build interface over the C ABI.
+
+``QueryParams`` mirrors ant::QueryParams (algorithms/utils/Graph/query_params.h:12-42);
+``Index.qsearch_all`` mirrors qsearchAll (algorithms/utils/Graph/beamSearch.h:257-303):
+queries in, per-query neighbour ids out, k > L rejected (the reference aborts).
+``Index.build_vamana`` mirrors build_vamana (algorithms/nsw.h:547-663) with the
+flags of the Vamana driver (data_tools/ANNs/Vamana.cpp:14-85).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import BuildParams, BuildStats, IndexDesc, SearchParams, check
+
+_u32p = C.POINTER(C.c_uint32)
+_f32p = C.POINTER(C.c_float)
+
+
+def _p(a, t=_u32p):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+@dataclass
+class QueryParams:
+    """ant::QueryParams: k, beam width (beamSize), cut, limit, degree_limit."""
+    k: int = 10
+    beamSize: int = 10
+    cut: float = 1.35
+    limit: int = 0          # 0 = number of base vectors
+    degree_limit: int = 0   # 0 = max degree
+    visited_factor: int = 8  # visited-list cap = factor * beamSize (qsearchAll uses 8)
+
+
+@dataclass
+class SearchResult:
+    ids: np.ndarray      # (nq, k) u32, UINT32_MAX padding
+    dists: np.ndarray    # (nq, k) f32, +inf padding
+    count: np.ndarray    # (nq,) results per query
+    visited: np.ndarray  # (nq,) nodes expanded (QueryStatic::visited)
+    cmps: np.ndarray     # (nq,) distance computations (QueryStatic::distances)
+
+
+class Index:
+    """Device-resident base vectors + graph (one GPU)."""
+
+    def __init__(self, points: np.ndarray, dtype: str, metric: str = "l2", max_degree: int = 64,
+                 graph: np.ndarray | None = None, device: int = 0):
+        points = np.ascontiguousarray(points)
+        if points.ndim != 2:
+            raise ValueError("points must be (n, dims)")
+        self.n, self.dims = points.shape
+        self.dtype, self.metric, self.R = dtype, metric, int(max_degree)
+        desc = IndexDesc(_lib.DTYPES[dtype], _lib.METRICS[metric], self.dims, self.R, self.n, device)
+        h = C.c_void_p()
+        L = _lib.lib()
+        check(L.nbpg_index_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        check(L.nbpg_index_set_points(self._h, points.ctypes.data, 0, self.n))
+        if graph is not None:
+            self.set_graph(graph)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().nbpg_index_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_graph(self, graph: np.ndarray) -> None:
+        g = np.ascontiguousarray(graph, dtype=np.uint32)
+        if g.shape != (self.n, self.R + 1):
+            raise ValueError(f"graph must be ({self.n}, {self.R + 1})")
+        check(_lib.lib().nbpg_index_set_graph(self._h, _p(g), 0, self.n))
+
+    def get_graph(self) -> np.ndarray:
+        g = np.empty((self.n, self.R + 1), np.uint32)
+        check(_lib.lib().nbpg_index_get_graph(self._h, _p(g), 0, self.n))
+        return g
+
+    def device_info(self):
+        pts, rs, g, gs = C.c_void_p(), C.c_uint32(), C.c_void_p(), C.c_uint32()
+        check(_lib.lib().nbpg_index_device_info(self._h, C.byref(pts), C.byref(rs), C.byref(g), C.byref(gs)))
+        return pts.value, rs.value, g.value, gs.value
+
+    # -- search ----------------------------------------------------------------
+    def search(self, queries: np.ndarray, qp: QueryParams, start_points=(0,), kernel: str = "batched",
+               Ls=None, ks=None, warps_per_cta: int = 0) -> SearchResult:
+        """Strict search of host queries; results identical to the reference's."""
+        q = np.ascontiguousarray(queries)
+        if q.ndim != 2 or q.shape[1] != self.dims:
+            raise ValueError("queries must be (nq, dims)")
+        nq = q.shape[0]
+        Ls = None if Ls is None else np.ascontiguousarray(Ls, dtype=np.uint32)
+        ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.uint32)
+        kst = int(ks.max()) if ks is not None and nq else int(qp.k)
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        prm = SearchParams(int(qp.k), int(qp.beamSize), float(qp.cut), int(qp.limit), int(qp.degree_limit),
+                           int(qp.visited_factor), _lib.KERNELS[kernel], int(warps_per_cta))
+        ids = np.empty((nq, kst), np.uint32)
+        ds = np.empty((nq, kst), np.float32)
+        cnt = np.empty(nq, np.uint32)
+        vis = np.empty(nq, np.uint32)
+        cmps = np.empty(nq, np.uint32)
+        check(_lib.lib().nbpg_search(self._h, q.ctypes.data, nq, C.byref(prm), _p(Ls), _p(ks), _p(sp), len(sp), kst,
+                                     _p(ids), _p(ds, _f32p), _p(cnt), _p(vis), _p(cmps)))
+        return SearchResult(ids, ds, cnt, vis, cmps)
+
+    def qsearch_all(self, queries: np.ndarray, qp: QueryParams, start_points=(0,)) -> list[np.ndarray]:
+        """qsearchAll: list of neighbour-id arrays, one per query."""
+        r = self.search(queries, qp, start_points)
+        return [r.ids[i, :r.count[i]] for i in range(len(r.count))]
+
+    def search_device(self, d_queries: int, nq: int, qp: QueryParams, d_out_ids: int, k_stride: int,
+                      d_out_dists: int | None = None, d_count: int | None = None, d_visited: int | None = None,
+                      d_cmps: int | None = None, start_points=(0,), kernel: str = "batched", stream: int = 0,
+                      d_Ls: int | None = None, d_ks: int | None = None, warps_per_cta: int = 0) -> None:
+        """Enqueue a search on device buffers (raw pointers; rows of the index's device row stride)."""
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        prm = SearchParams(int(qp.k), int(qp.beamSize), float(qp.cut), int(qp.limit), int(qp.degree_limit),
+                           int(qp.visited_factor), _lib.KERNELS[kernel], int(warps_per_cta))
+        check(_lib.lib().nbpg_search_device(self._h, d_queries, nq, C.byref(prm), d_Ls, d_ks, _p(sp), len(sp),
+                                            k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
+
+    # -- build -----------------------------------------------------------------
+    def build_vamana(self, L: int = 70, VL: int = 140, top_degree: int = 0, num_split: int = 4, num_passes: int = 2,
+                     limit: int = 0, dir_bias_scale: float = 0.0, min_alpha: float = 1.0, max_alpha: float = 1.1,
+                     min_cos_angle: float = 0.0, max_cos_angle: float = 0.0, dynamic_prune: bool = False,
+                     rand_sp: bool = False, repair_isolate: bool = True, sp_seed: int = 0, with_stats: bool = False):
+        prm = BuildParams(L, VL, top_degree, num_split, num_passes, limit, dir_bias_scale, min_alpha, max_alpha,
+                          min_cos_angle, max_cos_angle, int(dynamic_prune), int(rand_sp), int(repair_isolate),
+                          sp_seed)
+        st = BuildStats()
+        sv = np.zeros(self.n, np.uint32) if with_stats else None
+        sd = np.zeros(self.n, np.uint32) if with_stats else None
+        check(_lib.lib().nbpg_build(self._h, C.byref(prm), C.byref(st), _p(sv), _p(sd)))
+        return st, sv, sd
+
+
+def ground_truth(base: np.ndarray, queries: np.ndarray, dtype: str, metric: str = "l2", k: int = 100,
+                 exact: bool = False, device: int = 0):
+    """compute_groundtruth (CompGT.cpp:29-134) on the GPU: (ids, dists), rows sorted by (dist, id)."""
+    base = np.ascontiguousarray(base)
+    queries = np.ascontiguousarray(queries)
+    nq = queries.shape[0]
+    ids = np.empty((nq, k), np.uint32)
+    ds = np.empty((nq, k), np.float32)
+    check(_lib.lib().nbpg_gt(_lib.DTYPES[dtype], _lib.METRICS[metric], base.shape[1], base.ctypes.data, base.shape[0],
+                             queries.ctypes.data, nq, k, int(exact), _p(ids), _p(ds, _f32p), device))
+    return ids, ds

@@ -1,0 +1,97 @@
+"""Strict search on the GPU, through the C ABI, against the CPU oracle: ids, integer
+distances, result counts, expansions and distance-computation counts must be identical."""
+import numpy as np
+import pytest
+
+from conftest import dataset
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_index(base, g, dtype, metric):
+    from nbpg_gb300.index import Index
+    return Index(base, dtype, metric, max_degree=g.shape[1] - 1, graph=g)
+
+
+def _check(r, o, nq):
+    ids, dists, cnt, vis, cmps = o
+    kst = ids.shape[1]
+    assert np.array_equal(r.count, cnt)
+    assert np.array_equal(r.ids[:, :kst], ids)
+    assert np.array_equal(r.dists[:, :kst], dists)
+    assert np.array_equal(r.visited, vis)
+    assert np.array_equal(r.cmps, cmps)
+
+
+CASES = [("u8", "l2", 32), ("u8", "ip", 32), ("i8", "l2", 24), ("i8", "ip", 24), ("u4", "l2", 16),
+         ("u4", "ip", 16), ("i4", "l2", 16), ("u8", "l2", 100)]
+
+
+@pytest.mark.parametrize("dtype,metric,dims", CASES)
+@pytest.mark.parametrize("kernel", ["batched", "plain"])
+def test_search_matches_oracle(gpu_lib, oracle_lib, dtype, metric, dims, kernel):
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset(dtype, metric, dims=dims)
+    idx = _gpu_index(base, g, dtype, metric)
+    for L, k in [(1, 1), (10, 10), (16, 5), (50, 10), (100, 100)]:
+        r = idx.search(q, QueryParams(k=k, beamSize=L, cut=1.35), kernel=kernel)
+        o = oracle_lib.search(dtype, metric, base, g, q, L=L, k=k, cut=1.35)
+        _check(r, o, len(q))
+
+
+@pytest.mark.parametrize("L", [182, 256])
+def test_search_global_visited_filter(gpu_lib, oracle_lib, L):
+    """L >= 182 puts the 16384-slot visited filter in global scratch."""
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2", n=4000, R=32, L=48)
+    idx = _gpu_index(base, g, "u8", "l2")
+    r = idx.search(q, QueryParams(k=10, beamSize=L))
+    _check(r, oracle_lib.search("u8", "l2", base, g, q, L=L, k=10), len(q))
+
+
+def test_search_uneven_L_k(gpu_lib, oracle_lib):
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2")
+    rng = np.random.default_rng(3)
+    Ls = rng.choice([32, 64, 128, 256], size=len(q)).astype(np.uint32)
+    ks = np.minimum(rng.choice([1, 10, 100], size=len(q)), Ls).astype(np.uint32)
+    idx = _gpu_index(base, g, "u8", "l2")
+    r = idx.search(q, QueryParams(k=10, beamSize=256), Ls=Ls, ks=ks)
+    _check(r, oracle_lib.search("u8", "l2", base, g, q, L=Ls, k=ks), len(q))
+
+
+def test_search_multiple_start_points_and_limits(gpu_lib, oracle_lib):
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2")
+    idx = _gpu_index(base, g, "u8", "l2")
+    sp = (7, 0, 1234)
+    for limit, dl in [(0, 0), (15, 0), (40, 8)]:
+        r = idx.search(q, QueryParams(k=10, beamSize=40, limit=limit, degree_limit=dl), start_points=sp)
+        o = oracle_lib.search("u8", "l2", base, g, q, L=40, k=10, limit=limit or None, degree_limit=dl or None,
+                              start_points=sp)
+        _check(r, o, len(q))
+
+
+def test_search_rejects_k_above_L(gpu_lib):
+    from nbpg_gb300._lib import NbpgError
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2")
+    idx = _gpu_index(base, g, "u8", "l2")
+    with pytest.raises(NbpgError) as e:
+        idx.search(q, QueryParams(k=20, beamSize=10))
+    assert e.value.status == 1
+    with pytest.raises(NbpgError):
+        idx.search(q, QueryParams(k=10, beamSize=32), Ls=np.full(len(q), 8, np.uint32))
+
+
+def test_search_isolated_start_and_empty_rows(gpu_lib, oracle_lib):
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2")
+    g = g.copy()
+    g[0, 0] = 0            # start point with no neighbours
+    g[5:200, 0] = 0        # ragged: many empty rows
+    idx = _gpu_index(base, g, "u8", "l2")
+    r = idx.search(q, QueryParams(k=10, beamSize=20))
+    _check(r, oracle_lib.search("u8", "l2", base, g, q, L=20, k=10), len(q))
+    r = idx.search(q, QueryParams(k=10, beamSize=20), start_points=(3,))
+    _check(r, oracle_lib.search("u8", "l2", base, g, q, L=20, k=10, start_points=(3,)), len(q))
