@@ -166,4 +166,13 @@ __device__ __forceinline__ float finish_dist(uint32_t acc)
     else return -__int2float_rn(r);
 }
 
+// Keys fold -0 onto +0; the reference's inner-product distance of an orthogonal
+// pair is -0.0f (-static_cast<float>(0), point.h:53), so restore that sign on output.
+template <int MET>
+__device__ __forceinline__ float output_dist(float d)
+{
+    if constexpr (MET == M_IP) return d == 0.0f ? -0.0f : d;
+    else return d;
+}
+
 }  // namespace nbpg

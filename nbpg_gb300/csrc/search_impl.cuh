@@ -437,7 +437,7 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
         if (j < kk) {
             const uint64_t key = fr[b][j];
             a.out_ids[o] = key_id(key);
-            if (a.out_dists) a.out_dists[o] = key_dist(key);
+            if (a.out_dists) a.out_dists[o] = output_dist<MET>(key_dist(key));
         } else {
             a.out_ids[o] = kNoId;
             if (a.out_dists) a.out_dists[o] = __int_as_float(0x7f800000);

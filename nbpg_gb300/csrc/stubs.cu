@@ -1,12 +1,6 @@
 // Entry points whose kernels are not in this build yet.
 #include "internal.h"
 using namespace nbpg;
-extern "C" nbpg_status nbpg_gt(uint32_t, uint32_t, uint32_t, const void *, uint64_t, const void *, uint32_t, uint32_t,
-                               uint32_t, uint32_t *, float *, int32_t)
-{
-    set_error("nbpg_gt: not built");
-    return NBPG_ERR_UNSUPPORTED;
-}
 extern "C" nbpg_status nbpg_build(nbpg_index *, const nbpg_build_params *, nbpg_build_stats *, uint32_t *, uint32_t *)
 {
     set_error("nbpg_build: not built");

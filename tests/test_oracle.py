@@ -1,0 +1,53 @@
+"""The CPU oracle against the reference: harness over the reference headers (where it
+was built) and golden vectors generated from the reference binaries."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import dataset
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_distance_known_answers(oracle_lib):
+    a = np.array([0, 255, 17, 200], np.uint8)
+    b = np.array([255, 0, 17, 100], np.uint8)
+    assert oracle_lib.distance("u8", "l2", a, b) == 255 ** 2 * 2 + 100 ** 2
+    assert oracle_lib.distance("u8", "ip", a, b) == -(17 * 17 + 200 * 100)
+    ai, bi = a.view(np.int8), b.view(np.int8)  # [0,-1,17,-56] . [-1,0,17,100]
+    assert oracle_lib.distance("i8", "l2", ai, bi) == 1 + 1 + 0 + 156 ** 2
+    assert oracle_lib.distance("i8", "ip", ai, bi) == -(0 + 0 + 289 - 5600)
+    # 4-bit codes: each nibble scaled by 16; the signed type loses its sign
+    x = np.array([0xF0, 0x0F], np.uint8)
+    y = np.array([0x00, 0x00], np.uint8)
+    assert oracle_lib.distance("u4", "l2", x, y) == 2 * 240 ** 2
+    assert oracle_lib.distance("i4", "l2", x, y) == 2 * 240 ** 2
+    assert oracle_lib.distance("i4", "ip", x, x) == -(2 * 240 * 240)
+    # orthogonal inner product is -0.0 in the reference
+    z = oracle_lib.distance("u8", "ip", np.zeros(4, np.uint8), a)
+    assert z == 0 and np.signbit(z)
+
+
+def test_filter_slots(oracle_lib):
+    expect = {1: 1024, 45: 1024, 64: 1024, 65: 2048, 90: 2048, 91: 4096, 128: 4096, 129: 8192, 181: 8192,
+              182: 16384, 256: 16384}
+    for L, s in expect.items():
+        assert oracle_lib.filter_slots(L) == s
+
+
+def test_oracle_matches_reference_harness(oracle_lib, ref_lib):
+    base, q, g = dataset("u8", "l2")
+    for L, k in [(10, 10), (50, 10), (100, 100)]:
+        for metric in ("l2", "ip"):
+            o = oracle_lib.search("u8", metric, base, g, q, L=L, k=k)
+            r = ref_lib.search("u8", metric, base, g, q, L=L, k=k)
+            for x, y in zip(o, r):
+                assert np.array_equal(x, y)
+    for split, passes, dyn in [(0, 1, False), (4, 2, True)]:
+        go = oracle_lib.build_graph("u8", "l2", base[:1500], R=16, L=24, VL=30, num_split=split, num_passes=passes,
+                                    dynamic_prune=dyn, max_alpha=1.2, min_alpha=1.05, sp_seed=3)
+        gr = ref_lib.build_graph("u8", "l2", base[:1500], R=16, L=24, VL=30, num_split=split, num_passes=passes,
+                                 dynamic_prune=dyn, max_alpha=1.2, min_alpha=1.05, sp_seed=3)
+        assert np.array_equal(go[0], gr[0]) and np.array_equal(go[1], gr[1]) and np.array_equal(go[2], gr[2])
+        assert go[3] == gr[3]
