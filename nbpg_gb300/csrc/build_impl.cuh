@@ -1,0 +1,416 @@
+// Batched NBPG/Vamana insert on GB300 (algorithms/nsw.h:110-286).
+//
+// One batch of inserts runs as six launches, all batch-synchronous like the
+// reference's OpenMP phases (searches read the graph as it was before the batch):
+//   1. build_search_prune_kernel  one warp per insert: strict beam search from the
+//      insert's start points (LIST mode, visited cap VL), then the existing
+//      neighbours not yet seen, merge_union with the visited list, sort_candidates,
+//      RobustPrune (nsw.h:122-175, prune.h:50-87,159-209).  Visited entries are
+//      counted into `popular` in a popularity pass (nsw.h:220-230).
+//   2. forward_write_kernel       G[index] = pruned list (nsw.h:416-429).
+//   3-5. reverse edges grouped by target without a sort: atomic per-target counts
+//      give each edge its rank, the first edge of each target bump-allocates a
+//      contiguous block, edges scatter into it (merge_edges.h:53-81 up to order).
+//   6. rev_merge_kernel           one warp per target: the VL smallest (dist, source)
+//      reverse edges (merge_edges.h:98-119), plus existing neighbours not repeated,
+//      new distances, sort or truncate to R (nsw.h:463-511, 329-378).
+#pragma once
+#include "search_impl.cuh"
+
+namespace nbpg {
+
+struct BuildArgs {
+    SearchArgs s;             // base/graph geometry, limit, degree_limit, layout
+    const uint32_t *inserts;  // this batch's node ids
+    uint32_t bs;
+    const uint32_t *sp;       // bs * nsp_per start points
+    uint32_t nsp_per;
+    uint32_t L, VL, R, top_degree;
+    const float *alpha_node;  // per-node alpha (popularity pass) or null
+    float alpha_all;
+    const float *cos_node;
+    float cos_all;
+    uint32_t *res_ids;  // bs * R pruned neighbour ids
+    float *res_d;       // bs * R their distances
+    uint32_t *res_cnt;  // bs
+    float *popular;     // per node visited counts (popularity pass) or null
+    uint32_t *stat_vis, *stat_dist;  // per node BuildStats counters (may be null)
+    uint32_t *queue;                 // work counter for kernel 1 / kernel 6
+    // reverse edges
+    uint32_t *rank;        // bs * R
+    uint32_t *cnt_node;    // n, zero between batches
+    uint32_t *off_node;    // n
+    uint32_t *bump;        // [0] allocator, [1] group count
+    uint32_t *grp_target;  // groups
+    uint64_t *edges;       // grouped (dist, source) keys
+};
+
+constexpr double kPruneEps = 1e-5;  // kEpsilon, prune.h:212
+
+// cosine at p from squared distances, rounding as written (prune.h:218-225)
+__device__ __forceinline__ float cos_at_p(float d_p_star, float d_p_prime, float d_star_prime)
+{
+    const float b = __fsqrt_rn(d_p_prime);
+    const float c = __fsqrt_rn(d_p_star);
+    if (b == 0.f || c == 0.f) return 1.f;
+    const float num = __fsub_rn(__fadd_rn(d_p_prime, d_p_star), d_star_prime);
+    return __fdiv_rn(num, __fmul_rn(__fmul_rn(2.f, b), c));
+}
+
+__device__ __forceinline__ void load_row_regs(const SearchArgs &a, uint32_t id, uint4 (&qv)[2], int lane)
+{
+    const uint4 *row = reinterpret_cast<const uint4 *>(a.base + size_t(id) * a.row_stride);
+    const uint32_t lq = uint32_t(lane) % a.lpr;
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+        const uint32_t c = lq + v * a.lpr;
+        qv[v] = (v < int(a.vpl) && c < a.vecs) ? __ldg(row + c) : make_uint4(0, 0, 0, 0);
+    }
+}
+
+template <int DT, int MET>
+__device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t gslot, int lane)
+{
+    const SearchArgs &a = B.s;
+    const SlotLayout &lay = a.lay;
+    const uint32_t index = B.inserts[t];
+    const uint32_t R = B.R, VL = B.VL;
+    const uint8_t *prow = a.base + size_t(index) * a.row_stride;
+
+    // beam search from the start points (beam_search with k = 0, cut = 0)
+    const SearchState st = search_core<DT, MET, true>(a, prow, B.L, 0, VL, B.sp + size_t(t) * B.nsp_per, B.nsp_per,
+                                                      slot, gslot, lane, index);
+    uint32_t rp = 0;
+
+    uint64_t *tmp = st.fr0;   // existing neighbours (<= R)
+    uint64_t *pool = st.fr1;  // merged candidate pool (<= VL)
+    uint32_t *filt = reinterpret_cast<uint32_t *>(slot + lay.off_filt);
+    uint8_t *alive = slot + lay.off_fl0;
+    uint32_t *H = st.H;
+
+    uint4 qv[2];
+    load_row_regs(a, index, qv, lane);
+
+    // existing neighbours not seen by the search (nsw.h:150-161); has_been_seen inserts
+    const uint32_t *grow = a.graph + size_t(index) * a.gstride;
+    const uint32_t deg = __ldg(grow);
+    uint32_t nf = 0;
+    for (uint32_t c = 0; c * 32 < deg; ++c) {
+        const uint32_t i = c * 32 + lane;
+        const bool act = i < deg;
+        const uint32_t nb = act ? __ldg(grow + 1 + i) : kNoId;
+        const uint32_t sl = act ? filter_slot(nb, st.smask) : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(kFull, sl);
+        const unsigned earlier = peers & lanemask_lt();
+        const int src = earlier ? 31 - __clz(earlier) : lane;
+        const uint32_t prev_nb = __shfl_sync(kFull, nb, src);
+        const uint32_t hv = (act && !earlier) ? H[sl] : kNoId;
+        const bool seen = act && (earlier ? (prev_nb == nb) : (hv == nb));
+        __syncwarp();
+        if (act && !(peers & lanemask_gt())) H[sl] = nb;
+        __syncwarp();
+        const bool keep = act && !seen;
+        const unsigned km = __ballot_sync(kFull, keep);
+        if (keep) filt[nf + __popc(km & lanemask_lt())] = nb;
+        nf += __popc(km);
+    }
+    __syncwarp();
+    warp_row_keys<DT, MET>(a, qv, filt, nf, tmp, lane);
+    rp += nf;
+
+    // merge_union of the (unsorted) neighbour list with the sorted visited list, cap VL
+    // (utilities.h:128-165): a sequential two-pointer walk, run by lane 0.
+    uint32_t np = 0;
+    if (lane == 0) {
+        const uint64_t *v = st.vis;
+        uint32_t i = 0, j = 0, k = 0;
+        while (i < nf && j < st.vs && k < VL) {
+            if (tmp[i] < v[j]) pool[k++] = tmp[i++];
+            else if (v[j] < tmp[i]) pool[k++] = v[j++];
+            else { pool[k++] = tmp[i++]; ++j; }
+        }
+        while (i < nf && k < VL) pool[k++] = tmp[i++];
+        while (j < st.vs && k < VL) pool[k++] = v[j++];
+        np = k;
+    }
+    np = __shfl_sync(kFull, np, 0);
+    __syncwarp();
+
+    // sort_candidates (prune.h:50-74): p forced last, sort, drop repeats, drop p
+    const uint64_t pkey = (uint64_t(f2ord(3.402823466e38f)) << 32) | index;
+    for (uint32_t i = lane; i < np; i += 32)
+        if (key_id(pool[i]) == index) pool[i] = pkey;
+    __syncwarp();
+    sort_keys(pool, np, lane);
+    {
+        uint32_t outc = 0;
+        uint64_t carry = kKeyMax;
+        for (uint32_t base = 0; base < np; base += 32) {
+            const uint32_t i = base + lane;
+            const uint64_t v = i < np ? pool[i] : kKeyMax;
+            uint64_t prev = __shfl_up_sync(kFull, v, 1);
+            if (lane == 0) prev = carry;
+            carry = __shfl_sync(kFull, v, 31);
+            const bool keep = i < np && v != prev;
+            const unsigned m = __ballot_sync(kFull, keep);
+            __syncwarp();
+            if (keep) pool[outc + __popc(m & lanemask_lt())] = v;
+            outc += __popc(m);
+            __syncwarp();
+        }
+        np = outc;
+        if (np > 0 && key_id(pool[np - 1]) == index) --np;
+    }
+
+    // RobustPrune (limitedSimilarityPrune, prune.h:159-209)
+    const double alpha = double(B.alpha_node ? B.alpha_node[index] : B.alpha_all);
+    const double cosa = double(B.cos_node ? B.cos_node[index] : B.cos_all);
+    uint32_t sel = 0;
+    if (alpha <= kPruneEps && cosa <= kPruneEps) {
+        sel = np < R ? np : R;
+    } else {
+        for (uint32_t i = lane; i < np; i += 32) alive[i] = 1;
+        __syncwarp();
+        const uint32_t lpr = a.lpr, rows_per = 32u / lpr;
+        const uint32_t grp = uint32_t(lane) / lpr, lq = uint32_t(lane) % lpr;
+        uint32_t scan = 0;
+        while (sel < R && scan < np) {
+            const uint64_t sk = pool[scan];
+            ++scan;
+            if (!alive[scan - 1]) continue;  // pruned (index -1 in the reference)
+            const uint32_t ps = key_id(sk);
+            const float dps = key_dist(sk);
+            __syncwarp();
+            if (lane == 0) pool[sel] = sk;
+            ++sel;
+            __syncwarp();
+            uint4 pv[2];
+            load_row_regs(a, ps, pv, lane);
+            uint32_t cm = 0;
+            for (uint32_t r0 = scan; r0 < np; r0 += rows_per * 4) {
+                uint4 bv[4][2];
+                uint32_t pos[4];
+                bool live[4];
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    pos[p] = r0 + p * rows_per + grp;
+                    live[p] = pos[p] < np && alive[pos[p]];
+                    const uint32_t id = live[p] ? key_id(pool[pos[p]]) : 0u;
+#pragma unroll
+                    for (int v = 0; v < 2; ++v) {
+                        const uint32_t c = lq + v * lpr;
+                        bv[p][v] = (live[p] && v < int(a.vpl) && c < a.vecs)
+                                       ? __ldg(reinterpret_cast<const uint4 *>(a.base + size_t(id) * a.row_stride) + c)
+                                       : make_uint4(0, 0, 0, 0);
+                    }
+                }
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    uint32_t acc = 0;
+#pragma unroll
+                    for (int v = 0; v < 2; ++v)
+                        if (v < int(a.vpl)) acc = acc_vec<DT, MET>(bv[p][v], pv[v], acc);
+                    for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+                    if (lq == 0 && live[p]) {
+                        ++cm;
+                        const float dsp = finish_dist<DT, MET>(acc);
+                        const float dpp = key_dist(pool[pos[p]]);
+                        bool pruned = false;
+                        if (alpha > kPruneEps && alpha * double(dsp) <= double(dpp)) pruned = true;
+                        else if (cosa > kPruneEps && double(cos_at_p(dps, dpp, dsp)) > cosa) pruned = true;
+                        if (pruned) alive[pos[p]] = 0;
+                    }
+                }
+                __syncwarp();
+            }
+            for (uint32_t o = 16; o > 0; o >>= 1) cm += __shfl_xor_sync(kFull, cm, o);
+            rp += cm;
+        }
+    }
+    __syncwarp();
+
+    // results
+    for (uint32_t j = lane; j < sel; j += 32) {
+        B.res_ids[size_t(t) * R + j] = key_id(pool[j]);
+        B.res_d[size_t(t) * R + j] = key_dist(pool[j]);
+    }
+    if (lane == 0) {
+        B.res_cnt[t] = sel;
+        if (B.stat_dist) B.stat_dist[index] += st.cmps + rp;
+        if (B.stat_vis) B.stat_vis[index] += uint32_t(st.nvis);
+    }
+    if (B.popular)
+        for (uint32_t i = lane; i < st.vs; i += 32) atomicAdd(&B.popular[key_id(st.vis[i])], 1.0f);
+    __syncwarp();
+}
+
+template <int DT, int MET>
+__global__ void __launch_bounds__(512) build_search_prune_kernel(BuildArgs B)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint8_t *slot = smem + size_t(warp) * B.s.lay.bytes;
+    const uint32_t gslot = blockIdx.x * (blockDim.x >> 5) + warp;
+    while (true) {
+        uint32_t w = 0;
+        if (lane == 0) w = atomicAdd(B.queue, 1u);
+        w = __shfl_sync(kFull, w, 0);
+        if (w >= B.bs) break;
+        build_one<DT, MET>(B, w, slot, gslot, lane);
+    }
+}
+
+// G[index] = pruned list; slots past the degree zeroed.
+__global__ void forward_write_kernel(BuildArgs B)
+{
+    const uint32_t t = blockIdx.x;
+    if (t >= B.bs) return;
+    const uint32_t index = B.inserts[t];
+    const uint32_t cnt = B.res_cnt[t];
+    uint32_t *row = const_cast<uint32_t *>(B.s.graph) + size_t(index) * B.s.gstride;
+    for (uint32_t j = threadIdx.x; j <= B.R; j += blockDim.x)
+        row[j] = j == 0 ? cnt : (j - 1 < cnt ? B.res_ids[size_t(t) * B.R + j - 1] : 0u);
+}
+
+__global__ void rev_count_kernel(BuildArgs B)
+{
+    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= size_t(B.bs) * B.R) return;
+    const uint32_t t = uint32_t(e / B.R), j = uint32_t(e % B.R);
+    if (j >= B.res_cnt[t]) return;
+    B.rank[e] = atomicAdd(&B.cnt_node[B.res_ids[e]], 1u);
+}
+
+__global__ void rev_alloc_kernel(BuildArgs B)
+{
+    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= size_t(B.bs) * B.R) return;
+    const uint32_t t = uint32_t(e / B.R), j = uint32_t(e % B.R);
+    if (j >= B.res_cnt[t] || B.rank[e] != 0) return;
+    const uint32_t target = B.res_ids[e];
+    B.off_node[target] = atomicAdd(&B.bump[0], B.cnt_node[target]);
+    B.grp_target[atomicAdd(&B.bump[1], 1u)] = target;
+}
+
+__global__ void rev_scatter_kernel(BuildArgs B)
+{
+    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= size_t(B.bs) * B.R) return;
+    const uint32_t t = uint32_t(e / B.R), j = uint32_t(e % B.R);
+    if (j >= B.res_cnt[t]) return;
+    const uint32_t target = B.res_ids[e];
+    B.edges[B.off_node[target] + B.rank[e]] = make_key(B.res_d[e], B.inserts[t]);
+}
+
+// per-warp shared memory of rev_merge_kernel
+constexpr uint32_t kMergeCap = 256;  // candidate keys (VL + R <= 256)
+constexpr uint32_t kMergeWarpBytes = kMergeCap * 8 + 128 * 4 + 128 * 8;
+
+template <int DT, int MET>
+__global__ void __launch_bounds__(256) rev_merge_kernel(BuildArgs B)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const SearchArgs &a = B.s;
+    const uint32_t VL = B.VL, R = B.R;
+    uint8_t *ws = smem + size_t(warp) * kMergeWarpBytes;
+    uint64_t *cand = reinterpret_cast<uint64_t *>(ws);
+    uint32_t *ids = reinterpret_cast<uint32_t *>(ws + kMergeCap * 8);
+    uint64_t *exact = reinterpret_cast<uint64_t *>(ws + kMergeCap * 8 + 128 * 4);
+    const uint32_t ngroups = B.bump[1];
+    while (true) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(B.queue, 1u);
+        g = __shfl_sync(kFull, g, 0);
+        if (g >= ngroups) break;
+        const uint32_t target = B.grp_target[g];
+        const uint32_t size = B.cnt_node[target];
+        const uint64_t *E = B.edges + B.off_node[target];
+
+        // the VL smallest (dist, source) reverse edges, sorted (merge_edges.h:98-119)
+        uint32_t cs = 0;
+        {
+            uint64_t v[8];
+            const uint32_t first = size < kMergeCap ? size : kMergeCap;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) v[r] = uint32_t(r * 32 + lane) < first ? E[r * 32 + lane] : kKeyMax;
+            warp_bitonic_sort<8>(v, lane);
+            uint32_t done = first;
+            while (done < size) {
+                // keep the VL best in [0, VL), refill [VL, cap) with unseen keys, re-sort
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const uint32_t i = r * 32 + lane;
+                    if (i >= VL) {
+                        const uint32_t src = done + (i - VL);
+                        v[r] = src < size ? E[src] : kKeyMax;
+                    }
+                }
+                done += kMergeCap - VL;
+                warp_bitonic_sort<8>(v, lane);
+            }
+            cs = size < VL ? size : VL;
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                if (uint32_t(r * 32 + lane) < cs) cand[r * 32 + lane] = v[r];
+            __syncwarp();
+        }
+        const uint32_t pre = cs;
+
+        // existing neighbours not already present, in adjacency order (nsw.h:358-378)
+        const uint32_t *grow = a.graph + size_t(target) * a.gstride;
+        const uint32_t deg = grow[0];
+        for (uint32_t c = 0; c * 32 < deg; ++c) {
+            const uint32_t i = c * 32 + lane;
+            const uint32_t nb = i < deg ? grow[1 + i] : kNoId;
+            bool dup = false;
+            if (i < deg) {
+                for (uint32_t q = 0; q < pre && !dup; ++q) dup = key_id(cand[q]) == nb;
+                for (uint32_t q = 0; q < i && !dup; ++q) dup = grow[1 + q] == nb;
+            }
+            const bool add = i < deg && !dup && cs + __popc(__ballot_sync(kFull, i < deg && !dup) & lanemask_lt()) < VL + R;
+            const unsigned m = __ballot_sync(kFull, add);
+            if (add) ids[cs - pre + __popc(m & lanemask_lt())] = nb;
+            cs += __popc(m);
+            __syncwarp();
+        }
+
+        // distances of the appended neighbours: top_degree exact, the last exact, the
+        // middle interpolated (nsw.h:329-355)
+        uint32_t rp = 0;
+        if (cs > pre) {
+            uint4 qv[2];
+            load_row_regs(a, target, qv, lane);
+            const uint32_t end = (pre + B.top_degree) < cs ? pre + B.top_degree : cs;
+            const uint32_t nex = end - pre;
+            warp_row_keys<DT, MET>(a, qv, ids, nex, exact, lane);
+            if (end < cs) warp_row_keys<DT, MET>(a, qv, ids + (cs - 1 - pre), 1, exact + nex, lane);  // the last, exact
+            rp = nex + (end < cs ? 1u : 0u);
+            for (uint32_t j = pre + lane; j < end; j += 32) cand[j] = exact[j - pre];
+            if (end < cs) {
+                const float ad = key_dist(cand[end - 1]);
+                const float bd = key_dist(exact[nex]);
+                const float delta = __fdiv_rn(__fsub_rn(ad, bd), float(cs - end));
+                for (uint32_t j = end + lane; j < cs - 1; j += 32) {
+                    const float dj = __fadd_rn(ad, __fmul_rn(float(j - end + 1), delta));
+                    cand[j] = make_key(dj, ids[j - pre]);
+                }
+                if (lane == 0) cand[cs - 1] = exact[nex];
+            }
+            __syncwarp();
+        }
+        // sort by (dist, id), truncate to R, write (nsw.h:488-511)
+        sort_keys(cand, cs, lane);
+        const uint32_t outn = cs < R ? cs : R;
+        uint32_t *row = const_cast<uint32_t *>(a.graph) + size_t(target) * a.gstride;
+        for (uint32_t j = lane; j <= R; j += 32)
+            row[j] = j == 0 ? outn : (j - 1 < outn ? key_id(cand[j - 1]) : 0u);
+        if (lane == 0) {
+            if (B.stat_dist) B.stat_dist[target] += rp;
+            B.cnt_node[target] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace nbpg

@@ -200,37 +200,33 @@ __device__ __forceinline__ uint32_t warp_upper_bound(const uint64_t *s, uint32_t
     return n;
 }
 
-// One query, executed by the whole warp.  slot: this warp's shared-memory slot;
-// gslot: index of its global scratch block; self: node excluded from expansion
-// (Points[a].same_as(p), beamSearch.h:79) or kNoId.
+// The search itself (filtered_beam_search with Points == Q_Points), executed by the
+// whole warp on one query row.  slot: this warp's shared-memory slot; gslot: index of
+// its global scratch block; sp/nsp: start points; self: node excluded from expansion
+// (Points[a].same_as(p), beamSearch.h:79) or kNoId.  Leaves the frontier, visited list
+// and visited filter in place and describes them in the returned state.
+struct SearchState {
+    uint64_t *fr0, *fr1, *vis;
+    uint32_t *H;
+    int b;
+    uint32_t fs, vs, cmps, smask;
+    uint64_t nvis;
+    bool taint;
+    __device__ uint64_t *frontier() const { return b ? fr1 : fr0; }
+};
+
 template <int DT, int MET, bool LIST>
-__device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, uint32_t gslot, int lane,
-                             uint32_t self = kNoId)
+__device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_bytes, uint32_t L, uint32_t k,
+                                   uint64_t max_visited, const uint32_t *sp, uint32_t nsp, uint8_t *slot,
+                                   uint32_t gslot, int lane, uint32_t self)
 {
     const SlotLayout &lay = a.lay;
-    const uint32_t L = a.Ls ? a.Ls[qi] : a.L_all;
-    const uint32_t k = a.ks ? a.ks[qi] : a.k_all;
     const uint32_t S = filter_slots_for(L);
     const uint32_t smask = S - 1;
-    const uint64_t max_visited = uint64_t(a.visited_factor) * L;
-    if (L == 0 || k == 0 || k > L || L > a.lay.Lcap || a.nsp > L || k > a.k_stride ||
-        (LIST && !a.g_vis && max_visited > a.lay.Vcap) || (!a.g_hash && S > a.lay.Scap) ||
-        (a.g_hash && S > a.g_hash_slots) || (LIST && a.g_vis && max_visited > a.g_vis_cap)) {
-        // rejected (the reference aborts on k > L, beamSearch.h:268-273): empty row + error flag
-        for (uint32_t j = lane; j < a.k_stride; j += 32) {
-            a.out_ids[size_t(qi) * a.k_stride + j] = kNoId;
-            if (a.out_dists) a.out_dists[size_t(qi) * a.k_stride + j] = __int_as_float(0x7f800000);
-        }
-        if (lane == 0) {
-            if (a.out_count) a.out_count[qi] = 0;
-            if (a.out_visited) a.out_visited[qi] = 0;
-            if (a.out_cmps) a.out_cmps[qi] = 0;
-            if (a.err) atomicExch(a.err, 1u);
-        }
-        __syncwarp();
-        return;
-    }
-
+    SearchState st{};
+    st.smask = smask;
+    st.fr0 = reinterpret_cast<uint64_t *>(slot + lay.off_fr0);
+    st.fr1 = reinterpret_cast<uint64_t *>(slot + lay.off_fr1);
     uint64_t *fr[2] = {reinterpret_cast<uint64_t *>(slot + lay.off_fr0), reinterpret_cast<uint64_t *>(slot + lay.off_fr1)};
     uint8_t *fl[2] = {slot + lay.off_fl0, slot + lay.off_fl1};
     uint64_t *cand = reinterpret_cast<uint64_t *>(slot + lay.off_cand);
@@ -239,12 +235,14 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     uint64_t *vis = nullptr;
     if constexpr (LIST)
         vis = a.g_vis ? a.g_vis + size_t(gslot) * a.g_vis_cap : reinterpret_cast<uint64_t *>(slot + lay.off_vis);
+    st.vis = vis;
     uint32_t *H = a.g_hash ? a.g_hash + size_t(gslot) * a.g_hash_slots : reinterpret_cast<uint32_t *>(slot + lay.off_hash);
+    st.H = H;
 
     // query vector in registers: this lane's 16-byte pieces of the row
     uint4 qv[2];
     {
-        const uint4 *qrow = reinterpret_cast<const uint4 *>(a.queries + size_t(qi) * a.row_stride);
+        const uint4 *qrow = reinterpret_cast<const uint4 *>(qrow_bytes);
         const uint32_t lq = uint32_t(lane) % a.lpr;
 #pragma unroll
         for (int v = 0; v < 2; ++v) {
@@ -258,11 +256,10 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     __syncwarp();
 
     // init_starting_points (query_params.h:204-221)
-    const uint32_t nsp = a.nsp;
-    warp_row_keys<DT, MET>(a, qv, a.sp, nsp, fr[0], lane);
+    warp_row_keys<DT, MET>(a, qv, sp, nsp, fr[0], lane);
     if (lane == 0)
         for (uint32_t s = 0; s < nsp; ++s) {
-            const uint32_t v = a.sp[s];
+            const uint32_t v = sp[s];
             H[filter_slot(v, smask)] = v;
         }
     __syncwarp();
@@ -430,12 +427,55 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
         __syncwarp();
     }
 
+    st.b = b;
+    st.fs = fs;
+    st.vs = vs;
+    st.cmps = cmps;
+    st.nvis = nvis;
+    st.taint = taint;
+    return st;
+}
+
+// One query of a search request: argument checks, search_core, outputs.
+template <int DT, int MET, bool LIST>
+__device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, uint32_t gslot, int lane)
+{
+    const uint32_t L = a.Ls ? a.Ls[qi] : a.L_all;
+    const uint32_t k = a.ks ? a.ks[qi] : a.k_all;
+    const uint32_t S = filter_slots_for(L);
+    const uint64_t max_visited = uint64_t(a.visited_factor) * L;
+    if (L == 0 || k == 0 || k > L || L > a.lay.Lcap || a.nsp > L || k > a.k_stride ||
+        (LIST && !a.g_vis && max_visited > a.lay.Vcap) || (!a.g_hash && S > a.lay.Scap) ||
+        (a.g_hash && S > a.g_hash_slots) || (LIST && a.g_vis && max_visited > a.g_vis_cap)) {
+        // rejected (the reference aborts on k > L, beamSearch.h:268-273): empty row + error flag
+        for (uint32_t j = lane; j < a.k_stride; j += 32) {
+            a.out_ids[size_t(qi) * a.k_stride + j] = kNoId;
+            if (a.out_dists) a.out_dists[size_t(qi) * a.k_stride + j] = __int_as_float(0x7f800000);
+        }
+        if (lane == 0) {
+            if (a.out_count) a.out_count[qi] = 0;
+            if (a.out_visited) a.out_visited[qi] = 0;
+            if (a.out_cmps) a.out_cmps[qi] = 0;
+            if (a.err) atomicExch(a.err, 1u);
+        }
+        __syncwarp();
+        return;
+    }
+
+    const SearchState st = search_core<DT, MET, LIST>(a, a.queries + size_t(qi) * a.row_stride, L, k, max_visited,
+                                                      a.sp, a.nsp, slot, gslot, lane, kNoId);
+    const uint64_t *frb = st.frontier();
+    const uint32_t fs = st.fs;
+    const uint64_t nvis = st.nvis;
+    const uint32_t cmps = st.cmps;
+    const bool taint = st.taint;
+
     // results: frontier[0:min(k, fs)] (beamSearch.h:249-254)
     const uint32_t kk = k < fs ? k : fs;
     for (uint32_t j = lane; j < a.k_stride; j += 32) {
         const size_t o = size_t(qi) * a.k_stride + j;
         if (j < kk) {
-            const uint64_t key = fr[b][j];
+            const uint64_t key = frb[j];
             a.out_ids[o] = key_id(key);
             if (a.out_dists) a.out_dists[o] = output_dist<MET>(key_dist(key));
         } else {
