@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""NBPG search on one GB300: QPS at recall@10 >= 0.95 on a 1M x 128 u8 NBPG index.
+
+Workload (the NBPG configuration of the benchmark): 1,000,000 base + 10,000 query
+u8 vectors of dim 128 drawn from a 1000-centre Gaussian mixture (centres U[0,120],
+sigma 20, rounded and clipped; seeded synthetic data standing in for SIFT1M);
+NBPG build R=64, L=100, VL=140, num_passes=2, num_split=4, dynamic prune,
+min_alpha=1.05 (max_alpha 1.1, the Vamana default), built on the GPU; ground truth
+k=100 by the GPU brute-force kNN in CompGT-compatible mode.  The beam width L is
+the smallest of the reference's sweep values in [10, 200] reaching recall@10 >= 0.95.
+
+A step = one strict batched search of all 10k queries at that L (k=10, cut=1.35,
+start point 0): the persistent kernel pulling queries from a device queue.
+`value` is device-resident QPS over the timed steps (CUDA events on the launching
+stream); `e2e` is the same search through the C ABI (nbpg_search) from pinned host
+queries to host results.  The index (128 MB vectors + 272 MB graph) is larger than
+L2, so no flush is needed between steps.
+
+--impl reference times the reference algorithm on the host cores instead: the CPU
+restatement of qsearchAll (OpenMP, all threads) on the same index, built on the CPU.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(n=1_000_000, nq=10_000, dim=128, centres=1000, R=64, L_build=100, VL=140, num_split=4, num_passes=2,
+           dynamic_prune=True, min_alpha=1.05, max_alpha=1.1, k=10, recall_target=0.95, cut=1.35, gt_k=100)
+# beam widths of the reference's sweep (check_nn_recall.h:206-208) up to 200
+L_SWEEP = [10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 22, 24, 26, 28, 30, 32, 34, 36, 38, 40, 45, 50, 55, 60, 65,
+           70, 80, 90, 100, 120, 140, 160, 180, 200]
+METRIC = "QPS @ recall@10>=0.95, 1M x128 u8, batched vs plain GPU kernel; p50/p99 ms"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_data():
+    from nbpg_gb300 import synth
+    t = time.time()
+    base, q = synth.u8_mixture(CFG["n"], CFG["nq"], dim=CFG["dim"], n_centres=CFG["centres"])
+    log(f"[bench] data {base.shape} {q.shape} in {time.time() - t:.1f}s")
+    return base, q
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_query():
+    p = os.path.join(ROOT, "profiles", "search_traffic.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["dram_bytes_per_query"])
+        except Exception:
+            return None
+    return None
+
+
+def cpu_search_qps(base, g, q, L, threads, min_seconds=8.0):
+    """The reference algorithm on the host: OpenMP search over the queries, repeated until min_seconds."""
+    from oracle.oracle import oracle
+    O = oracle()
+    O.search("u8", "l2", base, g, q[:64], L=L, k=CFG["k"], cut=CFG["cut"], threads=threads)
+    reps, t = 0, time.perf_counter()
+    while True:
+        O.search("u8", "l2", base, g, q, L=L, k=CFG["k"], cut=CFG["cut"], threads=threads)
+        reps += 1
+        el = time.perf_counter() - t
+        if el >= min_seconds or reps >= 50:
+            return reps * len(q) / el, reps
+
+
+def run_reference(args):
+    """CPU arm: build on the host with the CPU restatement, choose L, time the search."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.oracle import oracle
+    from nbpg_gb300.recall import recall_at_k
+    threads = os.cpu_count() or 1
+    base, q = make_data()
+    O = oracle()
+    t = time.time()
+    g, _, _, _ = O.build_graph("u8", "l2", base, R=CFG["R"], L=CFG["L_build"], VL=CFG["VL"],
+                               num_split=CFG["num_split"], num_passes=CFG["num_passes"],
+                               dynamic_prune=CFG["dynamic_prune"], min_alpha=CFG["min_alpha"],
+                               max_alpha=CFG["max_alpha"], sp_seed=0, threads=threads)
+    log(f"[bench/ref] CPU build {time.time() - t:.1f}s on {threads} threads")
+    sample = q[:2000]
+    t = time.time()
+    gi, gd = O.gt("u8", "l2", base, sample, k=CFG["gt_k"], exact=False, threads=threads)
+    log(f"[bench/ref] CPU ground truth for {len(sample)} queries {time.time() - t:.1f}s")
+    L_op = None
+    for L in L_SWEEP:
+        ids = O.search("u8", "l2", base, g, sample, L=L, k=CFG["k"], cut=CFG["cut"], threads=threads)[0]
+        r = recall_at_k(ids, gi, gd, CFG["k"])
+        if r >= CFG["recall_target"]:
+            L_op, rec = L, r
+            break
+    if L_op is None:
+        L_op, rec = L_SWEEP[-1], r
+    for _ in range(args.warmup):
+        O.search("u8", "l2", base, g, sample, L=L_op, k=CFG["k"], cut=CFG["cut"], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        O.search("u8", "l2", base, g, sample, L=L_op, k=CFG["k"], cut=CFG["cut"], threads=threads)
+        times.append(time.perf_counter() - t)
+    qps = len(sample) * len(times) / sum(times)
+    line = {"metric": METRIC, "value": qps, "unit": "queries/s", "impl": "reference", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded 1000-centre u8 Gaussian mixture standing in for SIFT1M)",
+            "config": {"workload": "NBPG 1M x 128 u8 search, 10k queries, k=10", "L": L_op, "recall@10": rec,
+                       "index_built_on": "host CPU (restatement of build_vamana)", "n_base": CFG["n"]},
+            "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} queries per step at L={L_op}, {args.steps} steps"},
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from nbpg_gb300 import _lib
+    from nbpg_gb300.index import Index, QueryParams, ground_truth
+    from nbpg_gb300.recall import recall_at_k
+
+    base, q = make_data()
+    k = CFG["k"]
+    nq = len(q)
+
+    # index + build on the GPU
+    idx = Index(base, "u8", "l2", max_degree=CFG["R"], device=local)
+    t = time.time()
+    st, _, _ = idx.build_vamana(L=CFG["L_build"], VL=CFG["VL"], num_split=CFG["num_split"],
+                                num_passes=CFG["num_passes"], dynamic_prune=CFG["dynamic_prune"],
+                                min_alpha=CFG["min_alpha"], max_alpha=CFG["max_alpha"], sp_seed=0)
+    build_s = time.time() - t
+    g = idx.get_graph()
+    avg_deg = float(g[:, 0].mean())
+    log(f"[bench] GPU build {build_s:.2f}s ({st.batches} batches, {st.isolated} isolated), avg degree {avg_deg:.1f}")
+
+    t = time.time()
+    gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
+    gt_s = time.time() - t
+    log(f"[bench] GPU ground truth (CompGT mode) {gt_s:.2f}s")
+    gei, ged = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=True, device=local)
+
+    # L sweep (reference sweep values up to 200) with the batched kernel
+    L_op, rec, sweep = None, 0.0, []
+    for L in L_SWEEP:
+        r = idx.search(q, QueryParams(k=k, beamSize=L, cut=CFG["cut"]))
+        rc = recall_at_k(r.ids, gi, gd, k)
+        sweep.append((L, round(rc, 4)))
+        if rc >= CFG["recall_target"]:
+            L_op, rec = L, rc
+            res_op = r
+            break
+    if L_op is None:
+        L_op, rec, res_op = L_SWEEP[-1], rc, r
+    rec_exact = recall_at_k(res_op.ids, gei, ged, k)
+    log(f"[bench] operating point L={L_op}: recall@10 {rec:.4f} (CompGT GT), {rec_exact:.4f} (exact GT)")
+
+    # device-resident buffers
+    _, row_stride, _, _ = idx.device_info()
+    qdev = torch.zeros((nq, row_stride), dtype=torch.uint8, device="cuda")
+    qdev[:, :CFG["dim"]] = torch.from_numpy(q).cuda()
+    o_ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+    o_d = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    o_c = torch.empty(nq, dtype=torch.int32, device="cuda")
+    o_v = torch.empty(nq, dtype=torch.int32, device="cuda")
+    o_m = torch.empty(nq, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    qp = QueryParams(k=k, beamSize=L_op, cut=CFG["cut"])
+
+    def dev_search(kernel="batched"):
+        idx.search_device(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, o_d.data_ptr(), o_c.data_ptr(),
+                          o_v.data_ptr(), o_m.data_ptr(), kernel=kernel, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        dev_search()
+    torch.cuda.synchronize()
+    # parity of the timed path with the host-API result at the operating point
+    assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "device-path results differ"
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for e0, e1 in evs:
+            e0.record(stream)
+            dev_search()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_s = float(tt.item())
+        if rank == 0:
+            dist.barrier()
+    value = world * nq * args.steps / total_s
+    ms_step = 1e3 * total_s / args.steps
+
+    # plain one-query-per-block kernel at the same L
+    for _ in range(2):
+        dev_search("plain")
+    torch.cuda.synchronize()
+    pe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for e0, e1 in pe:
+        e0.record(stream)
+        dev_search("plain")
+        e1.record(stream)
+    torch.cuda.synchronize()
+    plain_qps = nq * len(pe) / (sum(a.elapsed_time(b) for a, b in pe) / 1e3)
+    assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "plain kernel results differ"
+
+    # e2e through the C ABI: pinned host queries in, host results out, every step
+    L = _lib.lib()
+    qh = torch.from_numpy(q).pin_memory()
+    oh_ids = torch.empty((nq, k), dtype=torch.int32).pin_memory()
+    oh_d = torch.empty((nq, k), dtype=torch.float32).pin_memory()
+    oh_c, oh_v, oh_m = (torch.empty(nq, dtype=torch.int32).pin_memory() for _ in range(3))
+    prm = _lib.SearchParams(k, L_op, CFG["cut"], 0, 0, 8, 0, 0)
+    sp = (C.c_uint32 * 1)(0)
+    u32p = C.POINTER(C.c_uint32)
+
+    def host_search():
+        _lib.check(L.nbpg_search(idx.handle, qh.data_ptr(), nq, C.byref(prm), None, None, sp, 1, k,
+                                 C.cast(oh_ids.data_ptr(), u32p), C.cast(oh_d.data_ptr(), C.POINTER(C.c_float)),
+                                 C.cast(oh_c.data_ptr(), u32p), C.cast(oh_v.data_ptr(), u32p),
+                                 C.cast(oh_m.data_ptr(), u32p)))
+
+    for _ in range(args.warmup):
+        host_search()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        host_search()
+    e2e_s = time.perf_counter() - t
+    e2e_qps = world * nq * args.steps / e2e_s
+    assert np.array_equal(oh_ids.numpy().view(np.uint32), res_op.ids), "e2e results differ"
+    h2d = nq * CFG["dim"]
+    d2h = nq * k * 8 + nq * 12 + 4
+
+    # roofline of the search kernel: algorithmic bytes per launch
+    vis = res_op.visited.astype(np.float64)
+    cmps = res_op.cmps.astype(np.float64)
+    row = float(CFG["dim"])
+    alg_bytes = float((vis * 4.0 * (1.0 + avg_deg) + cmps * row + row).sum())
+    peak, peak_src = measured_peaks()
+    achieved = alg_bytes / (total_s / args.steps) / 1e9
+    tpq = traffic_per_query()
+
+    # CPU baseline (rank 0, N=1): the reference algorithm on the host cores
+    cpu = None
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        cq, reps = cpu_search_qps(base, g, q, L_op, threads, args.cpu_seconds)
+        cpu = {"value": cq, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": f"{nq} queries x {reps} reps at L={L_op}, k={k} (CPU restatement of qsearchAll, OpenMP)"}
+
+    clocks = clk.summary()
+    line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded 1000-centre u8 Gaussian mixture standing in for SIFT1M)",
+            "config": {"workload": "NBPG 1M x 128 u8 search, 10k queries, k=10, batched persistent kernel",
+                       "n_base": CFG["n"], "n_query": nq, "R": CFG["R"], "build": "L=100 VL=140 passes=2 split=4 "
+                       "dynamic_prune min_alpha=1.05 max_alpha=1.1 (GPU build)", "L": L_op, "cut": CFG["cut"],
+                       "recall@10": round(rec, 4), "recall@10_exact_gt": round(rec_exact, 4),
+                       "l2_policy": "index (400 MB) larger than L2; no flush",
+                       "plain_kernel_qps": plain_qps, "batched_over_plain": value / plain_qps,
+                       "build_s": round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
+                       "L_sweep": sweep, "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_src,
+                         "traffic": None if tpq is None else tpq * nq},
+            "cpu_baseline": cpu, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -368,7 +368,10 @@ __global__ void __launch_bounds__(256) rev_merge_kernel(BuildArgs B)
                 for (uint32_t q = 0; q < pre && !dup; ++q) dup = key_id(cand[q]) == nb;
                 for (uint32_t q = 0; q < i && !dup; ++q) dup = grow[1 + q] == nb;
             }
-            const bool add = i < deg && !dup && cs + __popc(__ballot_sync(kFull, i < deg && !dup) & lanemask_lt()) < VL + R;
+            // every lane takes part in both ballots (a full-mask ballot under a
+            // short-circuit would leave lanes out)
+            const unsigned cand_m = __ballot_sync(kFull, i < deg && !dup);
+            const bool add = i < deg && !dup && cs + __popc(cand_m & lanemask_lt()) < VL + R;
             const unsigned m = __ballot_sync(kFull, add);
             if (add) ids[cs - pre + __popc(m & lanemask_lt())] = nb;
             cs += __popc(m);

@@ -8,8 +8,12 @@
 //   COMPGT: fill the first k ids, tracking (toppos, topdist) with a strict '>' scan;
 //           afterwards admit d < topdist into slot toppos and rescan with the value of
 //           topk[0] read BEFORE the overwrite (the stale read of CompGT.cpp:82-84).
-//           topdist never increases, so only d < topdist-at-tile-start can be admitted:
-//           the warp ballots those survivors and replays them one by one.
+//           The stale read can make topdist rise (to the value just evicted from
+//           slot 0), but B = max(topdist, largest value in the list) never rises: an
+//           admission puts in a value below topdist, and the new topdist is a value
+//           that was in the list before it.  So only d < B-at-tile-start can be
+//           admitted in a tile: the warp ballots those survivors and replays them one
+//           by one against the live topdist.
 //   EXACT:  keep the k smallest (dist, id) keys sorted; survivors below the current
 //           k-th key are inserted in order.
 //
@@ -65,11 +69,13 @@ __global__ void __launch_bounds__(GT_THREADS) gt_kernel(GtArgs a)
     uint32_t cnt[GT_QPW];
     uint32_t toppos[GT_QPW];
     float topdist[GT_QPW];
+    float lmax[GT_QPW];  // largest value held in the list (COMPGT survivor bound)
 #pragma unroll
     for (int j = 0; j < GT_QPW; ++j) {
         cnt[j] = 0;
         toppos[j] = 0;
         topdist[j] = -3.402823466e38f;
+        lmax[j] = -3.402823466e38f;
     }
 
     const uint64_t ntiles = (a.n + GT_BT - 1) / GT_BT;
@@ -138,6 +144,7 @@ __global__ void __launch_bounds__(GT_THREADS) gt_kernel(GtArgs a)
                 cnt[j] = c;
                 topdist[j] = __shfl_sync(kFull, topdist[j], 0);
                 toppos[j] = __shfl_sync(kFull, toppos[j], 0);
+                lmax[j] = topdist[j];  // during the fill topdist is the running maximum
                 if (c == k && a.exact) {
                     // sort the k filled keys once (k <= 256)
                     uint64_t v[8];
@@ -155,7 +162,8 @@ __global__ void __launch_bounds__(GT_THREADS) gt_kernel(GtArgs a)
             // admission phase over ids [b0 + start, b0 + bcount)
             const uint32_t start = (b0 < k) ? uint32_t(k - b0) : 0u;
             if (!a.exact) {
-                const float T0 = topdist[j];
+                const float T0 = fmaxf(lmax[j], topdist[j]);
+                bool admitted = false;
                 for (uint32_t base = start; base < bcount; base += 32) {
                     const uint32_t i = base + lane;
                     const float d = i < bcount ? dq[i] : 0.0f;
@@ -186,7 +194,15 @@ __global__ void __launch_bounds__(GT_THREADS) gt_kernel(GtArgs a)
                         }
                         if (bv > old0) { topdist[j] = bv; toppos[j] = bi; }
                         else { topdist[j] = old0; toppos[j] = 0; }
+                        admitted = true;
                     }
+                }
+                if (admitted) {
+                    float mx = -3.402823466e38f;
+                    for (uint32_t l = lane; l < k; l += 32) mx = fmaxf(mx, __uint_as_float(uint32_t(tk[l] >> 32)));
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+                    lmax[j] = mx;
                 }
             } else {
                 for (uint32_t base = start; base < bcount; base += 32) {
