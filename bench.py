@@ -195,13 +195,40 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_search(idx, q, L, args):
+    """Warmup + timed steps of the batched search only (the command the ncu captures run)."""
+    import torch
+    from nbpg_gb300.index import QueryParams
+    nq, k = len(q), CFG["k"]
+    _, row_stride, _, _ = idx.device_info()
+    qdev = torch.zeros((nq, row_stride), dtype=torch.uint8, device="cuda")
+    qdev[:, :CFG["dim"]] = torch.from_numpy(q).cuda()
+    o_ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+    o_v = torch.empty(nq, dtype=torch.int32, device="cuda")
+    o_m = torch.empty(nq, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    qp = QueryParams(k=k, beamSize=L, cut=CFG["cut"])
+    for i in range(args.warmup + args.steps):
+        idx.search_device(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, None, None, o_v.data_ptr(), o_m.data_ptr(),
+                          stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    v, m = o_v.cpu().numpy(), o_m.cpu().numpy()
+    print(json.dumps({"profile": "batched search", "L": L, "nq": nq, "launches": 2 * (args.warmup + args.steps),
+                      "visited_mean": float(v.mean()), "cmps_mean": float(m.mean())}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--save-graph", default=None, help="write the built graph (.graph format) here")
+    ap.add_argument("--load-graph", default=None, help="use this graph instead of building one")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: index + --L, then warmup + steps of the batched search only")
+    ap.add_argument("--L", type=int, default=0, help="beam width for --profile (default: the sweep's choice)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -225,15 +252,25 @@ def main():
     nq = len(q)
 
     # index + build on the GPU
+    from nbpg_gb300 import formats
     idx = Index(base, "u8", "l2", max_degree=CFG["R"], device=local)
-    t = time.time()
-    st, _, _ = idx.build_vamana(L=CFG["L_build"], VL=CFG["VL"], num_split=CFG["num_split"],
-                                num_passes=CFG["num_passes"], dynamic_prune=CFG["dynamic_prune"],
-                                min_alpha=CFG["min_alpha"], max_alpha=CFG["max_alpha"], sp_seed=0)
-    build_s = time.time() - t
+    build_s = None
+    if args.load_graph:
+        idx.set_graph(formats.read_graph(args.load_graph))
+    else:
+        t = time.time()
+        st, _, _ = idx.build_vamana(L=CFG["L_build"], VL=CFG["VL"], num_split=CFG["num_split"],
+                                    num_passes=CFG["num_passes"], dynamic_prune=CFG["dynamic_prune"],
+                                    min_alpha=CFG["min_alpha"], max_alpha=CFG["max_alpha"], sp_seed=0)
+        build_s = time.time() - t
+        log(f"[bench] GPU build {build_s:.2f}s ({st.batches} batches, {st.isolated} isolated)")
     g = idx.get_graph()
+    if args.save_graph:
+        formats.write_graph(args.save_graph, g)
     avg_deg = float(g[:, 0].mean())
-    log(f"[bench] GPU build {build_s:.2f}s ({st.batches} batches, {st.isolated} isolated), avg degree {avg_deg:.1f}")
+    log(f"[bench] average degree {avg_deg:.2f}")
+    if args.profile:
+        return profile_search(idx, q, args.L or 19, args)
 
     t = time.time()
     gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
@@ -265,7 +302,10 @@ def main():
     o_c = torch.empty(nq, dtype=torch.int32, device="cuda")
     o_v = torch.empty(nq, dtype=torch.int32, device="cuda")
     o_m = torch.empty(nq, dtype=torch.int32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: a NULL stream handle would mean "the index's own stream" to the
+    # library, and events on the legacy default stream would not order with it
+    stream = torch.cuda.Stream()
+    assert stream.cuda_stream != 0
     qp = QueryParams(k=k, beamSize=L_op, cut=CFG["cut"])
 
     def dev_search(kernel="batched"):
@@ -369,7 +409,7 @@ def main():
                        "recall@10": round(rec, 4), "recall@10_exact_gt": round(rec_exact, 4),
                        "l2_policy": "index (400 MB) larger than L2; no flush",
                        "plain_kernel_qps": plain_qps, "batched_over_plain": value / plain_qps,
-                       "build_s": round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
+                       "build_s": None if build_s is None else round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
                        "L_sweep": sweep, "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": 2 * args.steps,
