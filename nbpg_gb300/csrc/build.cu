@@ -23,28 +23,28 @@ SlotLayout make_slot_layout(uint32_t Lmax, uint32_t R, bool vis_smem, uint32_t V
 
 enum class Popular { FixedMin = 1, FixedMax, Cal, Prune };
 
-template <int DT, int MET>
+template <int DT, int MET, int VPL>
 struct BuildKernels {
     static cudaError_t setup(size_t smem_search, size_t smem_merge)
     {
-        cudaError_t e = cudaFuncSetAttribute(build_search_prune_kernel<DT, MET>,
+        cudaError_t e = cudaFuncSetAttribute(build_search_prune_kernel<DT, MET, VPL>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_search));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(rev_merge_kernel<DT, MET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(rev_merge_kernel<DT, MET, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(smem_merge));
         return e;
     }
     static cudaError_t occ(uint32_t threads, size_t smem, int *blocks)
     {
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, build_search_prune_kernel<DT, MET>, int(threads), smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, build_search_prune_kernel<DT, MET, VPL>, int(threads), smem);
     }
     static void search(uint32_t grid, uint32_t threads, size_t smem, const BuildArgs &B, cudaStream_t st)
     {
-        build_search_prune_kernel<DT, MET><<<grid, threads, smem, st>>>(B);
+        build_search_prune_kernel<DT, MET, VPL><<<grid, threads, smem, st>>>(B);
     }
     static void merge(uint32_t grid, uint32_t threads, size_t smem, const BuildArgs &B, cudaStream_t st)
     {
-        rev_merge_kernel<DT, MET><<<grid, threads, smem, st>>>(B);
+        rev_merge_kernel<DT, MET, VPL><<<grid, threads, smem, st>>>(B);
     }
 };
 
@@ -55,24 +55,32 @@ struct KernelTable {
     void (*merge)(uint32_t, uint32_t, size_t, const BuildArgs &, cudaStream_t);
 };
 
-template <int DT, int MET>
+template <int DT, int MET, int VPL>
 static KernelTable table_of()
 {
-    return {BuildKernels<DT, MET>::setup, BuildKernels<DT, MET>::occ, BuildKernels<DT, MET>::search,
-            BuildKernels<DT, MET>::merge};
+    return {BuildKernels<DT, MET, VPL>::setup, BuildKernels<DT, MET, VPL>::occ, BuildKernels<DT, MET, VPL>::search,
+            BuildKernels<DT, MET, VPL>::merge};
 }
 
-static bool kernel_table(uint32_t dtype, uint32_t metric, KernelTable &t)
+template <int VPL>
+static bool kernel_table_v(uint32_t dtype, uint32_t metric, KernelTable &t)
 {
     const bool l2 = metric == NBPG_L2;
     switch (dtype) {
-    case NBPG_U8: t = l2 ? table_of<DT_U8, M_L2>() : table_of<DT_U8, M_IP>(); return true;
-    case NBPG_I8: t = l2 ? table_of<DT_I8, M_L2>() : table_of<DT_I8, M_IP>(); return true;
+    case NBPG_U8: t = l2 ? table_of<DT_U8, M_L2, VPL>() : table_of<DT_U8, M_IP, VPL>(); return true;
+    case NBPG_I8: t = l2 ? table_of<DT_I8, M_L2, VPL>() : table_of<DT_I8, M_IP, VPL>(); return true;
     case NBPG_U4:
-    case NBPG_I4: t = l2 ? table_of<DT_U4, M_L2>() : table_of<DT_U4, M_IP>(); return true;
+    case NBPG_I4: t = l2 ? table_of<DT_U4, M_L2, VPL>() : table_of<DT_U4, M_IP, VPL>(); return true;
     default: return false;
     }
 }
+
+static bool kernel_table(uint32_t dtype, uint32_t metric, uint32_t vpl, KernelTable &t)
+{
+    return vpl == 1 ? kernel_table_v<1>(dtype, metric, t) : kernel_table_v<4>(dtype, metric, t);
+}
+
+void row_geometry(uint32_t row_stride, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl);
 
 // dfs.h:46-59
 static bool add_edge_if_possible(std::vector<uint32_t> &G, uint32_t R, size_t from, size_t to)
@@ -142,8 +150,11 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
         set_error("dir_bias_scale > 0 is not supported by the GPU build");
         return NBPG_ERR_UNSUPPORTED;
     }
+    uint32_t vecs, lpr, vpl;
+    row_geometry(idx->row_stride, vecs, lpr, vpl);
+    NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");
     KernelTable kt{};
-    NBPG_CHECK_ARG(kernel_table(idx->desc.dtype, idx->desc.metric, kt), "unsupported dtype");
+    NBPG_CHECK_ARG(kernel_table(idx->desc.dtype, idx->desc.metric, vpl, kt), "unsupported dtype");
     cudaStream_t st = idx->stream;
     nbpg_status s;
 
@@ -151,11 +162,9 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     SearchArgs sa{};
     sa.base = idx->d_points;
     sa.row_stride = idx->row_stride;
-    sa.vecs = idx->row_stride / 16;
-    sa.lpr = 1;
-    while (sa.lpr < sa.vecs && sa.lpr < 32) sa.lpr <<= 1;
-    sa.vpl = (sa.vecs + sa.lpr - 1) / sa.lpr;
-    NBPG_CHECK_ARG(sa.vpl <= 2, "rows above 1024 bytes are not supported");
+    sa.vecs = vecs;
+    sa.lpr = lpr;
+    sa.vpl = vpl;
     sa.graph = idx->d_graph;
     sa.gstride = idx->gstride;
     sa.R = R;

@@ -57,18 +57,19 @@ __device__ __forceinline__ float cos_at_p(float d_p_star, float d_p_prime, float
     return __fdiv_rn(num, __fmul_rn(__fmul_rn(2.f, b), c));
 }
 
-__device__ __forceinline__ void load_row_regs(const SearchArgs &a, uint32_t id, uint4 (&qv)[2], int lane)
+template <int VPL>
+__device__ __forceinline__ void load_row_regs(const SearchArgs &a, uint32_t id, uint4 (&qv)[VPL], int lane)
 {
     const uint4 *row = reinterpret_cast<const uint4 *>(a.base + size_t(id) * a.row_stride);
     const uint32_t lq = uint32_t(lane) % a.lpr;
 #pragma unroll
-    for (int v = 0; v < 2; ++v) {
+    for (int v = 0; v < VPL; ++v) {
         const uint32_t c = lq + v * a.lpr;
-        qv[v] = (v < int(a.vpl) && c < a.vecs) ? __ldg(row + c) : make_uint4(0, 0, 0, 0);
+        qv[v] = c < a.vecs ? __ldg(row + c) : make_uint4(0, 0, 0, 0);
     }
 }
 
-template <int DT, int MET>
+template <int DT, int MET, int VPL>
 __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t gslot, int lane)
 {
     const SearchArgs &a = B.s;
@@ -78,7 +79,7 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
     const uint8_t *prow = a.base + size_t(index) * a.row_stride;
 
     // beam search from the start points (beam_search with k = 0, cut = 0)
-    const SearchState st = search_core<DT, MET, true>(a, prow, B.L, 0, VL, B.sp + size_t(t) * B.nsp_per, B.nsp_per,
+    const SearchState st = search_core<DT, MET, true, VPL>(a, prow, B.L, 0, VL, B.sp + size_t(t) * B.nsp_per, B.nsp_per,
                                                       slot, gslot, lane, index);
     uint32_t rp = 0;
 
@@ -88,8 +89,8 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
     uint8_t *alive = slot + lay.off_fl0;
     uint32_t *H = st.H;
 
-    uint4 qv[2];
-    load_row_regs(a, index, qv, lane);
+    uint4 qv[VPL];
+    load_row_regs<VPL>(a, index, qv, lane);
 
     // existing neighbours not seen by the search (nsw.h:150-161); has_been_seen inserts
     const uint32_t *grow = a.graph + size_t(index) * a.gstride;
@@ -115,7 +116,7 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
         nf += __popc(km);
     }
     __syncwarp();
-    warp_row_keys<DT, MET>(a, qv, filt, nf, tmp, lane);
+    warp_row_keys<DT, MET, VPL>(a, qv, filt, nf, tmp, lane);
     rp += nf;
 
     // merge_union of the (unsorted) neighbour list with the sorted visited list, cap VL
@@ -184,11 +185,11 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
             if (lane == 0) pool[sel] = sk;
             ++sel;
             __syncwarp();
-            uint4 pv[2];
-            load_row_regs(a, ps, pv, lane);
+            uint4 pv[VPL];
+            load_row_regs<VPL>(a, ps, pv, lane);
             uint32_t cm = 0;
             for (uint32_t r0 = scan; r0 < np; r0 += rows_per * 4) {
-                uint4 bv[4][2];
+                uint4 bv[4][VPL];
                 uint32_t pos[4];
                 bool live[4];
 #pragma unroll
@@ -197,9 +198,9 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
                     live[p] = pos[p] < np && alive[pos[p]];
                     const uint32_t id = live[p] ? key_id(pool[pos[p]]) : 0u;
 #pragma unroll
-                    for (int v = 0; v < 2; ++v) {
+                    for (int v = 0; v < VPL; ++v) {
                         const uint32_t c = lq + v * lpr;
-                        bv[p][v] = (live[p] && v < int(a.vpl) && c < a.vecs)
+                        bv[p][v] = (live[p] && c < a.vecs)
                                        ? __ldg(reinterpret_cast<const uint4 *>(a.base + size_t(id) * a.row_stride) + c)
                                        : make_uint4(0, 0, 0, 0);
                     }
@@ -208,8 +209,7 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
                 for (int p = 0; p < 4; ++p) {
                     uint32_t acc = 0;
 #pragma unroll
-                    for (int v = 0; v < 2; ++v)
-                        if (v < int(a.vpl)) acc = acc_vec<DT, MET>(bv[p][v], pv[v], acc);
+                    for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], pv[v], acc);
                     for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
                     if (lq == 0 && live[p]) {
                         ++cm;
@@ -244,7 +244,7 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
     __syncwarp();
 }
 
-template <int DT, int MET>
+template <int DT, int MET, int VPL>
 __global__ void __launch_bounds__(512) build_search_prune_kernel(BuildArgs B)
 {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(512) build_search_prune_kernel(BuildArgs B)
         if (lane == 0) w = atomicAdd(B.queue, 1u);
         w = __shfl_sync(kFull, w, 0);
         if (w >= B.bs) break;
-        build_one<DT, MET>(B, w, slot, gslot, lane);
+        build_one<DT, MET, VPL>(B, w, slot, gslot, lane);
     }
 }
 
@@ -306,7 +306,7 @@ __global__ void rev_scatter_kernel(BuildArgs B)
 constexpr uint32_t kMergeCap = 256;  // candidate keys (VL + R <= 256)
 constexpr uint32_t kMergeWarpBytes = kMergeCap * 8 + 128 * 4 + 128 * 8;
 
-template <int DT, int MET>
+template <int DT, int MET, int VPL>
 __global__ void __launch_bounds__(256) rev_merge_kernel(BuildArgs B)
 {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -382,12 +382,12 @@ __global__ void __launch_bounds__(256) rev_merge_kernel(BuildArgs B)
         // middle interpolated (nsw.h:329-355)
         uint32_t rp = 0;
         if (cs > pre) {
-            uint4 qv[2];
-            load_row_regs(a, target, qv, lane);
+            uint4 qv[VPL];
+            load_row_regs<VPL>(a, target, qv, lane);
             const uint32_t end = (pre + B.top_degree) < cs ? pre + B.top_degree : cs;
             const uint32_t nex = end - pre;
-            warp_row_keys<DT, MET>(a, qv, ids, nex, exact, lane);
-            if (end < cs) warp_row_keys<DT, MET>(a, qv, ids + (cs - 1 - pre), 1, exact + nex, lane);  // the last, exact
+            warp_row_keys<DT, MET, VPL>(a, qv, ids, nex, exact, lane);
+            if (end < cs) warp_row_keys<DT, MET, VPL>(a, qv, ids + (cs - 1 - pre), 1, exact + nex, lane);  // the last, exact
             rp = nex + (end < cs ? 1u : 0u);
             for (uint32_t j = pre + lane; j < end; j += 32) cand[j] = exact[j - pre];
             if (end < cs) {

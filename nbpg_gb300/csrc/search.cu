@@ -9,15 +9,25 @@
 
 namespace nbpg {
 
-static const SearchOps *ops_for(uint32_t dtype)
+static const SearchOps *ops_for(uint32_t dtype, uint32_t vpl)
 {
+    const int w = vpl == 1 ? 0 : 1;
     switch (dtype) {
-    case NBPG_U8: return &search_ops_u8;
-    case NBPG_I8: return &search_ops_i8;
+    case NBPG_U8: return &search_ops_u8[w];
+    case NBPG_I8: return &search_ops_i8[w];
     case NBPG_U4:
-    case NBPG_I4: return &search_ops_u4;  // identical arithmetic: i4 codes lose their sign (point.h:27-32)
+    case NBPG_I4: return &search_ops_u4[w];  // identical arithmetic: i4 codes lose their sign (point.h:27-32)
     default: return nullptr;
     }
+}
+
+// Lane geometry of the distance passes: lpr lanes per row (power of two), vpl uint4 per lane.
+void row_geometry(uint32_t row_stride, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl)
+{
+    vecs = row_stride / 16;
+    lpr = 1;
+    while (lpr < vecs && lpr < 32) lpr <<= 1;
+    vpl = vecs <= 32 ? 1 : 4;
 }
 
 SlotLayout make_slot_layout(uint32_t Lmax, uint32_t R, bool vis_smem, uint32_t Vcap, bool hash_smem, uint32_t Scap)
@@ -111,7 +121,10 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
         std::sort(s.begin(), s.end());
         NBPG_CHECK_ARG(std::adjacent_find(s.begin(), s.end()) == s.end(), "start points must be distinct");
     }
-    const SearchOps *ops = ops_for(idx->desc.dtype);
+    uint32_t vecs, lpr, vpl;
+    row_geometry(idx->row_stride, vecs, lpr, vpl);
+    NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");
+    const SearchOps *ops = ops_for(idx->desc.dtype, vpl);
     NBPG_CHECK_ARG(ops, "unsupported dtype");
     if (!st) st = idx->stream;
 
@@ -152,11 +165,9 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
     SearchArgs a{};
     a.base = idx->d_points;
     a.row_stride = idx->row_stride;
-    a.vecs = idx->row_stride / 16;
-    a.lpr = 1;
-    while (a.lpr < a.vecs && a.lpr < 32) a.lpr <<= 1;
-    a.vpl = (a.vecs + a.lpr - 1) / a.lpr;
-    NBPG_CHECK_ARG(a.vpl <= 2, "rows above 1024 bytes are not supported");
+    a.vecs = vecs;
+    a.lpr = lpr;
+    a.vpl = vpl;
     a.graph = idx->d_graph;
     a.gstride = idx->gstride;
     a.R = R;

@@ -3,5 +3,7 @@
 #include "search_ops.h"
 
 namespace nbpg {
-const SearchOps search_ops_i8 = {SearchDispatch<DT_I8>::set_attr, SearchDispatch<DT_I8>::occ, SearchDispatch<DT_I8>::launch};
+const SearchOps search_ops_i8[2] = {
+    {SearchDispatch<DT_I8, 1>::set_attr, SearchDispatch<DT_I8, 1>::occ, SearchDispatch<DT_I8, 1>::launch},
+    {SearchDispatch<DT_I8, 4>::set_attr, SearchDispatch<DT_I8, 4>::occ, SearchDispatch<DT_I8, 4>::launch}};
 }  // namespace nbpg

@@ -42,7 +42,7 @@ struct SearchArgs {
     uint32_t row_stride;  // bytes per device row (multiple of 16)
     uint32_t vecs;        // uint4 per row
     uint32_t lpr;         // lanes per row in distance passes (power of 2)
-    uint32_t vpl;         // uint4 per lane per row (1 or 2)
+    uint32_t vpl;         // uint4 per lane per row (the VPL template argument: 1 or 4)
     const uint32_t *graph;
     uint32_t gstride;  // u32 per graph row
     uint32_t R;
@@ -80,41 +80,67 @@ struct SearchArgs {
 // within the group).  Four row-passes are issued before any arithmetic so their
 // loads are in flight together.  Result keys go to out[0..cnt).
 // ---------------------------------------------------------------------------
-template <int DT, int MET>
-__device__ __forceinline__ void warp_row_keys(const SearchArgs &a, const uint4 (&qv)[2], const uint32_t *ids,
-                                              uint32_t cnt, uint64_t *out, int lane)
+template <int DT, int MET, int VPL, bool FILTER>
+__device__ __forceinline__ uint32_t warp_row_keys_impl(const SearchArgs &a, const uint4 (&qv)[VPL], const uint32_t *ids,
+                                                       uint32_t cnt, uint64_t *out, uint64_t thr, int lane)
 {
     const uint32_t lpr = a.lpr, rows_per = 32u / lpr;
     const uint32_t grp = uint32_t(lane) / lpr, lq = uint32_t(lane) % lpr;
-    constexpr int P = 4;
+    constexpr int P = VPL == 1 ? 4 : 2;
+    uint32_t stored = 0;
     for (uint32_t r0 = 0; r0 < cnt; r0 += rows_per * P) {
-        uint4 bv[P][2];
+        uint4 bv[P][VPL];
         uint32_t id[P];
 #pragma unroll
         for (int p = 0; p < P; ++p) {
             const uint32_t r = r0 + p * rows_per + grp;
             id[p] = r < cnt ? ids[r] : kNoId;
+            const uint4 *row = reinterpret_cast<const uint4 *>(a.base + size_t(id[p]) * a.row_stride);
 #pragma unroll
-            for (int v = 0; v < 2; ++v) {
+            for (int v = 0; v < VPL; ++v) {
                 const uint32_t c = lq + v * lpr;
-                if (r < cnt && v < int(a.vpl) && c < a.vecs)
-                    bv[p][v] = __ldg(reinterpret_cast<const uint4 *>(a.base + size_t(id[p]) * a.row_stride) + c);
-                else
-                    bv[p][v] = make_uint4(0, 0, 0, 0);
+                bv[p][v] = (r < cnt && c < a.vecs) ? __ldg(row + c) : make_uint4(0, 0, 0, 0);
             }
         }
 #pragma unroll
         for (int p = 0; p < P; ++p) {
             uint32_t acc = 0;
 #pragma unroll
-            for (int v = 0; v < 2; ++v)
-                if (v < int(a.vpl)) acc = acc_vec<DT, MET>(bv[p][v], qv[v], acc);
+            for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], qv[v], acc);
             for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
             const uint32_t r = r0 + p * rows_per + grp;
-            if (lq == 0 && r < cnt) out[r] = make_key(finish_dist<DT, MET>(acc), id[p]);
+            const uint64_t key = make_key(finish_dist<DT, MET>(acc), id[p]);
+            if constexpr (FILTER) {
+                const bool keep = lq == 0 && r < cnt && key < thr;
+                const unsigned m = __ballot_sync(kFull, keep);
+                if (keep) out[stored + __popc(m & lanemask_lt())] = key;
+                stored += __popc(m);
+            } else {
+                if (lq == 0 && r < cnt) out[r] = key;
+            }
         }
     }
     __syncwarp();
+    return FILTER ? stored : cnt;
+}
+
+// Distances of `cnt` rows (ids[0..cnt)) to the query held in registers; keys to out[0..cnt).
+// Lanes are grouped lpr per row; each lane loads VPL uint4 (16-byte, coalesced within
+// the group), several row-passes in flight before any arithmetic.
+template <int DT, int MET, int VPL>
+__device__ __forceinline__ void warp_row_keys(const SearchArgs &a, const uint4 (&qv)[VPL], const uint32_t *ids,
+                                              uint32_t cnt, uint64_t *out, int lane)
+{
+    warp_row_keys_impl<DT, MET, VPL, false>(a, qv, ids, cnt, out, 0, lane);
+}
+
+// As warp_row_keys, but stores (compacted, any order) only keys below thr; returns how many.
+template <int DT, int MET, int VPL>
+__device__ __forceinline__ uint32_t warp_row_keys_below(const SearchArgs &a, const uint4 (&qv)[VPL],
+                                                        const uint32_t *ids, uint32_t cnt, uint64_t *out, uint64_t thr,
+                                                        int lane)
+{
+    return warp_row_keys_impl<DT, MET, VPL, true>(a, qv, ids, cnt, out, thr, lane);
 }
 
 // Sort keys[0..cnt) (cnt <= 256) in place, ascending.
@@ -137,13 +163,18 @@ __device__ __forceinline__ void sort_keys_kpl(uint64_t *keys, uint32_t cnt, int 
     __syncwarp();
 }
 
+static __device__ __noinline__ void sort_keys_large(uint64_t *keys, uint32_t cnt, int lane)
+{
+    if (cnt <= 128) sort_keys_kpl<4>(keys, cnt, lane);
+    else sort_keys_kpl<8>(keys, cnt, lane);
+}
+
 __device__ __forceinline__ void sort_keys(uint64_t *keys, uint32_t cnt, int lane)
 {
     if (cnt <= 1) return;
     if (cnt <= 32) sort_keys_kpl<1>(keys, cnt, lane);
     else if (cnt <= 64) sort_keys_kpl<2>(keys, cnt, lane);
-    else if (cnt <= 128) sort_keys_kpl<4>(keys, cnt, lane);
-    else sort_keys_kpl<8>(keys, cnt, lane);
+    else sort_keys_large(keys, cnt, lane);
 }
 
 // number of elements of sorted s[0..n) that are < key
@@ -215,7 +246,7 @@ struct SearchState {
     __device__ uint64_t *frontier() const { return b ? fr1 : fr0; }
 };
 
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_bytes, uint32_t L, uint32_t k,
                                    uint64_t max_visited, const uint32_t *sp, uint32_t nsp, uint8_t *slot,
                                    uint32_t gslot, int lane, uint32_t self)
@@ -227,8 +258,10 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     st.smask = smask;
     st.fr0 = reinterpret_cast<uint64_t *>(slot + lay.off_fr0);
     st.fr1 = reinterpret_cast<uint64_t *>(slot + lay.off_fr1);
-    uint64_t *fr[2] = {reinterpret_cast<uint64_t *>(slot + lay.off_fr0), reinterpret_cast<uint64_t *>(slot + lay.off_fr1)};
-    uint8_t *fl[2] = {slot + lay.off_fl0, slot + lay.off_fl1};
+    uint64_t *const fr0 = reinterpret_cast<uint64_t *>(slot + lay.off_fr0);
+    uint64_t *const fr1 = reinterpret_cast<uint64_t *>(slot + lay.off_fr1);
+    uint8_t *const fl0 = slot + lay.off_fl0;
+    uint8_t *const fl1 = slot + lay.off_fl1;
     uint64_t *cand = reinterpret_cast<uint64_t *>(slot + lay.off_cand);
     uint16_t *unv = reinterpret_cast<uint16_t *>(slot + lay.off_unv);
     uint32_t *filt = reinterpret_cast<uint32_t *>(slot + lay.off_filt);
@@ -240,14 +273,14 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     st.H = H;
 
     // query vector in registers: this lane's 16-byte pieces of the row
-    uint4 qv[2];
+    uint4 qv[VPL];
     {
         const uint4 *qrow = reinterpret_cast<const uint4 *>(qrow_bytes);
         const uint32_t lq = uint32_t(lane) % a.lpr;
 #pragma unroll
-        for (int v = 0; v < 2; ++v) {
+        for (int v = 0; v < VPL; ++v) {
             const uint32_t c = lq + v * a.lpr;
-            qv[v] = (v < int(a.vpl) && c < a.vecs) ? qrow[c] : make_uint4(0, 0, 0, 0);
+            qv[v] = c < a.vecs ? qrow[c] : make_uint4(0, 0, 0, 0);
         }
     }
 
@@ -256,16 +289,16 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     __syncwarp();
 
     // init_starting_points (query_params.h:204-221)
-    warp_row_keys<DT, MET>(a, qv, sp, nsp, fr[0], lane);
+    warp_row_keys<DT, MET, VPL>(a, qv, sp, nsp, fr0, lane);
     if (lane == 0)
         for (uint32_t s = 0; s < nsp; ++s) {
             const uint32_t v = sp[s];
             H[filter_slot(v, smask)] = v;
         }
     __syncwarp();
-    sort_keys(fr[0], nsp, lane);
+    sort_keys(fr0, nsp, lane);
     for (uint32_t i = lane; i < nsp; i += 32) {
-        fl[0][i] = 0;
+        fl0[i] = 0;
         unv[i] = uint16_t(i);
     }
     __syncwarp();
@@ -280,9 +313,16 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     const uint32_t R = a.R;
     const uint32_t nchunks = (R + 31) / 32;
 
+    // candidates stored (cst) vs appended (cs, which drives the deferral rule): while the
+    // frontier is full, a candidate at or beyond its last key can never survive the
+    // union's truncation to L, so it is counted but not stored.
+    uint32_t cst = 0;
+    uint64_t tail = fs == L ? fr0[L - 1] : kKeyMax;
     while (remain > offset && nvis < a.limit) {
+        uint64_t *const frb = b ? fr1 : fr0;
+        uint8_t *const flb = b ? fl1 : fl0;
         const uint32_t pos = unv[offset];
-        const uint64_t ck = fr[b][pos];
+        const uint64_t ck = frb[pos];
         const uint32_t cid = key_id(ck);
         const uint32_t *grow = a.graph + size_t(cid) * a.gstride;
 
@@ -298,7 +338,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         if (a.prefetch && lane < int(a.prefetch) * 3) {
             const uint32_t p = offset + 1 + lane / 3;
             if (p < remain && uint32_t(lane % 3) * 32 < a.gstride) {
-                const uint32_t nid = key_id(fr[b][unv[p]]);
+                const uint32_t nid = key_id(frb[unv[p]]);
                 prefetch_l2(a.graph + size_t(nid) * a.gstride + (lane % 3) * 32);
             }
         }
@@ -330,7 +370,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         __syncwarp();
 
         // distances of the new neighbours -> candidates (beamSearch.h:85-93)
-        warp_row_keys<DT, MET>(a, qv, filt, nf, cand + cs, lane);
+        cst += warp_row_keys_below<DT, MET, VPL>(a, qv, filt, nf, cand + cst, tail, lane);
         cs += nf;
         cmps += nf;
 
@@ -355,7 +395,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             vs = nvs;
             __syncwarp();
         } else {
-            if (lane == 0) fl[b][pos] = 1;
+            if (lane == 0) flb[pos] = 1;
             if (nvis > max_visited) taint = true;
             __syncwarp();
         }
@@ -368,37 +408,39 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         offset = 0;
 
         // sort + unique candidates, set_union with the frontier, truncate to L (beamSearch.h:128-138)
-        const uint32_t cu = sort_unique_minus(cand, cs, fr[b], fs, lane);
+        const uint32_t cu = sort_unique_minus(cand, cst, frb, fs, lane);
         const int nb2 = b ^ 1;
+        uint64_t *const frn = nb2 ? fr1 : fr0;
+        uint8_t *const fln = nb2 ? fl1 : fl0;
         const uint32_t U = fs + cu;
         const uint32_t n0 = U < L ? U : L;
         for (uint32_t i = lane; i < fs; i += 32) {
-            const uint64_t key = fr[b][i];
+            const uint64_t key = frb[i];
             const uint32_t p = i + lower_count(cand, cu, key);
             if (p < n0) {
-                fr[nb2][p] = key;
-                fl[nb2][p] = fl[b][i];
+                frn[p] = key;
+                fln[p] = flb[i];
             }
         }
         for (uint32_t j = lane; j < cu; j += 32) {
             const uint64_t key = cand[j];
-            const uint32_t p = j + lower_count(fr[b], fs, key);
+            const uint32_t p = j + lower_count(frb, fs, key);
             if (p < n0) {
-                fr[nb2][p] = key;
-                fl[nb2][p] = 0;
+                frn[p] = key;
+                fln[p] = 0;
             }
         }
         __syncwarp();
         uint32_t nfs = n0;
         // cut rule (beamSearch.h:140-149): threshold = float(cut * d_k), upper_bound of (0, thr)
         if (k > 0 && n0 > k) {
-            const float thr = __double2float_rn(a.cut * double(key_dist(fr[nb2][k])));
+            const float thr = __double2float_rn(a.cut * double(key_dist(frn[k])));
             uint32_t ub = 0;
             for (uint32_t base = 0; base < n0; base += 32) {
                 const uint32_t i = base + lane;
                 bool pr = false;
                 if (i < n0) {
-                    const uint64_t key = fr[nb2][i];
+                    const uint64_t key = frn[i];
                     const float d = key_dist(key);
                     pr = d < thr || (d == thr && key_id(key) == 0);
                 }
@@ -410,6 +452,8 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         b = nb2;
         fs = nfs;
         cs = 0;
+        cst = 0;
+        tail = fs == L ? frn[L - 1] : kKeyMax;
 
         // frontier \ visited -> unvisited (beamSearch.h:154-160)
         remain = 0;
@@ -417,8 +461,8 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             const uint32_t i = base + lane;
             bool un = false;
             if (i < fs) {
-                if constexpr (LIST) un = !contains(vis, vs, fr[b][i]);
-                else un = fl[b][i] == 0;
+                if constexpr (LIST) un = !contains(vis, vs, frn[i]);
+                else un = fln[i] == 0;
             }
             const unsigned m = __ballot_sync(kFull, un);
             if (un) unv[remain + __popc(m & lanemask_lt())] = uint16_t(i);
@@ -437,7 +481,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
 }
 
 // One query of a search request: argument checks, search_core, outputs.
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, uint32_t gslot, int lane)
 {
     const uint32_t L = a.Ls ? a.Ls[qi] : a.L_all;
@@ -462,7 +506,7 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
         return;
     }
 
-    const SearchState st = search_core<DT, MET, LIST>(a, a.queries + size_t(qi) * a.row_stride, L, k, max_visited,
+    const SearchState st = search_core<DT, MET, LIST, VPL>(a, a.queries + size_t(qi) * a.row_stride, L, k, max_visited,
                                                       a.sp, a.nsp, slot, gslot, lane, kNoId);
     const uint64_t *frb = st.frontier();
     const uint32_t fs = st.fs;
@@ -498,7 +542,7 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
 }
 
 // Persistent form: warps pull queries from a device queue until it runs dry.
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 __global__ void __launch_bounds__(512) search_batched_kernel(SearchArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -512,19 +556,19 @@ __global__ void __launch_bounds__(512) search_batched_kernel(SearchArgs a)
         w = __shfl_sync(kFull, w, 0);
         if (w >= total) break;
         const uint32_t qi = a.only ? a.only[1 + w] : (a.order ? a.order[w] : w);
-        search_query<DT, MET, LIST>(a, qi, slot, gslot, lane);
+        search_query<DT, MET, LIST, VPL>(a, qi, slot, gslot, lane);
     }
 }
 
 // Plain form: one query per thread block of one warp; everything in shared memory.
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 __global__ void __launch_bounds__(32) search_plain_kernel(SearchArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t total = a.only ? a.only[0] : a.nq;
     if (blockIdx.x >= total) return;
     const uint32_t qi = a.only ? a.only[1 + blockIdx.x] : blockIdx.x;
-    search_query<DT, MET, LIST>(a, qi, smem, blockIdx.x, threadIdx.x);
+    search_query<DT, MET, LIST, VPL>(a, qi, smem, blockIdx.x, threadIdx.x);
 }
 
 }  // namespace nbpg

@@ -18,53 +18,56 @@ struct LaunchPlan {
     bool ghash_main, ghash_list, gvis_list;
 };
 
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 inline cudaError_t set_smem_attr(bool plain, size_t smem)
 {
     if (plain)
-        return cudaFuncSetAttribute(search_plain_kernel<DT, MET, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        return cudaFuncSetAttribute(search_plain_kernel<DT, MET, LIST, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(smem));
-    return cudaFuncSetAttribute(search_batched_kernel<DT, MET, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(search_batched_kernel<DT, MET, LIST, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem));
 }
 
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 inline cudaError_t occupancy(bool plain, uint32_t threads, size_t smem, int *blocks)
 {
-    if (plain) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, search_plain_kernel<DT, MET, LIST>, int(threads), smem);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, search_batched_kernel<DT, MET, LIST>, int(threads), smem);
+    if (plain) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, search_plain_kernel<DT, MET, LIST, VPL>, int(threads), smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, search_batched_kernel<DT, MET, LIST, VPL>, int(threads), smem);
 }
 
-template <int DT, int MET, bool LIST>
+template <int DT, int MET, bool LIST, int VPL>
 inline void launch_one(bool plain, uint32_t grid, uint32_t warps, size_t smem, const SearchArgs &a, cudaStream_t st)
 {
-    if (plain) search_plain_kernel<DT, MET, LIST><<<grid, 32, smem, st>>>(a);
-    else search_batched_kernel<DT, MET, LIST><<<grid, warps * 32, smem, st>>>(a);
+    if (plain) search_plain_kernel<DT, MET, LIST, VPL><<<grid, 32, smem, st>>>(a);
+    else search_batched_kernel<DT, MET, LIST, VPL><<<grid, warps * 32, smem, st>>>(a);
 }
 
-// Dispatch on (metric, mode) for one element type.
-template <int DT>
+// Dispatch on (metric, mode) for one element type and lane width.
+template <int DT, int VPL>
 struct SearchDispatch {
     static cudaError_t set_attr(int metric, bool list, bool plain, size_t smem)
     {
-        if (metric == M_L2) return list ? set_smem_attr<DT, M_L2, true>(plain, smem) : set_smem_attr<DT, M_L2, false>(plain, smem);
-        return list ? set_smem_attr<DT, M_IP, true>(plain, smem) : set_smem_attr<DT, M_IP, false>(plain, smem);
+        if (metric == M_L2)
+            return list ? set_smem_attr<DT, M_L2, true, VPL>(plain, smem) : set_smem_attr<DT, M_L2, false, VPL>(plain, smem);
+        return list ? set_smem_attr<DT, M_IP, true, VPL>(plain, smem) : set_smem_attr<DT, M_IP, false, VPL>(plain, smem);
     }
     static cudaError_t occ(int metric, bool list, bool plain, uint32_t threads, size_t smem, int *blocks)
     {
         if (metric == M_L2)
-            return list ? occupancy<DT, M_L2, true>(plain, threads, smem, blocks) : occupancy<DT, M_L2, false>(plain, threads, smem, blocks);
-        return list ? occupancy<DT, M_IP, true>(plain, threads, smem, blocks) : occupancy<DT, M_IP, false>(plain, threads, smem, blocks);
+            return list ? occupancy<DT, M_L2, true, VPL>(plain, threads, smem, blocks)
+                        : occupancy<DT, M_L2, false, VPL>(plain, threads, smem, blocks);
+        return list ? occupancy<DT, M_IP, true, VPL>(plain, threads, smem, blocks)
+                    : occupancy<DT, M_IP, false, VPL>(plain, threads, smem, blocks);
     }
     static void launch(int metric, bool list, bool plain, uint32_t grid, uint32_t warps, size_t smem,
                        const SearchArgs &a, cudaStream_t st)
     {
         if (metric == M_L2) {
-            if (list) launch_one<DT, M_L2, true>(plain, grid, warps, smem, a, st);
-            else launch_one<DT, M_L2, false>(plain, grid, warps, smem, a, st);
+            if (list) launch_one<DT, M_L2, true, VPL>(plain, grid, warps, smem, a, st);
+            else launch_one<DT, M_L2, false, VPL>(plain, grid, warps, smem, a, st);
         } else {
-            if (list) launch_one<DT, M_IP, true>(plain, grid, warps, smem, a, st);
-            else launch_one<DT, M_IP, false>(plain, grid, warps, smem, a, st);
+            if (list) launch_one<DT, M_IP, true, VPL>(plain, grid, warps, smem, a, st);
+            else launch_one<DT, M_IP, false, VPL>(plain, grid, warps, smem, a, st);
         }
     }
 };

@@ -12,6 +12,7 @@ struct SearchOps {
                    cudaStream_t st);
 };
 
-extern const SearchOps search_ops_u8, search_ops_i8, search_ops_u4;
+// [element type][lane width: 0 -> 1 uint4, 1 -> 4 uint4]
+extern const SearchOps search_ops_u8[2], search_ops_i8[2], search_ops_u4[2];
 
 }  // namespace nbpg

@@ -3,5 +3,7 @@
 #include "search_ops.h"
 
 namespace nbpg {
-const SearchOps search_ops_u4 = {SearchDispatch<DT_U4>::set_attr, SearchDispatch<DT_U4>::occ, SearchDispatch<DT_U4>::launch};
+const SearchOps search_ops_u4[2] = {
+    {SearchDispatch<DT_U4, 1>::set_attr, SearchDispatch<DT_U4, 1>::occ, SearchDispatch<DT_U4, 1>::launch},
+    {SearchDispatch<DT_U4, 4>::set_attr, SearchDispatch<DT_U4, 4>::occ, SearchDispatch<DT_U4, 4>::launch}};
 }  // namespace nbpg

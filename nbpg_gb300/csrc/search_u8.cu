@@ -3,5 +3,7 @@
 #include "search_ops.h"
 
 namespace nbpg {
-const SearchOps search_ops_u8 = {SearchDispatch<DT_U8>::set_attr, SearchDispatch<DT_U8>::occ, SearchDispatch<DT_U8>::launch};
+const SearchOps search_ops_u8[2] = {
+    {SearchDispatch<DT_U8, 1>::set_attr, SearchDispatch<DT_U8, 1>::occ, SearchDispatch<DT_U8, 1>::launch},
+    {SearchDispatch<DT_U8, 4>::set_attr, SearchDispatch<DT_U8, 4>::occ, SearchDispatch<DT_U8, 4>::launch}};
 }  // namespace nbpg
