@@ -208,9 +208,12 @@ def profile_search(idx, q, L, args):
     o_m = torch.empty(nq, dtype=torch.int32, device="cuda")
     stream = torch.cuda.Stream()
     qp = QueryParams(k=k, beamSize=L, cut=CFG["cut"])
+    from nbpg_gb300.index import LaunchConfig
+    launch = LaunchConfig(kernel=args.kernel, warps_per_cta=args.warps, lane_width=args.lane_width,
+                          prefetch=args.prefetch)
     for i in range(args.warmup + args.steps):
         idx.search_device(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, None, None, o_v.data_ptr(), o_m.data_ptr(),
-                          stream=stream.cuda_stream)
+                          stream=stream.cuda_stream, launch=launch)
     torch.cuda.synchronize()
     v, m = o_v.cpu().numpy(), o_m.cpu().numpy()
     print(json.dumps({"profile": "batched search", "L": L, "nq": nq, "launches": 2 * (args.warmup + args.steps),
@@ -229,6 +232,10 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: index + --L, then warmup + steps of the batched search only")
     ap.add_argument("--L", type=int, default=0, help="beam width for --profile (default: the sweep's choice)")
+    ap.add_argument("--kernel", default="batched", choices=["batched", "plain"], help="--profile launch")
+    ap.add_argument("--warps", type=int, default=0, help="--profile launch: warps per CTA")
+    ap.add_argument("--lane-width", type=int, default=0, help="--profile launch: 16-byte words per lane per row")
+    ap.add_argument("--prefetch", type=int, default=-1, help="--profile launch: prefetched adjacency rows")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -308,9 +315,24 @@ def main():
     assert stream.cuda_stream != 0
     qp = QueryParams(k=k, beamSize=L_op, cut=CFG["cut"])
 
-    def dev_search(kernel="batched"):
+    from nbpg_gb300.index import LaunchConfig
+    tuned, tuned_ms = idx.autotune(qdev.data_ptr(), nq, qp)
+    log(f"[bench] autotuned launch: {tuned} ({tuned_ms:.3f} ms per launch)")
+
+    def dev_search(launch=tuned):
         idx.search_device(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, o_d.data_ptr(), o_c.data_ptr(),
-                          o_v.data_ptr(), o_m.data_ptr(), kernel=kernel, stream=stream.cuda_stream)
+                          o_v.data_ptr(), o_m.data_ptr(), launch=launch, stream=stream.cuda_stream)
+
+    def time_launch(launch, reps=20):
+        for _ in range(3):
+            dev_search(launch)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in ev:
+            e0.record(stream)
+            dev_search(launch)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return nq * reps / (sum(a.elapsed_time(b) for a, b in ev) / 1e3)
 
     for _ in range(args.warmup):
         dev_search()
@@ -341,18 +363,12 @@ def main():
     value = world * nq * args.steps / total_s
     ms_step = 1e3 * total_s / args.steps
 
-    # plain one-query-per-block kernel at the same L
-    for _ in range(2):
-        dev_search("plain")
-    torch.cuda.synchronize()
-    pe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
-    for e0, e1 in pe:
-        e0.record(stream)
-        dev_search("plain")
-        e1.record(stream)
-    torch.cuda.synchronize()
-    plain_qps = nq * len(pe) / (sum(a.elapsed_time(b) for a, b in pe) / 1e3)
+    # the two kernel forms at the same L: plain (one query per block, default launch) and
+    # the batched persistent kernel with its default launch
+    plain_qps = time_launch(LaunchConfig(kernel="plain"))
     assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "plain kernel results differ"
+    batched_default_qps = time_launch(LaunchConfig(kernel="batched"))
+    assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "batched kernel results differ"
 
     # e2e through the C ABI: pinned host queries in, host results out, every step
     L = _lib.lib()
@@ -360,7 +376,7 @@ def main():
     oh_ids = torch.empty((nq, k), dtype=torch.int32).pin_memory()
     oh_d = torch.empty((nq, k), dtype=torch.float32).pin_memory()
     oh_c, oh_v, oh_m = (torch.empty(nq, dtype=torch.int32).pin_memory() for _ in range(3))
-    prm = _lib.SearchParams(k, L_op, CFG["cut"], 0, 0, 8, 0, 0)
+    prm = tuned.params(qp)
     sp = (C.c_uint32 * 1)(0)
     u32p = C.POINTER(C.c_uint32)
 
@@ -403,12 +419,16 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded 1000-centre u8 Gaussian mixture standing in for SIFT1M)",
-            "config": {"workload": "NBPG 1M x 128 u8 search, 10k queries, k=10, batched persistent kernel",
+            "config": {"workload": "NBPG 1M x 128 u8 search, 10k queries, k=10, autotuned strict search launch",
                        "n_base": CFG["n"], "n_query": nq, "R": CFG["R"], "build": "L=100 VL=140 passes=2 split=4 "
                        "dynamic_prune min_alpha=1.05 max_alpha=1.1 (GPU build)", "L": L_op, "cut": CFG["cut"],
                        "recall@10": round(rec, 4), "recall@10_exact_gt": round(rec_exact, 4),
                        "l2_policy": "index (400 MB) larger than L2; no flush",
-                       "plain_kernel_qps": plain_qps, "batched_over_plain": value / plain_qps,
+                       "launch": {"kernel": tuned.kernel, "warps_per_cta": tuned.warps_per_cta,
+                                  "lane_width": tuned.lane_width, "prefetch": tuned.prefetch,
+                                  "chosen_by": "nbpg_search_autotune"},
+                       "plain_kernel_qps": plain_qps, "batched_default_qps": batched_default_qps,
+                       "tuned_over_plain": value / plain_qps,
                        "build_s": None if build_s is None else round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
                        "L_sweep": sweep, "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

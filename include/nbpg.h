@@ -98,7 +98,11 @@ typedef struct nbpg_search_params {
     uint32_t degree_limit;   /* QueryParams::degree_limit; 0 = R */
     uint32_t visited_factor; /* visited list cap = factor * L; 0 = 8 (beamSearch.h:276-280) */
     uint32_t kernel;         /* nbpg_kernel */
-    uint32_t warps_per_cta;  /* batched kernel CTA size in warps; 0 = autotuned */
+    uint32_t warps_per_cta;  /* batched kernel CTA size in warps; 0 = default */
+    uint32_t lane_width;     /* 16-byte words each lane loads per vector row: 1, 2 or 4
+                                (lanes per row = row words / lane_width); 0 = default */
+    int32_t prefetch;        /* adjacency rows of upcoming frontier entries prefetched to L2
+                                per expansion (batched kernel); -1 = default */
 } nbpg_search_params;
 
 /* Per-query outputs, k_stride entries per query row: ids (UINT32_MAX padding),
@@ -119,6 +123,16 @@ nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t 
                                const uint32_t *d_Ls, const uint32_t *d_ks, const uint32_t *start_points,
                                uint32_t n_start, uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
                                uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps, void *stream);
+
+/* Autotuner for the search launch: times CTA size x lane width x prefetch for the
+ * batched kernel, and the plain kernel, on the caller's device-resident queries with
+ * the caller's (L, k), and writes the fastest configuration into *tuned (a copy of
+ * *params with kernel, warps_per_cta, lane_width and prefetch filled in).  Results of
+ * every configuration are identical; only speed differs.  best_ms (may be NULL)
+ * receives the best time per launch.  Project-written; no vendor tuner involved. */
+nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                 const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
+                                 nbpg_search_params *tuned, float *best_ms);
 
 /* Device pointer of the index's packed base rows (row stride = nbpg_index_row_stride
  * bytes) and of its graph rows (nbpg_index_graph_stride u32 per node). */

@@ -33,7 +33,7 @@ class IndexDesc(C.Structure):
 class SearchParams(C.Structure):
     _fields_ = [("k", C.c_uint32), ("L", C.c_uint32), ("cut", C.c_double), ("limit", C.c_uint64),
                 ("degree_limit", C.c_uint32), ("visited_factor", C.c_uint32), ("kernel", C.c_uint32),
-                ("warps_per_cta", C.c_uint32)]
+                ("warps_per_cta", C.c_uint32), ("lane_width", C.c_uint32), ("prefetch", C.c_int32)]
 
 
 class BuildParams(C.Structure):
@@ -79,6 +79,8 @@ def lib() -> C.CDLL:
                               C.c_uint32, _u32p, _f32p, _u32p, _u32p, _u32p]
     L.nbpg_search_device.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _vp, _vp, _u32p, C.c_uint32,
                                      C.c_uint32, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.nbpg_search_autotune.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _u32p, C.c_uint32,
+                                       C.POINTER(SearchParams), C.POINTER(C.c_float)]
     L.nbpg_gt.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
                           C.c_uint32, _u32p, _f32p, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]

@@ -80,7 +80,7 @@ static bool kernel_table(uint32_t dtype, uint32_t metric, uint32_t vpl, KernelTa
     return vpl == 1 ? kernel_table_v<1>(dtype, metric, t) : kernel_table_v<4>(dtype, metric, t);
 }
 
-void row_geometry(uint32_t row_stride, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl);
+void row_geometry(uint32_t row_stride, uint32_t want, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl);
 
 // dfs.h:46-59
 static bool add_edge_if_possible(std::vector<uint32_t> &G, uint32_t R, size_t from, size_t to)
@@ -151,7 +151,7 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
         return NBPG_ERR_UNSUPPORTED;
     }
     uint32_t vecs, lpr, vpl;
-    row_geometry(idx->row_stride, vecs, lpr, vpl);
+    row_geometry(idx->row_stride, 0, vecs, lpr, vpl);
     NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");
     KernelTable kt{};
     NBPG_CHECK_ARG(kernel_table(idx->desc.dtype, idx->desc.metric, vpl, kt), "unsupported dtype");

@@ -30,6 +30,14 @@ __device__ __forceinline__ float ord2f(uint32_t o)
     return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
 }
 __device__ __forceinline__ uint64_t make_key(float d, uint32_t id) { return (uint64_t(f2ord(d)) << 32) | id; }
+// Key of a distance known to be a non-negative float (squared L2 of integer codes,
+// never -0): the order image is just the bits with the sign bit set.
+template <int MET>
+__device__ __forceinline__ uint64_t make_dist_key(float d, uint32_t id)
+{
+    if constexpr (MET == 0) return (uint64_t(__float_as_uint(d) | 0x80000000u) << 32) | id;
+    else return make_key(d, id);
+}
 __device__ __forceinline__ uint32_t key_id(uint64_t k) { return uint32_t(k); }
 __device__ __forceinline__ float key_dist(uint64_t k) { return ord2f(uint32_t(k >> 32)); }
 

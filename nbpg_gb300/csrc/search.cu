@@ -11,23 +11,29 @@ namespace nbpg {
 
 static const SearchOps *ops_for(uint32_t dtype, uint32_t vpl)
 {
-    const int w = vpl == 1 ? 0 : 1;
+#define NBPG_PICK(t) return vpl == 1 ? &search_ops_##t##_v1 : vpl == 2 ? &search_ops_##t##_v2 : &search_ops_##t##_v4
     switch (dtype) {
-    case NBPG_U8: return &search_ops_u8[w];
-    case NBPG_I8: return &search_ops_i8[w];
+    case NBPG_U8: NBPG_PICK(u8);
+    case NBPG_I8: NBPG_PICK(i8);
     case NBPG_U4:
-    case NBPG_I4: return &search_ops_u4[w];  // identical arithmetic: i4 codes lose their sign (point.h:27-32)
+    case NBPG_I4: NBPG_PICK(u4);  // identical arithmetic: i4 codes lose their sign (point.h:27-32)
     default: return nullptr;
     }
+#undef NBPG_PICK
 }
 
-// Lane geometry of the distance passes: lpr lanes per row (power of two), vpl uint4 per lane.
-void row_geometry(uint32_t row_stride, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl)
+// Lane geometry of the distance passes: vpl uint4 per lane (1, 2 or 4), lpr lanes per
+// row (a power of two, lpr * vpl >= row words).  want = 0 picks 1 for rows up to 512
+// bytes and 4 above; an unusable request falls back to that default.
+void row_geometry(uint32_t row_stride, uint32_t want, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl)
 {
     vecs = row_stride / 16;
-    lpr = 1;
-    while (lpr < vecs && lpr < 32) lpr <<= 1;
     vpl = vecs <= 32 ? 1 : 4;
+    if ((want == 2 || want == 4) && want <= vecs && (vecs + want - 1) / want <= 32) vpl = want;
+    if (want == 1 && vecs <= 32) vpl = 1;
+    const uint32_t need = (vecs + vpl - 1) / vpl;
+    lpr = 1;
+    while (lpr < need) lpr <<= 1;
 }
 
 SlotLayout make_slot_layout(uint32_t Lmax, uint32_t R, bool vis_smem, uint32_t Vcap, bool hash_smem, uint32_t Scap)
@@ -122,7 +128,7 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
         NBPG_CHECK_ARG(std::adjacent_find(s.begin(), s.end()) == s.end(), "start points must be distinct");
     }
     uint32_t vecs, lpr, vpl;
-    row_geometry(idx->row_stride, vecs, lpr, vpl);
+    row_geometry(idx->row_stride, P->lane_width, vecs, lpr, vpl);
     NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");
     const SearchOps *ops = ops_for(idx->desc.dtype, vpl);
     NBPG_CHECK_ARG(ops, "unsupported dtype");
@@ -191,7 +197,7 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
     a.out_visited = d_visited;
     a.out_cmps = d_cmps;
     a.err = q + 2;
-    a.prefetch = plain ? 0 : 2;
+    a.prefetch = plain ? 0 : (P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u));
 
     // main pass
     SearchArgs m = a;
@@ -296,5 +302,74 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
         set_error("a query was rejected on the device (k > L or L above the planned maximum)");
         return NBPG_ERR_INVALID_ARG;
     }
+    return NBPG_OK;
+}
+
+// Search-launch autotuner: every candidate configuration gives identical results, so
+// the fastest one on the caller's own queries wins.
+extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                            const nbpg_search_params *params, const uint32_t *start_points,
+                                            uint32_t n_start, nbpg_search_params *tuned, float *best_ms)
+{
+    if (!idx || !params || !tuned || !d_queries || nq == 0) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(idx->mu);
+    NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
+    const uint32_t k = params->k;
+    uint32_t *d_ids = nullptr;
+    NBPG_CUDA_TRY(cudaMalloc(&d_ids, size_t(nq) * std::max<uint32_t>(k, 1) * 4));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaStream_t st = idx->stream;
+
+    std::vector<uint32_t> widths;
+    for (uint32_t w : {1u, 2u, 4u}) {
+        uint32_t vecs, lpr, vpl;
+        row_geometry(idx->row_stride, w, vecs, lpr, vpl);
+        if (std::find(widths.begin(), widths.end(), vpl) == widths.end()) widths.push_back(vpl);
+    }
+    std::vector<nbpg_search_params> cands;
+    for (uint32_t w : widths) {
+        nbpg_search_params p = *params;
+        p.kernel = NBPG_KERNEL_PLAIN;
+        p.lane_width = w;
+        p.warps_per_cta = 0;
+        p.prefetch = 0;
+        cands.push_back(p);
+        for (uint32_t warps : {4u, 8u, 16u})
+            for (int pf : {0, 2}) {
+                p.kernel = NBPG_KERNEL_BATCHED;
+                p.warps_per_cta = warps;
+                p.prefetch = pf;
+                cands.push_back(p);
+            }
+    }
+    float best = 1e30f;
+    nbpg_status s = NBPG_OK;
+    nbpg_search_params win = *params;
+    for (const auto &p : cands) {
+        float t = 1e30f;
+        for (int rep = 0; rep < 3 && s == NBPG_OK; ++rep) {
+            if (rep > 0) cudaEventRecord(e0, st);
+            s = search_device_impl(idx, d_queries, nq, &p, nullptr, nullptr, start_points, n_start, k, d_ids, nullptr,
+                                   nullptr, nullptr, nullptr, st);
+            if (rep > 0) {
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                t = std::min(t, ms);
+            }
+        }
+        if (s != NBPG_OK) break;
+        if (t < best) { best = t; win = p; }
+    }
+    cudaStreamSynchronize(st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d_ids);
+    if (s != NBPG_OK) return s;
+    *tuned = win;
+    if (best_ms) *best_ms = best;
     return NBPG_OK;
 }

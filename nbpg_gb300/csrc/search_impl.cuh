@@ -42,7 +42,7 @@ struct SearchArgs {
     uint32_t row_stride;  // bytes per device row (multiple of 16)
     uint32_t vecs;        // uint4 per row
     uint32_t lpr;         // lanes per row in distance passes (power of 2)
-    uint32_t vpl;         // uint4 per lane per row (the VPL template argument: 1 or 4)
+    uint32_t vpl;         // uint4 per lane per row (the VPL template argument: 1, 2 or 4)
     const uint32_t *graph;
     uint32_t gstride;  // u32 per graph row
     uint32_t R;
@@ -109,7 +109,7 @@ __device__ __forceinline__ uint32_t warp_row_keys_impl(const SearchArgs &a, cons
             for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], qv[v], acc);
             for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
             const uint32_t r = r0 + p * rows_per + grp;
-            const uint64_t key = make_key(finish_dist<DT, MET>(acc), id[p]);
+            const uint64_t key = make_dist_key<MET>(finish_dist<DT, MET>(acc), id[p]);
             if constexpr (FILTER) {
                 const bool keep = lq == 0 && r < cnt && key < thr;
                 const unsigned m = __ballot_sync(kFull, keep);
@@ -169,10 +169,26 @@ static __device__ __noinline__ void sort_keys_large(uint64_t *keys, uint32_t cnt
     else sort_keys_kpl<8>(keys, cnt, lane);
 }
 
+// Small counts: each lane holds one key and counts the keys ranked before it
+// (smaller, or equal and held by a lower lane), then scatters to its rank.
+__device__ __forceinline__ void sort_keys_rank(uint64_t *keys, uint32_t cnt, int lane)
+{
+    const uint64_t v = uint32_t(lane) < cnt ? keys[lane] : kKeyMax;
+    uint32_t rank = 0;
+    for (uint32_t j = 0; j < cnt; ++j) {
+        const uint64_t o = __shfl_sync(kFull, v, int(j));
+        rank += (o < v) || (o == v && j < uint32_t(lane));
+    }
+    __syncwarp();
+    if (uint32_t(lane) < cnt) keys[rank] = v;
+    __syncwarp();
+}
+
 __device__ __forceinline__ void sort_keys(uint64_t *keys, uint32_t cnt, int lane)
 {
     if (cnt <= 1) return;
-    if (cnt <= 32) sort_keys_kpl<1>(keys, cnt, lane);
+    if (cnt <= 12) sort_keys_rank(keys, cnt, lane);
+    else if (cnt <= 32) sort_keys_kpl<1>(keys, cnt, lane);
     else if (cnt <= 64) sort_keys_kpl<2>(keys, cnt, lane);
     else sort_keys_large(keys, cnt, lane);
 }

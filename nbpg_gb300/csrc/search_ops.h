@@ -12,7 +12,11 @@ struct SearchOps {
                    cudaStream_t st);
 };
 
-// [element type][lane width: 0 -> 1 uint4, 1 -> 4 uint4]
-extern const SearchOps search_ops_u8[2], search_ops_i8[2], search_ops_u4[2];
+// one table per (element type, uint4 per lane per row)
+#define NBPG_DECL_OPS(t) extern const SearchOps search_ops_##t##_v1, search_ops_##t##_v2, search_ops_##t##_v4;
+NBPG_DECL_OPS(u8)
+NBPG_DECL_OPS(i8)
+NBPG_DECL_OPS(u4)
+#undef NBPG_DECL_OPS
 
 }  // namespace nbpg

@@ -1,0 +1,8 @@
+// Strict search kernels for one element type and lane width (see search_impl.cuh).
+#include "search_launch.cuh"
+#include "search_ops.h"
+
+namespace nbpg {
+const SearchOps search_ops_u4_v1 = {SearchDispatch<DT_U4, 1>::set_attr, SearchDispatch<DT_U4, 1>::occ,
+                                      SearchDispatch<DT_U4, 1>::launch};
+}  // namespace nbpg

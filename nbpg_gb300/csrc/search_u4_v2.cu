@@ -1,0 +1,8 @@
+// Strict search kernels for one element type and lane width (see search_impl.cuh).
+#include "search_launch.cuh"
+#include "search_ops.h"
+
+namespace nbpg {
+const SearchOps search_ops_u4_v2 = {SearchDispatch<DT_U4, 2>::set_attr, SearchDispatch<DT_U4, 2>::occ,
+                                      SearchDispatch<DT_U4, 2>::launch};
+}  // namespace nbpg

@@ -36,6 +36,20 @@ class QueryParams:
 
 
 @dataclass
+class LaunchConfig:
+    """How a search is launched (never what it returns): kernel form and its knobs."""
+    kernel: str = "batched"   # "batched" (persistent, device queue) or "plain" (one query per block)
+    warps_per_cta: int = 0    # 0 = default
+    lane_width: int = 0       # 16-byte words per lane per vector row; 0 = default
+    prefetch: int = -1        # upcoming adjacency rows prefetched to L2; -1 = default
+
+    def params(self, qp: "QueryParams") -> SearchParams:
+        return SearchParams(int(qp.k), int(qp.beamSize), float(qp.cut), int(qp.limit), int(qp.degree_limit),
+                            int(qp.visited_factor), _lib.KERNELS[self.kernel], int(self.warps_per_cta),
+                            int(self.lane_width), int(self.prefetch))
+
+
+@dataclass
 class SearchResult:
     ids: np.ndarray      # (nq, k) u32, UINT32_MAX padding
     dists: np.ndarray    # (nq, k) f32, +inf padding
@@ -96,7 +110,7 @@ class Index:
 
     # -- search ----------------------------------------------------------------
     def search(self, queries: np.ndarray, qp: QueryParams, start_points=(0,), kernel: str = "batched",
-               Ls=None, ks=None, warps_per_cta: int = 0) -> SearchResult:
+               Ls=None, ks=None, warps_per_cta: int = 0, launch: "LaunchConfig | None" = None) -> SearchResult:
         """Strict search of host queries; results identical to the reference's."""
         q = np.ascontiguousarray(queries)
         if q.ndim != 2 or q.shape[1] != self.dims:
@@ -106,8 +120,8 @@ class Index:
         ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.uint32)
         kst = int(ks.max()) if ks is not None and nq else int(qp.k)
         sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
-        prm = SearchParams(int(qp.k), int(qp.beamSize), float(qp.cut), int(qp.limit), int(qp.degree_limit),
-                           int(qp.visited_factor), _lib.KERNELS[kernel], int(warps_per_cta))
+        launch = launch or LaunchConfig(kernel=kernel, warps_per_cta=warps_per_cta)
+        prm = launch.params(qp)
         ids = np.empty((nq, kst), np.uint32)
         ds = np.empty((nq, kst), np.float32)
         cnt = np.empty(nq, np.uint32)
@@ -125,13 +139,25 @@ class Index:
     def search_device(self, d_queries: int, nq: int, qp: QueryParams, d_out_ids: int, k_stride: int,
                       d_out_dists: int | None = None, d_count: int | None = None, d_visited: int | None = None,
                       d_cmps: int | None = None, start_points=(0,), kernel: str = "batched", stream: int = 0,
-                      d_Ls: int | None = None, d_ks: int | None = None, warps_per_cta: int = 0) -> None:
+                      d_Ls: int | None = None, d_ks: int | None = None, warps_per_cta: int = 0,
+                      launch: "LaunchConfig | None" = None) -> None:
         """Enqueue a search on device buffers (raw pointers; rows of the index's device row stride)."""
         sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
-        prm = SearchParams(int(qp.k), int(qp.beamSize), float(qp.cut), int(qp.limit), int(qp.degree_limit),
-                           int(qp.visited_factor), _lib.KERNELS[kernel], int(warps_per_cta))
+        launch = launch or LaunchConfig(kernel=kernel, warps_per_cta=warps_per_cta)
+        prm = launch.params(qp)
         check(_lib.lib().nbpg_search_device(self._h, d_queries, nq, C.byref(prm), d_Ls, d_ks, _p(sp), len(sp),
                                             k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
+
+    def autotune(self, d_queries: int, nq: int, qp: QueryParams, start_points=(0,)):
+        """nbpg_search_autotune: the fastest LaunchConfig for these device queries, and its ms per launch."""
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        prm = LaunchConfig().params(qp)
+        out = SearchParams()
+        ms = C.c_float(0)
+        check(_lib.lib().nbpg_search_autotune(self._h, d_queries, nq, C.byref(prm), _p(sp), len(sp), C.byref(out),
+                                              C.byref(ms)))
+        kern = {v: k for k, v in _lib.KERNELS.items()}[out.kernel]
+        return LaunchConfig(kern, out.warps_per_cta, out.lane_width, out.prefetch), ms.value
 
     # -- build -----------------------------------------------------------------
     def build_vamana(self, L: int = 70, VL: int = 140, top_degree: int = 0, num_split: int = 4, num_passes: int = 2,

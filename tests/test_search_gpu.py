@@ -95,3 +95,31 @@ def test_search_isolated_start_and_empty_rows(gpu_lib, oracle_lib):
     _check(r, oracle_lib.search("u8", "l2", base, g, q, L=20, k=10), len(q))
     r = idx.search(q, QueryParams(k=10, beamSize=20), start_points=(3,))
     _check(r, oracle_lib.search("u8", "l2", base, g, q, L=20, k=10, start_points=(3,)), len(q))
+
+
+@pytest.mark.parametrize("dims", [32, 128, 100])
+def test_every_launch_config_gives_identical_results(gpu_lib, oracle_lib, dims):
+    """Lane width, CTA size, prefetch and kernel form change speed only."""
+    from nbpg_gb300.index import LaunchConfig, QueryParams
+    base, q, g = dataset("u8", "l2", dims=dims)
+    idx = _gpu_index(base, g, "u8", "l2")
+    o = oracle_lib.search("u8", "l2", base, g, q, L=40, k=10)
+    for kern in ("batched", "plain"):
+        for lw in (1, 2, 4):
+            for warps, pf in ((4, 0), (16, 2)):
+                lc = LaunchConfig(kernel=kern, warps_per_cta=warps, lane_width=lw, prefetch=pf)
+                _check(idx.search(q, QueryParams(k=10, beamSize=40), launch=lc), o, len(q))
+
+
+def test_autotuner_returns_a_valid_config(gpu_lib, oracle_lib):
+    import torch
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2", dims=128)
+    idx = _gpu_index(base, g, "u8", "l2")
+    _, rs, _, _ = idx.device_info()
+    qd = torch.zeros((len(q), rs), dtype=torch.uint8, device="cuda")
+    qd[:, :q.shape[1]] = torch.from_numpy(q).cuda()
+    qp = QueryParams(k=10, beamSize=32)
+    lc, ms = idx.autotune(qd.data_ptr(), len(q), qp)
+    assert lc.kernel in ("batched", "plain") and ms > 0
+    _check(idx.search(q, qp, launch=lc), oracle_lib.search("u8", "l2", base, g, q, L=32, k=10), len(q))
