@@ -134,6 +134,27 @@ nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queries, uint32_
                                  const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
                                  nbpg_search_params *tuned, float *best_ms);
 
+/* Strict search that allocates nothing: no counterpart in the reference.  For callers
+ * that cannot let a library call cudaMalloc on the request path — a database or
+ * serving process that owns a fixed device-memory budget reserved up front, where an
+ * allocation could fail or stall under pressure, or a host framework that only hands
+ * out pre-placed buffers.  The caller passes device-resident vectors (n rows, row
+ * pitch = dims rounded up to 16 bytes), graph (n rows of R+1 rounded up to 4 u32,
+ * [degree, ids...]), queries (same pitch) and outputs; results equal
+ * nbpg_search_device's.  The per-call scratch (work counters, queries re-run in exact
+ * mode, start points) is a fixed static device array of about 260 KB held by every
+ * device that loads the library until exit.  Limits: nq <= 65536, n_start <= 256,
+ * L <= 181 (visited filter in shared memory), no per-query L/k arrays.  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress): make that first
+ * call before any stream capture.  All calls share the array, so calls that overlap
+ * on the GPU race and must be serialised by the caller.  Runs on the current device
+ * and on `stream` (a cudaStream_t; NULL = the legacy default stream). */
+nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint32_t dims, uint64_t n, uint32_t max_degree,
+                                const void *d_points, const uint32_t *d_graph, const void *d_queries, uint32_t nq,
+                                const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
+                                uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists, uint32_t *d_out_count,
+                                uint32_t *d_out_visited, uint32_t *d_out_cmps, void *stream);
+
 /* Device pointer of the index's packed base rows (row stride = nbpg_index_row_stride
  * bytes) and of its graph rows (nbpg_index_graph_stride u32 per node). */
 nbpg_status nbpg_index_device_info(const nbpg_index *idx, void **d_points, uint32_t *row_stride,

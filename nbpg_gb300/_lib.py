@@ -81,6 +81,9 @@ def lib() -> C.CDLL:
                                      C.c_uint32, _vp, _vp, _vp, _vp, _vp, _vp]
     L.nbpg_search_autotune.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _u32p, C.c_uint32,
                                        C.POINTER(SearchParams), C.POINTER(C.c_float)]
+    L.nbpg_search_noalloc.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, _vp, _vp, _vp,
+                                      C.c_uint32, C.POINTER(SearchParams), _u32p, C.c_uint32, C.c_uint32, _vp, _vp,
+                                      _vp, _vp, _vp, _vp]
     L.nbpg_gt.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
                           C.c_uint32, _u32p, _f32p, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
