@@ -229,8 +229,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--save-graph", default=None, help="write the built graph (.graph format) here")
     ap.add_argument("--load-graph", default=None, help="use this graph instead of building one")
-    ap.add_argument("--profile", action="store_true",
-                    help="profiling run: index + --L, then warmup + steps of the batched search only")
+    ap.add_argument("--profile", default=None, choices=["search", "gt"],
+                    help="profiling run: warmup + steps of one kernel only (the search at --L, or the brute-force kNN)")
     ap.add_argument("--L", type=int, default=0, help="beam width for --profile (default: the sweep's choice)")
     ap.add_argument("--kernel", default="batched", choices=["batched", "plain"], help="--profile launch")
     ap.add_argument("--warps", type=int, default=0, help="--profile launch: warps per CTA")
@@ -276,8 +276,13 @@ def main():
         formats.write_graph(args.save_graph, g)
     avg_deg = float(g[:, 0].mean())
     log(f"[bench] average degree {avg_deg:.2f}")
-    if args.profile:
+    if args.profile == "search":
         return profile_search(idx, q, args.L or 19, args)
+    if args.profile == "gt":
+        for _ in range(args.warmup + args.steps):
+            ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
+        print(json.dumps({"profile": "ground truth", "launches": args.warmup + args.steps}), flush=True)
+        return
 
     t = time.time()
     gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)

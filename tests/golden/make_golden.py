@@ -1,0 +1,81 @@
+#!/usr/bin/env python3
+"""Generate golden vectors from the reference's own code (run where its sources exist).
+
+Inputs are small seeded synthetic sets.  Outputs, stored as tests/golden/*.npz:
+  * gt_*.npz      CompGT binary output (.gt ids/dists), k=100, u8/i8, L2 and --use_mips,
+                  including a tie-heavy set where CompGT's stale read matters;
+  * graph_*.npz   .graph files written by the Vamana binary with deterministic settings
+                  (--num_split 0, and --num_split 1 which runs the split stage, a popularity
+                  pass and the dynamic-prune pass), kept as raw bytes;
+  * search_*.npz  per-query ids, dists, counts, expansions and distance counts from the
+                  harness over the reference headers (qsearchAll's body) on those graphs.
+
+Usage: make -C oracle ref && python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from nbpg_gb300 import formats, synth  # noqa: E402
+from oracle.oracle import REF_COMPGT, REF_VAMANA, reference  # noqa: E402
+
+
+def datasets():
+    b, q = synth.u8_mixture(3000, 40, dim=32, n_centres=12, seed=7)
+    r = np.random.default_rng(5)
+    tb, tq = r.integers(0, 4, (2000, 8)).astype(np.uint8), r.integers(0, 4, (30, 8)).astype(np.uint8)
+    ib, iq = synth.i8_unit_mixture(2500, 30, dim=24, n_centres=10, seed=3)
+    return {"mix": ("u8", ".u8bin", b, q), "tie": ("u8", ".u8bin", tb, tq), "i8": ("i8", ".i8bin", ib, iq)}
+
+
+def main():
+    if not (os.path.exists(REF_COMPGT) and os.path.exists(REF_VAMANA) and reference()):
+        sys.exit("build the reference first: make -C oracle ref")
+    ref = reference()
+    tmp = tempfile.mkdtemp()
+    for name, (dt, ext, b, q) in datasets().items():
+        bp, qp = f"{tmp}/{name}_b{ext}", f"{tmp}/{name}_q{ext}"
+        formats.write_vectors(bp, b)
+        formats.write_vectors(qp, q)
+        for mips in (False, True):
+            gp = f"{tmp}/{name}_{int(mips)}.gt"
+            cmd = [REF_COMPGT, "--base_path", bp, "--query_path", qp, "--gt_path", gp, "--k", "100"]
+            if mips:
+                cmd.append("--use_mips")
+            subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+            ids, ds = formats.read_gt(gp)
+            np.savez_compressed(f"{HERE}/gt_{name}_{'ip' if mips else 'l2'}.npz", base=b, queries=q, ids=ids,
+                                dists=ds, dtype=dt)
+
+    dt, ext, b, q = datasets()["mix"]
+    bp = f"{tmp}/g_base{ext}"
+    formats.write_vectors(bp, b)
+    builds = {
+        "vamana": ["--num_split", "0", "--num_passes", "1", "--max_alpha", "1.2"],
+        "split1_dyn": ["--num_split", "1", "--num_passes", "2", "--dynamic_prune", "--min_alpha", "1.05",
+                       "--max_alpha", "1.2"],
+    }
+    for name, flags in builds.items():
+        ip = f"{tmp}/idx_{name}"
+        subprocess.run([REF_VAMANA, "--quant_base_path", bp, "--index_path", ip, "--R", "16", "--L", "24", "--VL",
+                        "32", "--rebuild", *flags], check=True, stdout=subprocess.DEVNULL)
+        raw = open(ip + ".graph", "rb").read()
+        np.savez_compressed(f"{HERE}/graph_{name}.npz", base=b, graph_file=np.frombuffer(raw, np.uint8),
+                            flags=np.array(" ".join(["--R 16 --L 24 --VL 32"] + flags)))
+        g = formats.read_graph(ip + ".graph")
+        for L, k in [(10, 10), (32, 10), (64, 50)]:
+            out = ref.search("u8", "l2", b, g, q, L=L, k=k, cut=1.35)
+            np.savez_compressed(f"{HERE}/search_{name}_L{L}_k{k}.npz", ids=out[0], dists=out[1], count=out[2],
+                                visited=out[3], cmps=out[4], queries=q)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
