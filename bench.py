@@ -402,6 +402,41 @@ def main():
     h2d = nq * CFG["dim"]
     d2h = nq * k * 8 + nq * 12 + 4
 
+    # serving: continuous batching with Poisson arrivals (requests admitted as batch slots
+    # and working-set budget free up); latency from each request's arrival to completion
+    serving = None
+    if rank == 0:
+        from nbpg_gb300.serve import Server
+        serving = {}
+        qq = np.concatenate([q] * 20)  # 200k requests
+        srv = Server(idx, max_L=L_op, max_k=k, max_batch=4096, max_in_flight=4, launch=tuned,
+                     qp=QueryParams(k=k, beamSize=L_op, cut=CFG["cut"]))
+        srv.replay(q[:5000], rate_qps=1e6, seed=9)  # warm-up
+        ref_ids = np.concatenate([res_op.ids] * 20)
+        for name, rate in [("at_half_peak", 0.5 * value), ("at_500k_qps", 5e5)]:
+            ids, ds, cnt, lat, el = srv.replay(qq, rate_qps=rate, seed=3)
+            p50, p99 = np.percentile(lat, [50, 99])
+            serving[name] = {"offered_qps": rate, "achieved_qps": len(qq) / el, "p50_ms": float(p50),
+                             "p99_ms": float(p99), "requests": len(qq), "L": L_op, "k": k,
+                             "same_as_batch": bool(np.array_equal(ids, ref_ids))}
+            log(f"[bench] serving {name}: offered {rate:.3g} QPS, achieved {len(qq) / el:.3g}, "
+                f"p50 {p50:.3f} ms, p99 {p99:.3f} ms")
+        srv.close()
+        # the serving configuration's request mix: L in {32,64,128,256}, k in {1,10,100}, k <= L
+        rng = np.random.default_rng(11)
+        Ls = rng.choice([32, 64, 128, 256], size=len(qq)).astype(np.uint32)
+        ks = np.minimum(rng.choice([1, 10, 100], size=len(qq)), Ls).astype(np.uint32)
+        srv = Server(idx, max_L=256, max_k=100, max_batch=4096, max_in_flight=4,
+                     qp=QueryParams(k=100, beamSize=256, cut=CFG["cut"]))
+        srv.replay(q[:5000], rate_qps=2e5, Ls=Ls[:5000], ks=ks[:5000], seed=9)
+        ids, ds, cnt, lat, el = srv.replay(qq, rate_qps=5e5, Ls=Ls, ks=ks, seed=5)
+        p50, p99 = np.percentile(lat, [50, 99])
+        serving["mixed_L_k_at_500k_qps"] = {"offered_qps": 5e5, "achieved_qps": len(qq) / el, "p50_ms": float(p50),
+                                           "p99_ms": float(p99), "requests": len(qq),
+                                           "L": "U{32,64,128,256}", "k": "U{1,10,100}, k<=L"}
+        log(f"[bench] serving mixed: achieved {len(qq) / el:.3g}, p50 {p50:.3f} ms, p99 {p99:.3f} ms")
+        srv.close()
+
     # roofline of the search kernel: algorithmic bytes per launch
     vis = res_op.visited.astype(np.float64)
     cmps = res_op.cmps.astype(np.float64)
@@ -441,7 +476,11 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src,
                          "traffic": None if tpq is None else tpq * nq},
-            "cpu_baseline": cpu, "clocks": clocks}
+            "cpu_baseline": cpu, "clocks": clocks,
+            "latency_ms": None if not serving else {"p50": serving["at_half_peak"]["p50_ms"],
+                                                     "p99": serving["at_half_peak"]["p99_ms"],
+                                                     "at_offered_qps": serving["at_half_peak"]["offered_qps"]},
+            "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -161,6 +161,52 @@ nbpg_status nbpg_index_device_info(const nbpg_index *idx, void **d_points, uint3
                                    uint32_t **d_graph, uint32_t *graph_stride);
 
 /* ---------------------------------------------------------------------------
+ * Serving: continuous batching over a device-resident index.  No counterpart in the
+ * reference, whose driver runs one OpenMP batch per parameter set
+ * (data_tools/ANNs/base/check_nn_recall.h:51-81).  Each request carries its own
+ * query row, L and k; results equal a strict search of that query alone.
+ * A dispatcher thread keeps up to max_in_flight batches on the device (each on its
+ * own stream with its own buffers and scratch) and, whenever one completes, admits
+ * the oldest pending requests while the working sets of everything in flight (per
+ * request: frontier, candidates, unvisited list, visited filter and exact-mode visited
+ * list for its L) fit memory_budget_bytes.  Latency of a request = from its arrival
+ * time to the dispatcher seeing its batch complete.  While a server is open, other
+ * calls on the same index are allowed but share its device.
+ * ------------------------------------------------------------------------- */
+typedef struct nbpg_server nbpg_server;
+
+typedef struct nbpg_serve_config {
+    uint32_t max_L, max_k;        /* largest beam width / k a request may ask for */
+    uint32_t max_batch;           /* requests per launch */
+    uint32_t max_in_flight;       /* concurrent batches (streams), <= 64 */
+    uint32_t queue_capacity;      /* pending requests held before submit refuses more */
+    uint64_t memory_budget_bytes; /* in-flight working-set budget; 0 = 2 x (SMs x shared memory per SM) */
+} nbpg_serve_config;
+
+/* params: launch configuration (kernel form, warps, lane width, prefetch) and the
+ * shared QueryParams (cut, limit, degree_limit, visited_factor); L and k come per request. */
+nbpg_status nbpg_serve_open(nbpg_index *idx, const nbpg_serve_config *cfg, const nbpg_search_params *params,
+                            nbpg_server **out);
+/* Queue `count` packed query rows (dims elements each).  Ls/ks: per request (NULL =
+ * max_L / max_k); request_ids returned by poll (NULL = 0); arrival_ns: CLOCK_MONOTONIC
+ * nanoseconds each request arrived (NULL = now).  *accepted < count when the queue is full. */
+nbpg_status nbpg_serve_submit(nbpg_server *s, const void *queries, uint32_t count, const uint32_t *Ls,
+                              const uint32_t *ks, const uint64_t *request_ids, const int64_t *arrival_ns,
+                              uint32_t *accepted);
+/* Collect up to max_results finished requests (ids/dists rows of k_stride >= max_k entries). */
+nbpg_status nbpg_serve_poll(nbpg_server *s, uint32_t max_results, uint32_t k_stride, uint64_t *request_ids,
+                            uint32_t *out_ids, float *out_dists, uint32_t *out_count, double *latency_ms,
+                            uint32_t *n_out);
+/* Replay n requests arriving as a Poisson process of rate_qps (seeded); returns each
+ * request's results (row i = request i) and latency, and the time from the first
+ * arrival to the last completion. */
+nbpg_status nbpg_serve_replay(nbpg_server *s, const void *queries, uint32_t n, const uint32_t *Ls,
+                              const uint32_t *ks, double rate_qps, uint64_t seed, uint32_t k_stride,
+                              uint32_t *out_ids, float *out_dists, uint32_t *out_count, double *latency_ms,
+                              double *elapsed_s);
+nbpg_status nbpg_serve_close(nbpg_server *s);
+
+/* ---------------------------------------------------------------------------
  * Brute-force kNN.  Replaces compute_groundtruth (data_tools/ANNs/data_proc/CompGT.cpp:29-134).
  * mode COMPGT replays CompGT's replace-max rule, stale read included
  * (CompGT.cpp:80-95), bit-exactly; mode EXACT returns the true (dist, id) top-k.

@@ -44,6 +44,11 @@ class BuildParams(C.Structure):
                 ("repair_isolate", C.c_int32), ("sp_seed", C.c_uint64)]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("max_L", C.c_uint32), ("max_k", C.c_uint32), ("max_batch", C.c_uint32), ("max_in_flight", C.c_uint32),
+                ("queue_capacity", C.c_uint32), ("memory_budget_bytes", C.c_uint64)]
+
+
 class BuildStats(C.Structure):
     _fields_ = [("isolated", C.c_uint64), ("seconds", C.c_double), ("batches", C.c_uint64)]
 
@@ -84,6 +89,14 @@ def lib() -> C.CDLL:
     L.nbpg_search_noalloc.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, _vp, _vp, _vp,
                                       C.c_uint32, C.POINTER(SearchParams), _u32p, C.c_uint32, C.c_uint32, _vp, _vp,
                                       _vp, _vp, _vp, _vp]
+    L.nbpg_serve_open.argtypes = [_vp, C.POINTER(ServeConfig), C.POINTER(SearchParams), C.POINTER(_vp)]
+    L.nbpg_serve_submit.argtypes = [_vp, _vp, C.c_uint32, _u32p, _u32p, C.POINTER(C.c_uint64),
+                                    C.POINTER(C.c_int64), _u32p]
+    L.nbpg_serve_poll.argtypes = [_vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64), _u32p, _f32p, _u32p,
+                                  C.POINTER(C.c_double), _u32p]
+    L.nbpg_serve_replay.argtypes = [_vp, _vp, C.c_uint32, _u32p, _u32p, C.c_double, C.c_uint64, C.c_uint32, _u32p,
+                                    _f32p, _u32p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.nbpg_serve_close.argtypes = [_vp]
     L.nbpg_gt.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
                           C.c_uint32, _u32p, _f32p, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]

@@ -62,8 +62,8 @@ extern "C" nbpg_status nbpg_index_destroy(nbpg_index *idx)
     if (idx->stream) cudaStreamSynchronize(idx->stream);
     if (idx->d_points) cudaFree(idx->d_points);
     if (idx->d_graph) cudaFree(idx->d_graph);
-    for (DevBuf *b : {&idx->queue, &idx->taint, &idx->sp, &idx->ghash, &idx->gvis, &idx->qbuf, &idx->obuf})
-        b->release();
+    idx->scratch.release();
+    for (DevBuf *b : {&idx->qbuf, &idx->obuf, &idx->ghash}) b->release();
     if (idx->stream) cudaStreamDestroy(idx->stream);
     delete idx;
     return NBPG_OK;

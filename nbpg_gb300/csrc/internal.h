@@ -63,6 +63,19 @@ struct DevBuf {
     T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Per-launch-sequence device scratch of the search: work counters, the tainted-query
+// list, start points, and global visited-filter / visited-list blocks for large L.
+// Launches that may overlap on the device need separate scratch.
+struct SearchScratch {
+    DevBuf queue, taint, sp, ghash, gvis;
+    std::vector<uint32_t> sp_host;  // start points currently in `sp`
+    void release()
+    {
+        for (DevBuf *b : {&queue, &taint, &sp, &ghash, &gvis}) b->release();
+        sp_host.clear();
+    }
+};
+
 }  // namespace nbpg
 
 struct nbpg_index {
@@ -76,7 +89,7 @@ struct nbpg_index {
     int sm_count = 0;
     size_t smem_optin = 0;
     // scratch
-    nbpg::DevBuf queue, taint, sp, ghash, gvis, qbuf, obuf;
-    std::vector<uint32_t> sp_host;  // start points currently in `sp`
+    nbpg::SearchScratch scratch;  // used by the index's own search calls
+    nbpg::DevBuf qbuf, obuf, ghash;  // host-API staging; build-time visited filters
     std::mutex mu;
 };

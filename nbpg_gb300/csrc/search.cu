@@ -105,10 +105,10 @@ static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, 
     return NBPG_OK;
 }
 
-nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t nq, const nbpg_search_params *P,
-                               const uint32_t *d_Ls, const uint32_t *d_ks, const uint32_t *sp, uint32_t nsp,
-                               uint32_t k_stride, uint32_t *d_ids, float *d_dists, uint32_t *d_count,
-                               uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st)
+nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
+                               const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
+                               const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
+                               uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st)
 {
     NBPG_CHECK_ARG(idx && P && d_ids, "null argument");
     NBPG_CHECK_ARG(idx->d_points && idx->d_graph, "index has no points/graph");
@@ -149,23 +149,23 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
     }
 
     // scratch: [0] queue main, [1] queue rerun, [2] error word; taint list; start points
-    if ((s = idx->queue.ensure(4 * sizeof(uint32_t))) != NBPG_OK) return s;
-    if ((s = idx->taint.ensure((size_t(nq) + 1) * sizeof(uint32_t))) != NBPG_OK) return s;
-    if ((s = idx->sp.ensure(256 * sizeof(uint32_t))) != NBPG_OK) return s;
+    if ((s = sc.queue.ensure(4 * sizeof(uint32_t))) != NBPG_OK) return s;
+    if ((s = sc.taint.ensure((size_t(nq) + 1) * sizeof(uint32_t))) != NBPG_OK) return s;
+    if ((s = sc.sp.ensure(256 * sizeof(uint32_t))) != NBPG_OK) return s;
     size_t nslots = std::max<size_t>(main.ghash || main.gvis ? size_t(main.grid) * main.warps : 0,
                                      rerun.ghash || rerun.gvis ? size_t(rerun.grid) * rerun.warps : 0);
     uint32_t hslots = std::max(main.ghash ? main.S : 0u, rerun.ghash ? rerun.S : 0u);
     uint32_t vcap = std::max(main.gvis ? main.Vcap : 0u, rerun.gvis ? rerun.Vcap : 0u);
-    if (hslots && (s = idx->ghash.ensure(nslots * hslots * sizeof(uint32_t))) != NBPG_OK) return s;
-    if (vcap && (s = idx->gvis.ensure(nslots * vcap * sizeof(uint64_t))) != NBPG_OK) return s;
+    if (hslots && (s = sc.ghash.ensure(nslots * hslots * sizeof(uint32_t))) != NBPG_OK) return s;
+    if (vcap && (s = sc.gvis.ensure(nslots * vcap * sizeof(uint64_t))) != NBPG_OK) return s;
 
-    uint32_t *q = idx->queue.as<uint32_t>();
+    uint32_t *q = sc.queue.as<uint32_t>();
     NBPG_CUDA_TRY(cudaMemsetAsync(q, 0, 4 * sizeof(uint32_t), st));
-    NBPG_CUDA_TRY(cudaMemsetAsync(idx->taint.ptr, 0, sizeof(uint32_t), st));
-    if (idx->sp_host.size() != nsp || !std::equal(sp, sp + nsp, idx->sp_host.begin())) {
-        NBPG_CUDA_TRY(cudaMemcpyAsync(idx->sp.ptr, sp, nsp * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    NBPG_CUDA_TRY(cudaMemsetAsync(sc.taint.ptr, 0, sizeof(uint32_t), st));
+    if (sc.sp_host.size() != nsp || !std::equal(sp, sp + nsp, sc.sp_host.begin())) {
+        NBPG_CUDA_TRY(cudaMemcpyAsync(sc.sp.ptr, sp, nsp * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         NBPG_CUDA_TRY(cudaStreamSynchronize(st));
-        idx->sp_host.assign(sp, sp + nsp);
+        sc.sp_host.assign(sp, sp + nsp);
     }
 
     SearchArgs a{};
@@ -188,7 +188,7 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
     a.limit = P->limit ? P->limit : n;
     a.degree_limit = P->degree_limit ? std::min(P->degree_limit, R) : R;
     a.visited_factor = vf;
-    a.sp = idx->sp.as<uint32_t>();
+    a.sp = sc.sp.as<uint32_t>();
     a.nsp = nsp;
     a.k_stride = k_stride;
     a.out_ids = d_ids;
@@ -202,11 +202,11 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
     // main pass
     SearchArgs m = a;
     m.queue = q;
-    m.taint = flag_first ? idx->taint.as<uint32_t>() : nullptr;
+    m.taint = flag_first ? sc.taint.as<uint32_t>() : nullptr;
     m.lay = main.lay;
-    m.g_hash = main.ghash ? idx->ghash.as<uint32_t>() : nullptr;
+    m.g_hash = main.ghash ? sc.ghash.as<uint32_t>() : nullptr;
     m.g_hash_slots = main.ghash ? hslots : 0;
-    m.g_vis = main.gvis ? idx->gvis.as<uint64_t>() : nullptr;
+    m.g_vis = main.gvis ? sc.gvis.as<uint64_t>() : nullptr;
     m.g_vis_cap = main.gvis ? vcap : 0;
     ops->launch(metric, !flag_first, plain, plain ? nq : main.grid, main.warps, main.smem, m, st);
     NBPG_CUDA_TRY(cudaGetLastError());
@@ -214,11 +214,11 @@ nbpg_status search_device_impl(nbpg_index *idx, const void *d_queries, uint32_t 
     if (flag_first) {
         SearchArgs r = a;
         r.queue = q + 1;
-        r.only = idx->taint.as<uint32_t>();
+        r.only = sc.taint.as<uint32_t>();
         r.lay = rerun.lay;
-        r.g_hash = rerun.ghash ? idx->ghash.as<uint32_t>() : nullptr;
+        r.g_hash = rerun.ghash ? sc.ghash.as<uint32_t>() : nullptr;
         r.g_hash_slots = rerun.ghash ? hslots : 0;
-        r.g_vis = rerun.gvis ? idx->gvis.as<uint64_t>() : nullptr;
+        r.g_vis = rerun.gvis ? sc.gvis.as<uint64_t>() : nullptr;
         r.g_vis_cap = rerun.gvis ? vcap : 0;
         r.prefetch = 0;
         ops->launch(metric, true, false, rerun.grid, rerun.warps, rerun.smem, r, st);
@@ -241,7 +241,8 @@ extern "C" nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries
     if (!idx) { set_error("null index"); return NBPG_ERR_INVALID_ARG; }
     std::lock_guard<std::mutex> g(idx->mu);
     cudaSetDevice(idx->desc.device);
-    return search_device_impl(idx, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride, d_out_ids,
+    return search_device_impl(idx, idx->scratch, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride,
+                              d_out_ids,
                               d_out_dists, d_out_count, d_out_visited, d_out_cmps, static_cast<cudaStream_t>(stream));
 }
 
@@ -287,8 +288,8 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     if (ks) NBPG_CUDA_TRY(cudaMemcpyAsync(d_k, ks, nq * 4, cudaMemcpyHostToDevice, st));
     else if (Ls) { std::vector<uint32_t> t(nq, P->k); NBPG_CUDA_TRY(cudaMemcpyAsync(d_k, t.data(), nq * 4, cudaMemcpyHostToDevice, st)); NBPG_CUDA_TRY(cudaStreamSynchronize(st)); }
     const bool per = Ls || ks;
-    s = search_device_impl(idx, dq, nq, &p, per ? d_L : nullptr, per ? d_k : nullptr, start_points, n_start, k_stride,
-                           d_ids, d_d, d_c, d_v, d_m, st);
+    s = search_device_impl(idx, idx->scratch, dq, nq, &p, per ? d_L : nullptr, per ? d_k : nullptr, start_points,
+                           n_start, k_stride, d_ids, d_d, d_c, d_v, d_m, st);
     if (s != NBPG_OK) return s;
     uint32_t err = 0;
     NBPG_CUDA_TRY(cudaMemcpyAsync(out_ids, d_ids, size_t(nq) * k_stride * 4, cudaMemcpyDeviceToHost, st));
@@ -296,7 +297,7 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     if (out_count) NBPG_CUDA_TRY(cudaMemcpyAsync(out_count, d_c, nq * 4, cudaMemcpyDeviceToHost, st));
     if (out_visited) NBPG_CUDA_TRY(cudaMemcpyAsync(out_visited, d_v, nq * 4, cudaMemcpyDeviceToHost, st));
     if (out_cmps) NBPG_CUDA_TRY(cudaMemcpyAsync(out_cmps, d_m, nq * 4, cudaMemcpyDeviceToHost, st));
-    NBPG_CUDA_TRY(cudaMemcpyAsync(&err, idx->queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+    NBPG_CUDA_TRY(cudaMemcpyAsync(&err, idx->scratch.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
     NBPG_CUDA_TRY(cudaStreamSynchronize(st));
     if (err) {
         set_error("a query was rejected on the device (k > L or L above the planned maximum)");
@@ -351,8 +352,8 @@ extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queri
         float t = 1e30f;
         for (int rep = 0; rep < 3 && s == NBPG_OK; ++rep) {
             if (rep > 0) cudaEventRecord(e0, st);
-            s = search_device_impl(idx, d_queries, nq, &p, nullptr, nullptr, start_points, n_start, k, d_ids, nullptr,
-                                   nullptr, nullptr, nullptr, st);
+            s = search_device_impl(idx, idx->scratch, d_queries, nq, &p, nullptr, nullptr, start_points, n_start, k,
+                                   d_ids, nullptr, nullptr, nullptr, nullptr, st);
             if (rep > 0) {
                 cudaEventRecord(e1, st);
                 cudaEventSynchronize(e1);
