@@ -134,6 +134,20 @@ nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queries, uint32_
                                  const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
                                  nbpg_search_params *tuned, float *best_ms);
 
+/* The whole search request (its scratch resets, the fast pass and the exact re-run
+ * of tainted queries) captured once as a CUDA graph over fixed device buffers, then
+ * replayed with one cudaGraphLaunch per batch.  Same arguments as nbpg_search_device;
+ * the queries/outputs are read/written in place at every launch.  No counterpart in
+ * the reference (which has no GPU path). */
+typedef struct nbpg_search_graph nbpg_search_graph;
+nbpg_status nbpg_search_graph_create(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                     const nbpg_search_params *params, const uint32_t *d_Ls, const uint32_t *d_ks,
+                                     const uint32_t *start_points, uint32_t n_start, uint32_t k_stride,
+                                     uint32_t *d_out_ids, float *d_out_dists, uint32_t *d_out_count,
+                                     uint32_t *d_out_visited, uint32_t *d_out_cmps, nbpg_search_graph **out);
+nbpg_status nbpg_search_graph_launch(nbpg_search_graph *g, void *stream);
+nbpg_status nbpg_search_graph_destroy(nbpg_search_graph *g);
+
 /* Strict search that allocates nothing: no counterpart in the reference.  For callers
  * that cannot let a library call cudaMalloc on the request path — a database or
  * serving process that owns a fixed device-memory budget reserved up front, where an

@@ -97,6 +97,10 @@ def lib() -> C.CDLL:
     L.nbpg_serve_replay.argtypes = [_vp, _vp, C.c_uint32, _u32p, _u32p, C.c_double, C.c_uint64, C.c_uint32, _u32p,
                                     _f32p, _u32p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.nbpg_serve_close.argtypes = [_vp]
+    L.nbpg_search_graph_create.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _vp, _vp, _u32p,
+                                           C.c_uint32, C.c_uint32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]
+    L.nbpg_search_graph_launch.argtypes = [_vp, _vp]
+    L.nbpg_search_graph_destroy.argtypes = [_vp]
     L.nbpg_gt.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
                           C.c_uint32, _u32p, _f32p, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]

@@ -63,7 +63,7 @@ extern "C" nbpg_status nbpg_index_destroy(nbpg_index *idx)
     if (idx->d_points) cudaFree(idx->d_points);
     if (idx->d_graph) cudaFree(idx->d_graph);
     idx->scratch.release();
-    for (DevBuf *b : {&idx->qbuf, &idx->obuf, &idx->ghash}) b->release();
+    for (DevBuf *b : {&idx->qbuf, &idx->obuf, &idx->ghash, &idx->order_buf}) b->release();
     if (idx->stream) cudaStreamDestroy(idx->stream);
     delete idx;
     return NBPG_OK;

@@ -68,6 +68,7 @@ struct DevBuf {
 // Launches that may overlap on the device need separate scratch.
 struct SearchScratch {
     DevBuf queue, taint, sp, ghash, gvis;
+    const uint32_t *order = nullptr;  // optional processing order of the next launch (device)
     std::vector<uint32_t> sp_host;  // start points currently in `sp`
     void release()
     {
@@ -90,6 +91,6 @@ struct nbpg_index {
     size_t smem_optin = 0;
     // scratch
     nbpg::SearchScratch scratch;  // used by the index's own search calls
-    nbpg::DevBuf qbuf, obuf, ghash;  // host-API staging; build-time visited filters
+    nbpg::DevBuf qbuf, obuf, ghash, order_buf;  // host-API staging; build-time visited filters
     std::mutex mu;
 };

@@ -199,8 +199,9 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     a.err = q + 2;
     a.prefetch = plain ? 0 : (P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u));
 
-    // main pass
+    // main pass (queries in the caller's order, or longest beam first when given)
     SearchArgs m = a;
+    m.order = sc.order;
     m.queue = q;
     m.taint = flag_first ? sc.taint.as<uint32_t>() : nullptr;
     m.lay = main.lay;
@@ -288,8 +289,22 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     if (ks) NBPG_CUDA_TRY(cudaMemcpyAsync(d_k, ks, nq * 4, cudaMemcpyHostToDevice, st));
     else if (Ls) { std::vector<uint32_t> t(nq, P->k); NBPG_CUDA_TRY(cudaMemcpyAsync(d_k, t.data(), nq * 4, cudaMemcpyHostToDevice, st)); NBPG_CUDA_TRY(cudaStreamSynchronize(st)); }
     const bool per = Ls || ks;
+    // uneven beam widths: hand out the longest searches first (longest-processing-time
+    // order) so the batch does not end on a tail of long queries
+    uint32_t *d_order = nullptr;
+    if (Ls) {
+        std::vector<uint32_t> ord(nq);
+        for (uint32_t i = 0; i < nq; ++i) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) { return Ls[x] > Ls[y]; });
+        if ((s = idx->order_buf.ensure(size_t(nq) * 4)) != NBPG_OK) return s;
+        d_order = idx->order_buf.as<uint32_t>();
+        NBPG_CUDA_TRY(cudaMemcpyAsync(d_order, ord.data(), size_t(nq) * 4, cudaMemcpyHostToDevice, st));
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    idx->scratch.order = d_order;
     s = search_device_impl(idx, idx->scratch, dq, nq, &p, per ? d_L : nullptr, per ? d_k : nullptr, start_points,
                            n_start, k_stride, d_ids, d_d, d_c, d_v, d_m, st);
+    idx->scratch.order = nullptr;
     if (s != NBPG_OK) return s;
     uint32_t err = 0;
     NBPG_CUDA_TRY(cudaMemcpyAsync(out_ids, d_ids, size_t(nq) * k_stride * 4, cudaMemcpyDeviceToHost, st));
@@ -372,5 +387,78 @@ extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queri
     if (s != NBPG_OK) return s;
     *tuned = win;
     if (best_ms) *best_ms = best;
+    return NBPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-graph form of one search request: every launch of the FLAG pass and the LIST
+// re-run, with their scratch resets, captured once and replayed.
+// ---------------------------------------------------------------------------
+struct nbpg_search_graph {
+    nbpg_index *idx = nullptr;
+    SearchScratch sc;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" nbpg_status nbpg_search_graph_create(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                                const nbpg_search_params *params, const uint32_t *d_Ls,
+                                                const uint32_t *d_ks, const uint32_t *start_points, uint32_t n_start,
+                                                uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
+                                                uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps,
+                                                nbpg_search_graph **out)
+{
+    NBPG_CHECK_ARG(idx && out, "null argument");
+    std::lock_guard<std::mutex> g(idx->mu);
+    NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
+    auto *G = new nbpg_search_graph();
+    G->idx = idx;
+    cudaStream_t st = idx->stream;
+    // one uncaptured run sizes the scratch, stages the start points and sets kernel attributes
+    nbpg_status s = search_device_impl(idx, G->sc, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride,
+                                       d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps, st);
+    cudaError_t e = cudaSuccess;
+    if (s == NBPG_OK) e = cudaStreamSynchronize(st);
+    if (s == NBPG_OK && e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (s == NBPG_OK && e == cudaSuccess) {
+        s = search_device_impl(idx, G->sc, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride,
+                               d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps, st);
+        cudaError_t e2 = cudaStreamEndCapture(st, &G->graph);
+        if (e2 != cudaSuccess) e = e2;
+    }
+    if (s == NBPG_OK && e == cudaSuccess) e = cudaGraphInstantiate(&G->exec, G->graph, 0);
+    if (s != NBPG_OK || e != cudaSuccess) {
+        if (s == NBPG_OK) {
+            set_error(std::string("search graph capture: ") + cudaGetErrorString(e));
+            s = NBPG_ERR_CUDA;
+        }
+        if (G->exec) cudaGraphExecDestroy(G->exec);
+        if (G->graph) cudaGraphDestroy(G->graph);
+        G->sc.release();
+        delete G;
+        return s;
+    }
+    *out = G;
+    return NBPG_OK;
+}
+
+extern "C" nbpg_status nbpg_search_graph_launch(nbpg_search_graph *G, void *stream)
+{
+    NBPG_CHECK_ARG(G, "null graph");
+    NBPG_CUDA_TRY(cudaSetDevice(G->idx->desc.device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : G->idx->stream;
+    NBPG_CUDA_TRY(cudaGraphLaunch(G->exec, st));
+    return NBPG_OK;
+}
+
+extern "C" nbpg_status nbpg_search_graph_destroy(nbpg_search_graph *G)
+{
+    if (!G) return NBPG_OK;
+    cudaSetDevice(G->idx->desc.device);
+    cudaDeviceSynchronize();
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
+    G->sc.release();
+    delete G;
     return NBPG_OK;
 }

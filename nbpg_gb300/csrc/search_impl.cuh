@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(32) search_plain_kernel(SearchArgs a)
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t total = a.only ? a.only[0] : a.nq;
     if (blockIdx.x >= total) return;
-    const uint32_t qi = a.only ? a.only[1 + blockIdx.x] : blockIdx.x;
+    const uint32_t qi = a.only ? a.only[1 + blockIdx.x] : (a.order ? a.order[blockIdx.x] : blockIdx.x);
     search_query<DT, MET, LIST, VPL>(a, qi, smem, blockIdx.x, threadIdx.x);
 }
 

@@ -68,6 +68,7 @@ struct BatchSlot {
     uint32_t *d_L = nullptr, *d_k = nullptr, *d_ids = nullptr, *d_cnt = nullptr;
     float *d_d = nullptr;
     uint32_t *h_L = nullptr, *h_k = nullptr, *h_ids = nullptr, *h_cnt = nullptr;
+    uint32_t *d_ord = nullptr, *h_ord = nullptr;  // longest-beam-first processing order
     float *h_d = nullptr;
     SearchScratch sc;
     std::vector<Req> reqs;
@@ -152,6 +153,12 @@ void nbpg_server::run()
                 cudaMemcpyAsync(free->d_q, free->h_q, size_t(nb) * row_stride, cudaMemcpyHostToDevice, st);
                 cudaMemcpyAsync(free->d_L, free->h_L, nb * 4, cudaMemcpyHostToDevice, st);
                 cudaMemcpyAsync(free->d_k, free->h_k, nb * 4, cudaMemcpyHostToDevice, st);
+                // mixed beam widths: start the longest searches first
+                for (uint32_t i = 0; i < nb; ++i) free->h_ord[i] = i;
+                std::stable_sort(free->h_ord, free->h_ord + nb,
+                                 [&](uint32_t x, uint32_t y) { return free->h_L[x] > free->h_L[y]; });
+                cudaMemcpyAsync(free->d_ord, free->h_ord, nb * 4, cudaMemcpyHostToDevice, st);
+                free->sc.order = free->d_ord;
                 nbpg_status s;
                 {
                     std::lock_guard<std::mutex> gi(idx->mu);
@@ -190,6 +197,8 @@ static void free_slot(BatchSlot &b)
     cudaFree(b.d_ids);
     cudaFree(b.d_cnt);
     cudaFree(b.d_d);
+    cudaFree(b.d_ord);
+    cudaFreeHost(b.h_ord);
     cudaFreeHost(b.h_q);
     cudaFreeHost(b.h_L);
     cudaFreeHost(b.h_k);
@@ -252,6 +261,8 @@ extern "C" nbpg_status nbpg_serve_open(nbpg_index *idx, const nbpg_serve_config 
         if (e == cudaSuccess) e = cudaMalloc(&b.d_ids, B * K * 4);
         if (e == cudaSuccess) e = cudaMalloc(&b.d_d, B * K * 4);
         if (e == cudaSuccess) e = cudaMalloc(&b.d_cnt, B * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&b.d_ord, B * 4);
+        if (e == cudaSuccess) e = cudaMallocHost(&b.h_ord, B * 4);
         if (e == cudaSuccess) e = cudaMallocHost(&b.h_q, B * s->row_stride);
         if (e == cudaSuccess) e = cudaMallocHost(&b.h_L, B * 4);
         if (e == cudaSuccess) e = cudaMallocHost(&b.h_k, B * 4);

@@ -159,6 +159,18 @@ class Index:
         kern = {v: k for k, v in _lib.KERNELS.items()}[out.kernel]
         return LaunchConfig(kern, out.warps_per_cta, out.lane_width, out.prefetch), ms.value
 
+    def search_graph(self, d_queries: int, nq: int, qp: QueryParams, d_out_ids: int, k_stride: int,
+                     d_out_dists=None, d_count=None, d_visited=None, d_cmps=None, start_points=(0,),
+                     launch: "LaunchConfig | None" = None, d_Ls=None, d_ks=None) -> "SearchGraph":
+        """Capture the search over these device buffers as a CUDA graph (nbpg_search_graph_create)."""
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        prm = (launch or LaunchConfig()).params(qp)
+        h = C.c_void_p()
+        check(_lib.lib().nbpg_search_graph_create(self._h, d_queries, nq, C.byref(prm), d_Ls, d_ks, _p(sp), len(sp),
+                                                  k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps,
+                                                  C.byref(h)))
+        return SearchGraph(h)
+
     # -- build -----------------------------------------------------------------
     def build_vamana(self, L: int = 70, VL: int = 140, top_degree: int = 0, num_split: int = 4, num_passes: int = 2,
                      limit: int = 0, dir_bias_scale: float = 0.0, min_alpha: float = 1.0, max_alpha: float = 1.1,
@@ -172,6 +184,27 @@ class Index:
         sd = np.zeros(self.n, np.uint32) if with_stats else None
         check(_lib.lib().nbpg_build(self._h, C.byref(prm), C.byref(st), _p(sv), _p(sd)))
         return st, sv, sd
+
+
+class SearchGraph:
+    """A captured search request; launch() replays it on a stream."""
+
+    def __init__(self, h):
+        self._h = h
+
+    def launch(self, stream: int = 0) -> None:
+        check(_lib.lib().nbpg_search_graph_launch(self._h, stream))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().nbpg_search_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ground_truth(base: np.ndarray, queries: np.ndarray, dtype: str, metric: str = "l2", k: int = 100,

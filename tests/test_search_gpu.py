@@ -123,3 +123,30 @@ def test_autotuner_returns_a_valid_config(gpu_lib, oracle_lib):
     lc, ms = idx.autotune(qd.data_ptr(), len(q), qp)
     assert lc.kernel in ("batched", "plain") and ms > 0
     _check(idx.search(q, qp, launch=lc), oracle_lib.search("u8", "l2", base, g, q, L=32, k=10), len(q))
+
+
+def test_cuda_graph_replay_matches(gpu_lib, oracle_lib):
+    import torch
+    from nbpg_gb300.index import LaunchConfig, QueryParams
+    base, q, g = dataset("u8", "l2", dims=32)
+    idx = _gpu_index(base, g, "u8", "l2")
+    _, rs, _, _ = idx.device_info()
+    nq, k = len(q), 10
+    qd = torch.zeros((nq, rs), dtype=torch.uint8, device="cuda")
+    qd[:, :q.shape[1]] = torch.from_numpy(q).cuda()
+    outs = [torch.zeros((nq, k), dtype=torch.int32, device="cuda"), torch.zeros((nq, k), dtype=torch.float32,
+            device="cuda")] + [torch.zeros(nq, dtype=torch.int32, device="cuda") for _ in range(3)]
+    o = oracle_lib.search("u8", "l2", base, g, q, L=48, k=k)
+    for kern in ("batched", "plain"):
+        gr = idx.search_graph(qd.data_ptr(), nq, QueryParams(k=k, beamSize=48), outs[0].data_ptr(), k,
+                              *(t.data_ptr() for t in outs[1:]), launch=LaunchConfig(kernel=kern))
+        for _ in range(3):
+            for t in outs:
+                t.zero_()
+            gr.launch()
+            torch.cuda.synchronize()
+            got = [outs[0].cpu().numpy().view(np.uint32), outs[1].cpu().numpy(),
+                   *(t.cpu().numpy().view(np.uint32) for t in outs[2:])]
+            for x, y in zip(got, o):
+                assert np.array_equal(x, y)
+        gr.close()
