@@ -375,6 +375,46 @@ def main():
     batched_default_qps = time_launch(LaunchConfig(kernel="batched"))
     assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "batched kernel results differ"
 
+    # the same request replayed as one captured CUDA graph per step
+    graph_qps = None
+    try:
+        gr = idx.search_graph(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, o_d.data_ptr(), o_c.data_ptr(),
+                              o_v.data_ptr(), o_m.data_ptr(), launch=tuned)
+        for _ in range(3):
+            gr.launch(stream.cuda_stream)
+        torch.cuda.synchronize()
+        ge = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(50)]
+        for e0, e1 in ge:
+            e0.record(stream)
+            gr.launch(stream.cuda_stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        graph_qps = nq * len(ge) / (sum(a.elapsed_time(b) for a, b in ge) / 1e3)
+        assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "graph replay results differ"
+        gr.close()
+    except Exception as exc:  # reported, not fatal
+        log(f"[bench] graph replay failed: {exc}")
+
+    # uneven batch: per-query L in {32,64,128,256}, k in {1,10,100} (k <= L); batched
+    # persistent kernel (longest beam first) vs the plain one-query-per-block kernel
+    rng = np.random.default_rng(7)
+    uL = rng.choice([32, 64, 128, 256], size=nq).astype(np.uint32)
+    uk = np.minimum(rng.choice([1, 10, 100], size=nq), uL).astype(np.uint32)
+    uqp = QueryParams(k=100, beamSize=256, cut=CFG["cut"])
+    uneven = {}
+    for name, lc in [("plain", LaunchConfig(kernel="plain")), ("batched", LaunchConfig(kernel="batched"))]:
+        r0 = idx.search(q, uqp, Ls=uL, ks=uk, launch=lc)
+        t = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            r = idx.search(q, uqp, Ls=uL, ks=uk, launch=lc)
+        uneven[name + "_qps"] = nq * reps / (time.perf_counter() - t)
+        uneven.setdefault("ids", r.ids)
+        assert np.array_equal(r.ids, uneven["ids"]) and np.array_equal(r0.ids, r.ids), "uneven results differ"
+    uneven.pop("ids")
+    uneven["batched_over_plain"] = uneven["batched_qps"] / uneven["plain_qps"]
+    log(f"[bench] uneven L/k: {uneven}")
+
     # e2e through the C ABI: pinned host queries in, host results out, every step
     L = _lib.lib()
     qh = torch.from_numpy(q).pin_memory()
@@ -468,7 +508,8 @@ def main():
                                   "lane_width": tuned.lane_width, "prefetch": tuned.prefetch,
                                   "chosen_by": "nbpg_search_autotune"},
                        "plain_kernel_qps": plain_qps, "batched_default_qps": batched_default_qps,
-                       "tuned_over_plain": value / plain_qps,
+                       "tuned_over_plain": value / plain_qps, "cuda_graph_qps": graph_qps,
+                       "uneven_L_k_batch": uneven,
                        "build_s": None if build_s is None else round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
                        "L_sweep": sweep, "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
