@@ -58,7 +58,28 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)
+    _build_cli()
     return LIB
+
+
+CLI = {"nbpg_vamana": "vamana.cpp", "nbpg_compgt": "compgt.cpp"}
+
+
+def _build_cli() -> None:
+    """The Vamana/CompGT drop-in executables (host C++ over the C ABI)."""
+    cxx = os.environ.get("CXX", "g++")
+    src_dir = os.path.join(HERE, "cli")
+    for exe, src in CLI.items():
+        out = os.path.join(OUT, exe)
+        srcp = os.path.join(src_dir, src)
+        deps = [srcp, os.path.join(src_dir, "flags.h"), os.path.join(INCLUDE, "nbpg.h"), LIB]
+        if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+            continue
+        cmd = [cxx, "-O2", "-std=c++17", srcp, f"-I{INCLUDE}", f"-L{OUT}", "-lnbpg_gb300",
+               "-Wl,-rpath,$ORIGIN", "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"building {exe} failed:\n{r.stderr}")
 
 
 if __name__ == "__main__":
