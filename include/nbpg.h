@@ -232,6 +232,15 @@ nbpg_status nbpg_gt(uint32_t dtype, uint32_t metric, uint32_t dims, const void *
                     const void *queries, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *out_ids,
                     float *out_dists, int32_t device);
 
+/* Distance engine for nbpg_gt_with_engine: AUTO picks TENSOR where it applies (row length
+ * up to 128 codes after 4-bit expansion, k <= 100) and DP4A otherwise; TENSOR on an
+ * unsupported shape returns NBPG_ERR_UNSUPPORTED.  Results are identical across engines. */
+typedef enum nbpg_gt_engine { NBPG_GT_AUTO = 0, NBPG_GT_DP4A = 1, NBPG_GT_TENSOR = 2 } nbpg_gt_engine;
+
+nbpg_status nbpg_gt_with_engine(uint32_t dtype, uint32_t metric, uint32_t dims, const void *base, uint64_t n,
+                                const void *queries, uint32_t nq, uint32_t k, uint32_t mode, uint32_t engine,
+                                uint32_t *out_ids, float *out_dists, int32_t device);
+
 /* ---------------------------------------------------------------------------
  * Build.  Replaces build_vamana (algorithms/nsw.h:547-663) with NSWIndex::batch_insert
  * (nsw.h:110-286), RobustPrune (algorithms/utils/Graph/prune.h:159-209), reverse-edge

@@ -103,6 +103,8 @@ def lib() -> C.CDLL:
     L.nbpg_search_graph_destroy.argtypes = [_vp]
     L.nbpg_gt.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
                           C.c_uint32, _u32p, _f32p, C.c_int32]
+    L.nbpg_gt_with_engine.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
+                                 C.c_uint32, C.c_uint32, _u32p, _f32p, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
     _lib = L
     return L

@@ -279,6 +279,11 @@ static cudaError_t launch_gt(const GtArgs &a, size_t smem, cudaStream_t st)
     return cudaGetLastError();
 }
 
+bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_optin);
+nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t stride, const uint8_t *d_base,
+                         uint64_t n, const uint8_t *d_q, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *d_ids,
+                         float *d_dists, cudaStream_t st);
+
 nbpg_status gt_device(uint32_t dtype, uint32_t metric, const GtArgs &a, cudaStream_t st, size_t smem_optin)
 {
     const uint32_t WS = a.row_stride / 4 + 1;
@@ -312,11 +317,20 @@ extern "C" nbpg_status nbpg_gt(uint32_t dtype, uint32_t metric, uint32_t dims, c
                                const void *queries, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *out_ids,
                                float *out_dists, int32_t device)
 {
+    return nbpg_gt_with_engine(dtype, metric, dims, base, n, queries, nq, k, mode, NBPG_GT_AUTO, out_ids, out_dists,
+                               device);
+}
+
+extern "C" nbpg_status nbpg_gt_with_engine(uint32_t dtype, uint32_t metric, uint32_t dims, const void *base,
+                                           uint64_t n, const void *queries, uint32_t nq, uint32_t k, uint32_t mode,
+                                           uint32_t engine, uint32_t *out_ids, float *out_dists, int32_t device)
+{
     NBPG_CHECK_ARG(base && queries && out_ids && out_dists, "null argument");
     NBPG_CHECK_ARG(dtype <= NBPG_I4 && metric <= NBPG_IP, "unsupported dtype/metric");
     NBPG_CHECK_ARG(k >= 1 && k <= 256, "k must be in [1, 256]");
     NBPG_CHECK_ARG(n >= k && n < 0xFFFFFFFFull, "need k <= n < 2^32-1");
     NBPG_CHECK_ARG(dims >= 1 && mode <= NBPG_GT_EXACT, "bad dims/mode");
+    NBPG_CHECK_ARG(engine <= NBPG_GT_TENSOR, "bad engine");
     if (nq == 0) return NBPG_OK;
     NBPG_CUDA_TRY(cudaSetDevice(device));
     const uint32_t rb = dims;  // packed bytes per row (u8/i8/u4/i4)
@@ -342,7 +356,14 @@ extern "C" nbpg_status nbpg_gt(uint32_t dtype, uint32_t metric, uint32_t dims, c
     if (e == cudaSuccess) e = cudaMemcpy2DAsync(db, rs, base, rb, rb, n, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpy2DAsync(dq, rs, queries, rb, rb, nq, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) fail(e);
-    if (s == NBPG_OK) {
+    const bool tc_ok = gt_tc_supported(dtype, dims, k, prop.sharedMemPerBlockOptin);
+    if (s == NBPG_OK && engine == NBPG_GT_TENSOR && !tc_ok) {
+        set_error("nbpg_gt: the tensor engine needs <= 128 codes per row and k <= 100");
+        s = NBPG_ERR_UNSUPPORTED;
+    }
+    if (s == NBPG_OK && engine != NBPG_GT_DP4A && tc_ok) {
+        s = gt_tc_device(dtype, metric, dims, rs, db, n, dq, nq, k, mode, di, dd, st);
+    } else if (s == NBPG_OK) {
         GtArgs a{db, n, rs, dq, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, di, dd};
         s = gt_device(dtype, metric, a, st, prop.sharedMemPerBlockOptin);
     }

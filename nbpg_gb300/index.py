@@ -207,14 +207,21 @@ class SearchGraph:
             pass
 
 
+GT_ENGINES = {"auto": 0, "dp4a": 1, "tensor": 2}
+
+
 def ground_truth(base: np.ndarray, queries: np.ndarray, dtype: str, metric: str = "l2", k: int = 100,
-                 exact: bool = False, device: int = 0):
-    """compute_groundtruth (CompGT.cpp:29-134) on the GPU: (ids, dists), rows sorted by (dist, id)."""
+                 exact: bool = False, device: int = 0, engine: str = "auto"):
+    """compute_groundtruth (CompGT.cpp:29-134) on the GPU: (ids, dists), rows sorted by (dist, id).
+
+    engine: "tensor" (tcgen05 bf16 MMA, rows of up to 128 codes, k <= 100), "dp4a"
+    (integer dot-product units, any row length, k <= 256) or "auto" (tensor where it applies)."""
     base = np.ascontiguousarray(base)
     queries = np.ascontiguousarray(queries)
     nq = queries.shape[0]
     ids = np.empty((nq, k), np.uint32)
     ds = np.empty((nq, k), np.float32)
-    check(_lib.lib().nbpg_gt(_lib.DTYPES[dtype], _lib.METRICS[metric], base.shape[1], base.ctypes.data, base.shape[0],
-                             queries.ctypes.data, nq, k, int(exact), _p(ids), _p(ds, _f32p), device))
+    check(_lib.lib().nbpg_gt_with_engine(_lib.DTYPES[dtype], _lib.METRICS[metric], base.shape[1], base.ctypes.data,
+                                    base.shape[0], queries.ctypes.data, nq, k, int(exact), GT_ENGINES[engine],
+                                    _p(ids), _p(ds, _f32p), device))
     return ids, ds

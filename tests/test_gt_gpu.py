@@ -23,14 +23,15 @@ def _data(kind):
     raise KeyError(kind)
 
 
+@pytest.mark.parametrize("engine", ["dp4a", "tensor"])
 @pytest.mark.parametrize("kind", ["mix", "tie", "i8", "u4", "d100"])
 @pytest.mark.parametrize("metric", ["l2", "ip"])
 @pytest.mark.parametrize("exact", [False, True])
-def test_gt_matches_oracle(gpu_lib, oracle_lib, kind, metric, exact):
+def test_gt_matches_oracle(gpu_lib, oracle_lib, kind, metric, exact, engine):
     from nbpg_gb300.index import ground_truth
     dtype, (base, q) = _data(kind)
     for k in (1, 10, 100):
-        ids, ds = ground_truth(base, q, dtype, metric, k=k, exact=exact)
+        ids, ds = ground_truth(base, q, dtype, metric, k=k, exact=exact, engine=engine)
         oi, od = oracle_lib.gt(dtype, metric, base, q, k=k, exact=exact)
         assert np.array_equal(ids, oi), (kind, metric, exact, k)
         assert np.array_equal(ds.view(np.uint32), od.view(np.uint32)), (kind, metric, exact, k)
@@ -43,8 +44,45 @@ def test_gt_edge_sizes(gpu_lib, oracle_lib):
     q = np.random.default_rng(2).integers(0, 256, (33, 16)).astype(np.uint8)       # ragged query block
     for k in (1, 100, 129):
         for exact in (False, True):
-            ids, ds = ground_truth(base, q, "u8", "l2", k=k, exact=exact)
-            oi, od = oracle_lib.gt("u8", "l2", base, q, k=k, exact=exact)
-            assert np.array_equal(ids, oi) and np.array_equal(ds, od)
+            for engine in (("dp4a", "tensor") if k <= 100 else ("dp4a", "auto")):
+                ids, ds = ground_truth(base, q, "u8", "l2", k=k, exact=exact, engine=engine)
+                oi, od = oracle_lib.gt("u8", "l2", base, q, k=k, exact=exact)
+                assert np.array_equal(ids, oi) and np.array_equal(ds, od), (k, exact, engine)
     with pytest.raises(NbpgError):
         ground_truth(base[:10], q, "u8", "l2", k=11)
+    with pytest.raises(NbpgError):  # k above the tensor engine's limit
+        ground_truth(base, q, "u8", "l2", k=101, engine="tensor")
+
+
+def test_gt_tensor_limits(gpu_lib, oracle_lib):
+    """Rows of 128 codes (the tensor engine's widest: u8 128, i4 64 bytes), 129 codes
+    (auto falls back to DP4A, tensor refuses), and query counts around the 128-query block."""
+    from nbpg_gb300 import synth
+    from nbpg_gb300._lib import NbpgError
+    from nbpg_gb300.index import ground_truth
+    r = np.random.default_rng(11)
+    b, q = synth.u8_mixture(3000, 257, dim=128, n_centres=8)
+    for nq in (1, 127, 128, 129, 257):
+        for exact in (False, True):
+            ids, ds = ground_truth(b, q[:nq], "u8", "l2", k=50, exact=exact, engine="tensor")
+            oi, od = oracle_lib.gt("u8", "l2", b, q[:nq], k=50, exact=exact)
+            assert np.array_equal(ids, oi) and np.array_equal(ds, od), (nq, exact)
+    i4b, i4q = r.integers(0, 256, (2000, 64)).astype(np.uint8), r.integers(0, 256, (40, 64)).astype(np.uint8)
+    for metric in ("l2", "ip"):
+        ids, ds = ground_truth(i4b, i4q, "i4", metric, k=20, engine="tensor")
+        oi, od = oracle_lib.gt("i4", metric, i4b, i4q, k=20)
+        assert np.array_equal(ids, oi) and np.array_equal(ds.view(np.uint32), od.view(np.uint32)), metric
+    # queries near zero and base rows far from it: the zero padding rows of the last
+    # tile would be every query's nearest neighbours if they were not excluded
+    far, near = r.integers(200, 256, (130, 16)).astype(np.uint8), r.integers(0, 4, (20, 16)).astype(np.uint8)
+    for exact in (False, True):
+        for metric in ("l2", "ip"):
+            ids, ds = ground_truth(far, near, "u8", metric, k=100, exact=exact, engine="tensor")
+            oi, od = oracle_lib.gt("u8", metric, far, near, k=100, exact=exact)
+            assert np.array_equal(ids, oi) and np.array_equal(ds.view(np.uint32), od.view(np.uint32)), (exact, metric)
+    w = r.integers(0, 256, (500, 129)).astype(np.uint8)
+    ids, ds = ground_truth(w, w[:9], "u8", "l2", k=10, engine="auto")
+    oi, od = oracle_lib.gt("u8", "l2", w, w[:9], k=10)
+    assert np.array_equal(ids, oi) and np.array_equal(ds, od)
+    with pytest.raises(NbpgError):
+        ground_truth(w, w[:9], "u8", "l2", k=10, engine="tensor")
