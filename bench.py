@@ -122,6 +122,57 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["bf16_tflops"]), "measured (cuBLAS bf16 burst)"
+    return 1900.0, "fallback"
+
+
+def time_gt_device(base, q, k, local, reps=3):
+    """Ground truth (CompGT mode) on device-resident data through nbpg_gt_device, both
+    engines, CUDA events on the launching stream; checks that the engines agree."""
+    import torch
+    from nbpg_gb300.index import ground_truth_device, gt_workspace_size
+    dev = torch.device("cuda", local)
+    n, dims = base.shape
+    nq = len(q)
+    db, dq = torch.from_numpy(base).to(dev), torch.from_numpy(q).to(dev)
+    st = torch.cuda.Stream(device=dev)
+    out, res = {}, {}
+    for eng in ("tensor", "dp4a"):
+        wsb = gt_workspace_size("u8", dims, n, nq, k, eng)
+        ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+        ids = torch.empty((nq, k), dtype=torch.int32, device=dev)
+        ds = torch.empty((nq, k), dtype=torch.float32, device=dev)
+
+        def call():
+            ground_truth_device(db.data_ptr(), n, dq.data_ptr(), nq, dims, dims, "u8", "l2", k, ids.data_ptr(),
+                                ds.data_ptr(), engine=eng, d_workspace=ws.data_ptr(), workspace_bytes=wsb,
+                                stream=st.cuda_stream)
+        call()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            call()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        out[f"{eng}_ms"] = e0.elapsed_time(e1) / reps
+        res[eng] = (ids.cpu().numpy(), ds.cpu().numpy())
+        del ws
+    peak, src = bf16_peak()
+    tflops = 2.0 * nq * n * dims / (out["tensor_ms"] * 1e-3) / 1e12
+    out.update({"engine": "tensor (tcgen05 bf16 MMA, TMEM accumulators, TMA)", "n_base": n, "n_query": nq, "k": k,
+                "mode": "CompGT", "achieved_tflops": tflops, "peak_tflops": peak, "frac": tflops / peak,
+                "peak_source": src, "includes": "bf16 conversion of base and queries + distance + top-k replay",
+                "engines_identical": bool(np.array_equal(res["tensor"][0], res["dp4a"][0]) and
+                                          np.array_equal(res["tensor"][1], res["dp4a"][1])),
+                "tensor_over_dp4a": out["dp4a_ms"] / out["tensor_ms"]})
+    return out
+
+
 def traffic_per_query():
     p = os.path.join(ROOT, "profiles", "search_traffic.json")
     if os.path.exists(p):
@@ -231,6 +282,7 @@ def main():
     ap.add_argument("--load-graph", default=None, help="use this graph instead of building one")
     ap.add_argument("--profile", default=None, choices=["search", "gt"],
                     help="profiling run: warmup + steps of one kernel only (the search at --L, or the brute-force kNN)")
+    ap.add_argument("--gt-engine", default="tensor", choices=["tensor", "dp4a"], help="--profile gt engine")
     ap.add_argument("--L", type=int, default=0, help="beam width for --profile (default: the sweep's choice)")
     ap.add_argument("--kernel", default="batched", choices=["batched", "plain"], help="--profile launch")
     ap.add_argument("--warps", type=int, default=0, help="--profile launch: warps per CTA")
@@ -257,6 +309,13 @@ def main():
     base, q = make_data()
     k = CFG["k"]
     nq = len(q)
+    if args.profile == "gt":
+        # brute-force kNN alone (no index): 1M x 128 u8 base, 10k queries, k=100, CompGT mode
+        for _ in range(args.warmup + args.steps):
+            ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local, engine=args.gt_engine)
+        print(json.dumps({"profile": "ground truth", "engine": args.gt_engine,
+                          "launches": args.warmup + args.steps}), flush=True)
+        return
 
     # index + build on the GPU
     from nbpg_gb300 import formats
@@ -278,17 +337,14 @@ def main():
     log(f"[bench] average degree {avg_deg:.2f}")
     if args.profile == "search":
         return profile_search(idx, q, args.L or 19, args)
-    if args.profile == "gt":
-        for _ in range(args.warmup + args.steps):
-            ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
-        print(json.dumps({"profile": "ground truth", "launches": args.warmup + args.steps}), flush=True)
-        return
-
     t = time.time()
     gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
     gt_s = time.time() - t
     log(f"[bench] GPU ground truth (CompGT mode) {gt_s:.2f}s")
     gei, ged = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=True, device=local)
+    gt_dev = time_gt_device(base, q, CFG["gt_k"], local)
+    log(f"[bench] ground truth on device: tensor {gt_dev['tensor_ms']:.2f} ms, DP4A {gt_dev['dp4a_ms']:.2f} ms, "
+        f"{gt_dev['achieved_tflops']:.1f} TFLOP/s, engines identical: {gt_dev['engines_identical']}")
 
     # L sweep (reference sweep values up to 200) with the batched kernel
     L_op, rec, sweep = None, 0.0, []
@@ -521,7 +577,7 @@ def main():
             "latency_ms": None if not serving else {"p50": serving["at_half_peak"]["p50_ms"],
                                                      "p99": serving["at_half_peak"]["p99_ms"],
                                                      "at_offered_qps": serving["at_half_peak"]["offered_qps"]},
-            "serving": serving}
+            "serving": serving, "ground_truth": gt_dev}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

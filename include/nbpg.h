@@ -241,6 +241,18 @@ nbpg_status nbpg_gt_with_engine(uint32_t dtype, uint32_t metric, uint32_t dims, 
                                 const void *queries, uint32_t nq, uint32_t k, uint32_t mode, uint32_t engine,
                                 uint32_t *out_ids, float *out_dists, int32_t device);
 
+/* Device-resident form, on the current device and `stream` (a cudaStream_t; NULL = the
+ * legacy default stream).  Rows are row_stride bytes apart (a multiple of 16, >= dims;
+ * bytes past dims must be zero), both arrays 16-byte aligned.  The tensor engine needs
+ * nbpg_gt_workspace_size() bytes of device workspace (0 for DP4A); d_workspace NULL
+ * makes the call allocate it.  Returns after the work has finished on `stream`. */
+nbpg_status nbpg_gt_workspace_size(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq, uint32_t k,
+                                   uint32_t engine, size_t *bytes);
+nbpg_status nbpg_gt_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t row_stride, const void *d_base,
+                           uint64_t n, const void *d_queries, uint32_t nq, uint32_t k, uint32_t mode,
+                           uint32_t engine, uint32_t *d_ids, float *d_dists, void *d_workspace,
+                           size_t workspace_bytes, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Build.  Replaces build_vamana (algorithms/nsw.h:547-663) with NSWIndex::batch_insert
  * (nsw.h:110-286), RobustPrune (algorithms/utils/Graph/prune.h:159-209), reverse-edge

@@ -105,6 +105,10 @@ def lib() -> C.CDLL:
                           C.c_uint32, _u32p, _f32p, C.c_int32]
     L.nbpg_gt_with_engine.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, _u32p, _f32p, C.c_int32]
+    L.nbpg_gt_workspace_size.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                                         C.POINTER(C.c_size_t)]
+    L.nbpg_gt_device.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32,
+                                 C.c_uint32, C.c_uint32, C.c_uint32, _vp, _vp, _vp, C.c_size_t, _vp]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
     _lib = L
     return L

@@ -282,7 +282,8 @@ static cudaError_t launch_gt(const GtArgs &a, size_t smem, cudaStream_t st)
 bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_optin);
 nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t stride, const uint8_t *d_base,
                          uint64_t n, const uint8_t *d_q, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *d_ids,
-                         float *d_dists, cudaStream_t st);
+                         float *d_dists, void *ws, cudaStream_t st);
+size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq);
 
 nbpg_status gt_device(uint32_t dtype, uint32_t metric, const GtArgs &a, cudaStream_t st, size_t smem_optin)
 {
@@ -362,7 +363,7 @@ extern "C" nbpg_status nbpg_gt_with_engine(uint32_t dtype, uint32_t metric, uint
         s = NBPG_ERR_UNSUPPORTED;
     }
     if (s == NBPG_OK && engine != NBPG_GT_DP4A && tc_ok) {
-        s = gt_tc_device(dtype, metric, dims, rs, db, n, dq, nq, k, mode, di, dd, st);
+        s = gt_tc_device(dtype, metric, dims, rs, db, n, dq, nq, k, mode, di, dd, nullptr, st);
     } else if (s == NBPG_OK) {
         GtArgs a{db, n, rs, dq, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, di, dd};
         s = gt_device(dtype, metric, a, st, prop.sharedMemPerBlockOptin);
@@ -379,5 +380,67 @@ extern "C" nbpg_status nbpg_gt_with_engine(uint32_t dtype, uint32_t metric, uint
     cudaFree(di);
     cudaFree(dd);
     cudaStreamDestroy(st);
+    return s;
+}
+
+// Engine that a call with these arguments runs (AUTO resolved), or NBPG_ERR_UNSUPPORTED.
+static nbpg_status resolve_engine(uint32_t dtype, uint32_t dims, uint32_t k, uint32_t engine, uint32_t *out)
+{
+    int dev = 0;
+    NBPG_CUDA_TRY(cudaGetDevice(&dev));
+    int optin = 0;
+    NBPG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const bool tc_ok = gt_tc_supported(dtype, dims, k, size_t(optin));
+    if (engine == NBPG_GT_TENSOR && !tc_ok) {
+        set_error("nbpg_gt: the tensor engine needs <= 128 codes per row and k <= 100");
+        return NBPG_ERR_UNSUPPORTED;
+    }
+    *out = (engine != NBPG_GT_DP4A && tc_ok) ? uint32_t(NBPG_GT_TENSOR) : uint32_t(NBPG_GT_DP4A);
+    return NBPG_OK;
+}
+
+extern "C" nbpg_status nbpg_gt_workspace_size(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq, uint32_t k,
+                                              uint32_t engine, size_t *bytes)
+{
+    NBPG_CHECK_ARG(bytes, "null argument");
+    NBPG_CHECK_ARG(dtype <= NBPG_I4 && dims >= 1 && engine <= NBPG_GT_TENSOR, "bad dtype/dims/engine");
+    uint32_t eng = 0;
+    const nbpg_status s = resolve_engine(dtype, dims, k, engine, &eng);
+    if (s != NBPG_OK) return s;
+    *bytes = eng == NBPG_GT_TENSOR ? gt_tc_workspace(dtype, dims, n, nq) : 0;
+    return NBPG_OK;
+}
+
+extern "C" nbpg_status nbpg_gt_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t row_stride,
+                                      const void *d_base, uint64_t n, const void *d_queries, uint32_t nq, uint32_t k,
+                                      uint32_t mode, uint32_t engine, uint32_t *d_ids, float *d_dists,
+                                      void *d_workspace, size_t workspace_bytes, void *stream)
+{
+    NBPG_CHECK_ARG(d_base && d_queries && d_ids && d_dists, "null argument");
+    NBPG_CHECK_ARG(dtype <= NBPG_I4 && metric <= NBPG_IP, "unsupported dtype/metric");
+    NBPG_CHECK_ARG(k >= 1 && k <= 256, "k must be in [1, 256]");
+    NBPG_CHECK_ARG(n >= k && n < 0xFFFFFFFFull, "need k <= n < 2^32-1");
+    NBPG_CHECK_ARG(dims >= 1 && mode <= NBPG_GT_EXACT && engine <= NBPG_GT_TENSOR, "bad dims/mode/engine");
+    NBPG_CHECK_ARG(row_stride >= dims && row_stride % 16 == 0, "row_stride must be >= dims and a multiple of 16");
+    NBPG_CHECK_ARG((reinterpret_cast<uintptr_t>(d_base) | reinterpret_cast<uintptr_t>(d_queries)) % 16 == 0,
+                   "base and queries must be 16-byte aligned");
+    if (nq == 0) return NBPG_OK;
+    uint32_t eng = 0;
+    nbpg_status s = resolve_engine(dtype, dims, k, engine, &eng);
+    if (s != NBPG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (eng == NBPG_GT_TENSOR) {
+        const size_t need = gt_tc_workspace(dtype, dims, n, nq);
+        NBPG_CHECK_ARG(!d_workspace || workspace_bytes >= need, "workspace smaller than nbpg_gt_workspace_size");
+        return gt_tc_device(dtype, metric, dims, row_stride, static_cast<const uint8_t *>(d_base), n,
+                            static_cast<const uint8_t *>(d_queries), nq, k, mode, d_ids, d_dists, d_workspace, st);
+    }
+    int dev = 0, optin = 0;
+    NBPG_CUDA_TRY(cudaGetDevice(&dev));
+    NBPG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    GtArgs a{static_cast<const uint8_t *>(d_base), n, row_stride, static_cast<const uint8_t *>(d_queries), nq, k,
+             mode == NBPG_GT_EXACT ? 1u : 0u, d_ids, d_dists};
+    s = gt_device(dtype, metric, a, st, size_t(optin));
+    if (s == NBPG_OK) NBPG_CUDA_TRY(cudaStreamSynchronize(st));
     return s;
 }

@@ -462,27 +462,64 @@ bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_opti
     return gt_tc_smem(katoms, k) <= smem_optin;
 }
 
-// Device-resident inputs (rows of dims bytes, stride bytes apart); outputs device arrays nq*k.
+// Workspace of the tensor engine: bf16 rows of base and queries (K = codes rounded up to
+// 64), fp32 squared norms, and the error flag; regions 256-byte aligned.
+struct TcLayout {
+    uint32_t K, katoms;
+    uint64_t n_pad, nq_pad;
+    size_t off_bq, off_bn, off_qn, off_err, bytes;
+};
+
+static TcLayout tc_layout(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq)
+{
+    TcLayout l;
+    const uint32_t elems = (dtype == NBPG_U4 || dtype == NBPG_I4) ? 2 * dims : dims;
+    l.K = (elems + TC_KATOM - 1) / TC_KATOM * TC_KATOM;
+    l.katoms = l.K / TC_KATOM;
+    l.n_pad = (n + TC_N - 1) / TC_N * TC_N;
+    l.nq_pad = (uint64_t(nq) + TC_M - 1) / TC_M * TC_M;
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    l.off_bq = up(l.n_pad * l.K * 2);
+    l.off_bn = l.off_bq + up(l.nq_pad * l.K * 2);
+    l.off_qn = l.off_bn + up(l.n_pad * 4);
+    l.off_err = l.off_qn + up(l.nq_pad * 4);
+    l.bytes = l.off_err + 256;
+    return l;
+}
+
+size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq)
+{
+    return tc_layout(dtype, dims, n, nq).bytes;
+}
+
+// Device-resident inputs (rows of dims bytes, stride bytes apart); outputs device arrays
+// nq*k.  ws: gt_tc_workspace() bytes, or NULL to allocate them here.  Returns after the
+// kernel has finished (the error flag of the bounded waits is read back).
 nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t stride, const uint8_t *d_base,
                          uint64_t n, const uint8_t *d_q, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *d_ids,
-                         float *d_dists, cudaStream_t st)
+                         float *d_dists, void *ws, cudaStream_t st)
 {
     const bool nib = dtype == NBPG_U4 || dtype == NBPG_I4;
-    const uint32_t elems = nib ? 2 * dims : dims;
-    const uint32_t K = (elems + TC_KATOM - 1) / TC_KATOM * TC_KATOM;
-    const uint32_t katoms = K / TC_KATOM;
-    const uint64_t n_pad = (n + TC_N - 1) / TC_N * TC_N;
-    const uint64_t nq_pad = (uint64_t(nq) + TC_M - 1) / TC_M * TC_M;
-    __nv_bfloat16 *bB = nullptr, *bQ = nullptr;
-    float *bn = nullptr, *qn = nullptr;
-    uint32_t *err = nullptr;
+    const TcLayout l = tc_layout(dtype, dims, n, nq);
+    const uint32_t K = l.K;
+    const uint64_t n_pad = l.n_pad, nq_pad = l.nq_pad;
+    void *owned = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!ws) {
+        e = cudaMalloc(&owned, l.bytes);
+        if (e != cudaSuccess) {
+            set_error(std::string("nbpg_gt (tensor path): ") + cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? NBPG_ERR_OOM : NBPG_ERR_CUDA;
+        }
+        ws = owned;
+    }
+    uint8_t *w = static_cast<uint8_t *>(ws);
+    __nv_bfloat16 *bB = reinterpret_cast<__nv_bfloat16 *>(w);
+    __nv_bfloat16 *bQ = reinterpret_cast<__nv_bfloat16 *>(w + l.off_bq);
+    float *bn = reinterpret_cast<float *>(w + l.off_bn), *qn = reinterpret_cast<float *>(w + l.off_qn);
+    uint32_t *err = reinterpret_cast<uint32_t *>(w + l.off_err);
     nbpg_status s = NBPG_OK;
-    cudaError_t e = cudaMalloc(&bB, n_pad * K * 2);
-    if (e == cudaSuccess) e = cudaMalloc(&bQ, nq_pad * K * 2);
-    if (e == cudaSuccess) e = cudaMalloc(&bn, n_pad * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&qn, nq_pad * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&err, 4);
-    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, 4, st);
+    e = cudaMemsetAsync(err, 0, 4, st);
     if (e == cudaSuccess) {
         const uint32_t thr = 128;
         switch (dtype) {
@@ -505,12 +542,12 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
         set_error("nbpg_gt: tensor map encoding failed");
         s = NBPG_ERR_CUDA;
     }
-    const size_t smem = gt_tc_smem(katoms, k);
+    const size_t smem = gt_tc_smem(l.katoms, k);
     if (e == cudaSuccess && s == NBPG_OK)
         e = cudaFuncSetAttribute(metric == NBPG_L2 ? gt_tc_kernel<M_L2> : gt_tc_kernel<M_IP>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e == cudaSuccess && s == NBPG_OK) {
-        TcArgs a{qn, bn, n, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, nib ? 256u : 1u, katoms,
+        TcArgs a{qn, bn, n, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, nib ? 256u : 1u, l.katoms,
                  uint32_t(n_pad / TC_N), d_ids, d_dists, err};
         if (metric == NBPG_L2) gt_tc_kernel<M_L2><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
         else gt_tc_kernel<M_IP><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
@@ -527,11 +564,10 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
         set_error("nbpg_gt (tensor path): a pipeline wait timed out");
         s = NBPG_ERR_TIMEOUT;
     }
-    cudaFree(bB);
-    cudaFree(bQ);
-    cudaFree(bn);
-    cudaFree(qn);
-    cudaFree(err);
+    if (owned) {
+        cudaStreamSynchronize(st);
+        cudaFree(owned);
+    }
     return s;
 }
 

@@ -225,3 +225,20 @@ def ground_truth(base: np.ndarray, queries: np.ndarray, dtype: str, metric: str 
                                     base.shape[0], queries.ctypes.data, nq, k, int(exact), GT_ENGINES[engine],
                                     _p(ids), _p(ds, _f32p), device))
     return ids, ds
+
+
+def gt_workspace_size(dtype: str, dims: int, n: int, nq: int, k: int, engine: str = "auto") -> int:
+    """Device workspace bytes that ground_truth_device needs (0 for the DP4A engine)."""
+    out = C.c_size_t(0)
+    check(_lib.lib().nbpg_gt_workspace_size(_lib.DTYPES[dtype], dims, n, nq, k, GT_ENGINES[engine], C.byref(out)))
+    return out.value
+
+
+def ground_truth_device(d_base: int, n: int, d_queries: int, nq: int, dims: int, row_stride: int, dtype: str,
+                        metric: str, k: int, d_out_ids: int, d_out_dists: int, exact: bool = False,
+                        engine: str = "auto", d_workspace: int = 0, workspace_bytes: int = 0, stream: int = 0):
+    """ground_truth on device buffers (raw addresses), on the current device and `stream`;
+    returns when the results are in d_out_ids / d_out_dists (nq x k each)."""
+    check(_lib.lib().nbpg_gt_device(_lib.DTYPES[dtype], _lib.METRICS[metric], dims, row_stride, d_base, n, d_queries,
+                                    nq, k, int(exact), GT_ENGINES[engine], d_out_ids, d_out_dists,
+                                    d_workspace or None, workspace_bytes, stream or None))

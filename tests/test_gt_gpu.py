@@ -86,3 +86,31 @@ def test_gt_tensor_limits(gpu_lib, oracle_lib):
     assert np.array_equal(ids, oi) and np.array_equal(ds, od)
     with pytest.raises(NbpgError):
         ground_truth(w, w[:9], "u8", "l2", k=10, engine="tensor")
+
+
+@pytest.mark.parametrize("engine", ["dp4a", "tensor"])
+def test_gt_device_entry(gpu_lib, oracle_lib, engine):
+    """nbpg_gt_device on device buffers with padded rows, caller workspace and internal allocation."""
+    import torch
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import ground_truth_device, gt_workspace_size
+    b, q = synth.u8_mixture(4000, 150, dim=40, n_centres=12)
+    stride = 48
+    pb, pq = np.zeros((len(b), stride), np.uint8), np.zeros((len(q), stride), np.uint8)
+    pb[:, :40], pq[:, :40] = b, q
+    dev = torch.device("cuda", 0)
+    db, dq = torch.from_numpy(pb).to(dev), torch.from_numpy(pq).to(dev)
+    k = 20
+    wsb = gt_workspace_size("u8", 40, len(b), len(q), k, engine)
+    assert (wsb > 0) == (engine == "tensor")
+    for use_ws in (True, False):
+        ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+        ids = torch.empty((len(q), k), dtype=torch.int32, device=dev)
+        ds = torch.empty((len(q), k), dtype=torch.float32, device=dev)
+        for exact in (False, True):
+            ground_truth_device(db.data_ptr(), len(b), dq.data_ptr(), len(q), 40, stride, "u8", "l2", k,
+                                ids.data_ptr(), ds.data_ptr(), exact=exact, engine=engine,
+                                d_workspace=ws.data_ptr() if use_ws else 0, workspace_bytes=wsb if use_ws else 0)
+            oi, od = oracle_lib.gt("u8", "l2", b, q, k=k, exact=exact)
+            assert np.array_equal(ids.cpu().numpy().view(np.uint32), oi), (use_ws, exact)
+            assert np.array_equal(ds.cpu().numpy(), od), (use_ws, exact)
