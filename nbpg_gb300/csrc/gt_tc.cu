@@ -11,7 +11,7 @@
 //
 // One CTA owns 128 queries (the MMA's M = the 128 TMEM lanes) and walks the base in
 // id order in tiles of 128 rows (N).  Warp 4 loads tiles with TMA (128-byte swizzle)
-// into a two-stage ring; warp 5 issues tcgen05.mma into one of two TMEM accumulators;
+// into a ring of 2-4 stages; warp 5 issues tcgen05.mma into one of four TMEM accumulators;
 // warps 0-3 are the epilogue: thread t reads lane t (query t) of the accumulator with
 // tcgen05.ld and replays the admission rule for its query over the tile's ids in order
 // (CompGT's replace-max with its stale read, or an exact sorted top-k).  All waits on
@@ -31,9 +31,11 @@ namespace nbpg {
 constexpr int TC_M = 128;        // queries per CTA
 constexpr int TC_N = 128;        // base rows per tile
 constexpr int TC_KATOM = 64;     // bf16 elements per 128-byte swizzled row
-constexpr int TC_STAGES = 2;
+constexpr uint32_t TC_MAX_STAGES = 4;  // shared-memory ring of base tiles: 2..4 deep as memory allows
+constexpr uint32_t TC_ACC = 4;         // TMEM accumulators of 128 columns: all 512 columns of the SM
 constexpr int TC_THREADS = 192;  // warps 0-3 epilogue, 4 TMA, 5 MMA
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+constexpr uint32_t TC_QUEUE = 8;  // flagged candidates queued per query before a drain
 
 struct TcArgs {
     const float *qnorm;  // nq_pad squared norms (exact integers)
@@ -42,6 +44,7 @@ struct TcArgs {
     uint32_t nq, k, exact, scale;  // scale: 1, or 256 for 4-bit codes
     uint32_t katoms;               // K / 64
     uint32_t ntiles;
+    uint32_t stages;               // depth of the base-tile ring
     uint32_t *out_ids;
     float *out_dists;
     uint32_t *err;
@@ -137,6 +140,148 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32])
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Per-query top-k list in shared memory, [k][128] so that thread t's entries stride 128,
+// with a tournament tree over list slots [lo, k) whose internal nodes (1 .. P-1, P the
+// power of two >= k - lo) hold the slot of their subtree's largest entry; a tie goes to
+// the lower slot, which is the first maximum of a left-to-right scan.  CompGT keeps
+// slots 1..k-1 in the tree (its rescan is seeded with slot 0, CompGT.cpp:82-90); the
+// exact mode keeps all k slots and orders ties by id (the larger id is the larger key).
+struct TkList {
+    float *d;        // [k][128] in shared memory
+    uint32_t *id;    // k ids: this query's row of the output (written on admission, read on ties)
+    uint8_t *win;    // [128 nodes][128]
+    int tid;
+    uint32_t k, lo, P, exact;
+};
+
+// Running state of one query's list.  CompGT: CompGT's toppos/topdist and the list
+// maximum.  Exact: top = slot of the largest key, topdist = its distance.
+struct TkState {
+    uint32_t cnt, toppos;
+    float topdist, lmax;
+};
+
+constexpr uint32_t kNoSlot = 0xFF;
+
+__device__ __forceinline__ uint32_t tt_node(const TkList &L, uint32_t x)
+{
+    if (x >= L.P) {
+        const uint32_t slot = L.lo + (x - L.P);
+        return slot < L.k ? slot : kNoSlot;
+    }
+    return L.win[x * TC_M + L.tid];
+}
+
+__device__ __forceinline__ uint32_t tt_pick(const TkList &L, uint32_t a, uint32_t b)
+{
+    if (b == kNoSlot) return a;
+    if (a == kNoSlot) return b;
+    const float da = L.d[a * TC_M + L.tid], db = L.d[b * TC_M + L.tid];
+    if (db != da) return db > da ? b : a;
+    return (L.exact && L.id[b] > L.id[a]) ? b : a;
+}
+
+__device__ __forceinline__ uint32_t tt_root(const TkList &L)
+{
+    return L.P > 1 ? uint32_t(L.win[TC_M + L.tid]) : (L.lo < L.k ? L.lo : kNoSlot);
+}
+
+__device__ __noinline__ void tt_build(const TkList &L)
+{
+    for (uint32_t x = L.P - 1; x >= 1; --x)
+        L.win[x * TC_M + L.tid] = uint8_t(tt_pick(L, tt_node(L, 2 * x), tt_node(L, 2 * x + 1)));
+}
+
+// Slot `slot` now holds (dv, iv): replay the matches on its path to the root, carrying
+// the winner so far; returns the new root slot.
+__device__ __forceinline__ uint32_t tt_update(const TkList &L, uint32_t slot, float dv, uint32_t iv)
+{
+    const int t = L.tid;
+    uint32_t cur = L.P + slot - L.lo, w = slot, wi = iv;
+    float wd = dv;
+    while (cur > 1) {
+        const uint32_t sib = cur ^ 1u;
+        const uint32_t ws = tt_node(L, sib);
+        if (ws != kNoSlot) {
+            const float ds = L.d[ws * TC_M + t];
+            bool sw;
+            if (ds != wd) sw = ds > wd;
+            else sw = L.exact ? L.id[ws] > wi : sib < cur;  // CompGT: the lower slot
+            if (sw) {
+                w = ws;
+                wd = ds;
+                if (L.exact) wi = L.id[ws];
+            }
+        }
+        cur >>= 1;
+        L.win[cur * TC_M + t] = uint8_t(w);
+    }
+    return w;
+}
+
+// v[j] for a j known only at run time, by a tree of selects (registers stay registers)
+template <typename T>
+__device__ __forceinline__ T pick32(const T (&v)[32], uint32_t j)
+{
+    T a[16], b[8], c[4], d[2];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) a[i] = (j & 16) ? v[i + 16] : v[i];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = (j & 8) ? a[i + 8] : a[i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[i] = (j & 4) ? b[i + 4] : b[i];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) d[i] = (j & 2) ? c[i + 2] : c[i];
+    return (j & 1) ? d[1] : d[0];
+}
+
+// Offer a candidate (ids arrive in increasing order) and return the survivor bound B:
+// +inf until the list holds k entries.
+__device__ __forceinline__ float tk_offer(const TkList &L, TkState &S, float dist, uint32_t id)
+{
+    const int t = L.tid;
+    const float kInf = __int_as_float(0x7f800000);
+    if (!L.exact) {
+        // CompGT.cpp:71-95
+        if (S.cnt < L.k) {
+            if (dist > S.topdist) { S.topdist = dist; S.toppos = S.cnt; }
+            S.lmax = fmaxf(S.lmax, dist);
+            L.d[S.cnt * TC_M + t] = dist;
+            L.id[S.cnt] = id;
+            if (++S.cnt == L.k) tt_build(L);
+        } else if (dist < S.topdist) {
+            // overwrite toppos; the rescan over slots 1..k-1 starts from topk[0] read before the write
+            const float old0 = L.d[t];
+            const uint32_t p = S.toppos;
+            L.d[p * TC_M + t] = dist;
+            L.id[p] = id;
+            const uint32_t r = p >= 1 ? tt_update(L, p, dist, id) : tt_root(L);
+            const float m1 = r == kNoSlot ? -kInf : L.d[r * TC_M + t];
+            if (m1 > old0) { S.topdist = m1; S.toppos = r; }
+            else { S.topdist = old0; S.toppos = 0; }
+            S.lmax = fmaxf(p == 0 ? dist : old0, m1);
+        }
+        return S.cnt < L.k ? kInf : fmaxf(S.topdist, S.lmax);
+    }
+    // exact: replace the largest key; a later id never wins a tie
+    if (S.cnt < L.k) {
+        L.d[S.cnt * TC_M + t] = dist;
+        L.id[S.cnt] = id;
+        if (++S.cnt == L.k) {
+            tt_build(L);
+            S.toppos = tt_root(L);
+            S.topdist = L.d[S.toppos * TC_M + t];
+        }
+    } else if (dist < S.topdist) {
+        const uint32_t r = S.toppos;
+        L.d[r * TC_M + t] = dist;
+        L.id[r] = id;
+        S.toppos = tt_update(L, r, dist, id);
+        S.topdist = L.d[S.toppos * TC_M + t];
+    }
+    return S.cnt < L.k ? kInf : S.topdist;
+}
+
 // Epilogue of one query (one thread, one TMEM lane).  Per 32-column chunk a cheap test
 // flags the candidates whose distance is below the survivor bound B; only those are
 // replayed through the admission rule, in id order.
@@ -149,12 +294,6 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32])
 // IP = -(q.b) * scale; the tests compare on the accumulator side (q.b, |b|^2 - 2 q.b) against
 // B / scale shifted by |q|^2, all exact below 2^24.
 template <int MET>
-__device__ __forceinline__ float accum_threshold(float B, float inv_scale, float qn)
-{
-    return MET == M_L2 ? B * inv_scale - qn : -B * inv_scale;
-}
-
-template <int MET>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gt_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a)
 {
@@ -164,20 +303,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t atom_bytes = TC_M * 128;  // one 64-element column of 128 rows (A and B tiles alike)
     const uint32_t tile_bytes = a.katoms * atom_bytes;
     uint8_t *sA = smem;
-    uint8_t *sB = smem + tile_bytes;                                        // TC_STAGES tiles
-    float *scr = reinterpret_cast<float *>(sB + TC_STAGES * tile_bytes);     // [32][128] flagged accumulators
-    uint64_t *bars = reinterpret_cast<uint64_t *>(scr + 32 * TC_M);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 16);
+    uint8_t *sB = smem + tile_bytes;                                        // a.stages tiles
+    uint8_t *win = sB + a.stages * tile_bytes;                              // [128][128] tree nodes
+    float *qv = reinterpret_cast<float *>(win + TC_M * TC_M);               // [TC_QUEUE][128] queued accumulators
+    uint32_t *qi = reinterpret_cast<uint32_t *>(qv + TC_QUEUE * TC_M);        // [TC_QUEUE][128] queued ids
+    uint64_t *bars = reinterpret_cast<uint64_t *>(qi + TC_QUEUE * TC_M);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 24);
     float *tk_d = reinterpret_cast<float *>(tmem_slot + 4);                 // [k][128]
-    uint32_t *tk_i = reinterpret_cast<uint32_t *>(tk_d + size_t(a.k) * TC_M);  // [k][128]
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t bar_full = smem_u32(bars + 0), bar_empty = smem_u32(bars + 2), bar_tfull = smem_u32(bars + 4),
-                   bar_tempty = smem_u32(bars + 6), bar_a = smem_u32(bars + 8), bar_done = smem_u32(bars + 9);
+    // full/empty: the base-tile ring; tfull/tempty: the TMEM accumulators
+    const uint32_t bar_full = smem_u32(bars + 0), bar_empty = smem_u32(bars + TC_MAX_STAGES),
+                   bar_tfull = smem_u32(bars + 2 * TC_MAX_STAGES),
+                   bar_tempty = smem_u32(bars + 2 * TC_MAX_STAGES + TC_ACC),
+                   bar_a = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC),
+                   bar_done = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 1);
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (uint32_t s = 0; s < a.stages; ++s) {
             mbar_init(bar_full + 8 * s, 1);
             mbar_init(bar_empty + 8 * s, 1);
+        }
+        for (uint32_t s = 0; s < TC_ACC; ++s) {
             mbar_init(bar_tfull + 8 * s, 1);
             mbar_init(bar_tempty + 8 * s, TC_M);
         }
@@ -186,7 +332,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 4) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -202,40 +348,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_expect_tx(bar_a, tile_bytes);
             for (uint32_t c = 0; c < a.katoms; ++c)
                 tma_load_2d(smem_u32(sA + c * atom_bytes), &tmA, int32_t(c * TC_KATOM), int32_t(q0), bar_a);
-            int64_t last0 = -1, last1 = -1;  // last tile issued on each stage
+            uint32_t issued = 0, s = 0, ph = 0;
             for (uint32_t t = 0; t < T; ++t) {
-                const uint32_t s = t & 1, ph = (t >> 1) & 1;
                 if (!mbar_wait(bar_empty + 8 * s, ph ^ 1, a.err)) break;
                 mbar_expect_tx(bar_full + 8 * s, tile_bytes);
                 for (uint32_t c = 0; c < a.katoms; ++c)
                     tma_load_2d(smem_u32(sB + s * tile_bytes + c * atom_bytes), &tmB, int32_t(c * TC_KATOM),
                                 int32_t(t * TC_N), bar_full + 8 * s);
-                if (s) last1 = t;
-                else last0 = t;
+                ++issued;
+                if (++s == a.stages) { s = 0; ph ^= 1; }
             }
             // every copy this thread issued has landed before the CTA may exit
             mbar_wait(bar_a, 0, a.err);
-            if (last0 >= 0) mbar_wait(bar_full, uint32_t(last0 >> 1) & 1, a.err);
-            if (last1 >= 0) mbar_wait(bar_full + 8, uint32_t(last1 >> 1) & 1, a.err);
+            for (uint32_t t = issued > a.stages ? issued - a.stages : 0; t < issued; ++t)
+                mbar_wait(bar_full + 8 * (t % a.stages), (t / a.stages) & 1, a.err);
         }
         __syncwarp();
     } else if (warp == 5) {
         if (lane == 0) {
             const uint32_t idesc = tc_idesc(TC_M, TC_N);
             bool ok = mbar_wait(bar_a, 0, a.err);
+            uint32_t s = 0, ph = 0;
             for (uint32_t t = 0; ok && t < T; ++t) {
-                const uint32_t s = t & 1, ph = (t >> 1) & 1;
+                const uint32_t ts = t % TC_ACC, tph = (t / TC_ACC) & 1;  // TMEM accumulator
                 if (!mbar_wait(bar_full + 8 * s, ph, a.err)) break;
-                if (!mbar_wait(bar_tempty + 8 * s, ph ^ 1, a.err)) break;
+                if (!mbar_wait(bar_tempty + 8 * ts, tph ^ 1, a.err)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t d = tmem + s * TC_N;
+                const uint32_t d = tmem + ts * TC_N;
                 const uint32_t aB = smem_u32(sA), bB = smem_u32(sB + s * tile_bytes);
                 for (uint32_t kk = 0; kk < a.katoms * (TC_KATOM / 16); ++kk) {
                     const uint32_t off = (kk >> 2) * atom_bytes + (kk & 3) * 32;  // 16 bf16 = 32 B per step
                     tc_mma(d, sw128_desc(aB + off), sw128_desc(bB + off), idesc, kk > 0 ? 1u : 0u);
                 }
-                tc_commit(bar_empty + 8 * s);  // operands of stage s consumed
-                tc_commit(bar_tfull + 8 * s);  // accumulator s ready
+                tc_commit(bar_empty + 8 * s);    // operands of stage s consumed
+                tc_commit(bar_tfull + 8 * ts);   // accumulator ts ready
+                if (++s == a.stages) { s = 0; ph ^= 1; }
             }
             // all issued MMAs complete before teardown
             tc_commit(bar_done);
@@ -249,132 +396,149 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t k = a.k;
         const float scale = float(a.scale), inv_scale = 1.0f / float(a.scale);  // 1 or 256: exact
         const float kInf = __int_as_float(0x7f800000);
-        uint32_t cnt = 0, toppos = 0;
-        float topdist = -3.402823466e38f, lmax = -3.402823466e38f;
-        float thr = MET == M_L2 ? kInf : -kInf;  // everything passes until the list holds k entries
+        TkList L;
+        L.d = tk_d;
+        L.id = live ? a.out_ids + size_t(q) * k : nullptr;
+        L.win = win;
+        L.tid = tid;
+        L.k = k;
+        L.exact = a.exact;
+        L.lo = a.exact ? 0u : 1u;
+        L.P = 1;
+        while (L.P < k - L.lo) L.P <<= 1;
+        TkState S{0u, 0u, -3.402823466e38f, -3.402823466e38f};
+        uint32_t qlen = 0;  // queued flagged candidates, in id order
+        // t_j = |b|^2 - 2 q.b (L2) or -q.b (IP) per candidate: the distance / scale minus
+        // |q|^2 (L2).  A candidate can survive only if t_j < thr = B / scale - |q|^2.
+        // Until the list holds k entries everything passes; padding queries never do.
+        float thr = live ? kInf : -kInf;
+        float4 bn_next[8];
+        if constexpr (MET == M_L2) {
+            const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) bn_next[j] = __ldg(bp + j);
+        }
         for (uint32_t t = 0; t < T; ++t) {
-            const uint32_t s = t & 1, ph = (t >> 1) & 1;
+            const uint32_t s = t % TC_ACC, ph = (t / TC_ACC) & 1;
             // warp-uniform wait so that the warp stays converged for tcgen05.ld
             const bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             for (uint32_t c = 0; c < TC_N / 32; ++c) {
                 const uint64_t id0 = uint64_t(t) * TC_N + c * 32;
-                float4 bn[8];
+                float bn[32];
                 if constexpr (MET == M_L2) {
-                    const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm + id0);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) bn[j] = __ldg(bp + j);
+                    for (int j = 0; j < 8; ++j) {
+                        bn[4 * j] = bn_next[j].x;
+                        bn[4 * j + 1] = bn_next[j].y;
+                        bn[4 * j + 2] = bn_next[j].z;
+                        bn[4 * j + 3] = bn_next[j].w;
+                    }
+                    // the next chunk's norms (n_pad entries; the last chunk re-reads its own)
+                    const uint64_t nx = id0 + 32 < uint64_t(T) * TC_N ? id0 + 32 : id0;
+                    const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm + nx);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) bn_next[j] = __ldg(bp + j);
                 }
                 uint32_t v[32];
                 __syncwarp();
                 tc_ld32(tmem + (uint32_t(warp * 32) << 16) + s * TC_N + c * 32, v);
-                // ids at or past n are zero padding rows of the last tile
-                uint32_t mask = 0;
-                if (live && id0 < a.n) mask = a.n - id0 >= 32 ? kFull : (1u << uint32_t(a.n - id0)) - 1u;
-                uint32_t pass = 0;
+                // chunk minimum of t_j by a tree (independent operations)
+                float m[16];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float acc = __uint_as_float(v[j]);
-                    bool p;
-                    if constexpr (MET == M_L2) {
-                        const float4 b4 = bn[j >> 2];
-                        const float bj = (j & 3) == 0 ? b4.x : (j & 3) == 1 ? b4.y : (j & 3) == 2 ? b4.z : b4.w;
-                        p = fmaf(-2.0f, acc, bj) < thr;
-                    } else {
-                        p = acc > thr;
-                    }
-                    pass |= uint32_t(p) << j;
+                for (int j = 0; j < 16; ++j) {
+                    if constexpr (MET == M_L2)
+                        m[j] = fminf(fmaf(-2.0f, __uint_as_float(v[j]), bn[j]),
+                                     fmaf(-2.0f, __uint_as_float(v[j + 16]), bn[j + 16]));
+                    else
+                        m[j] = fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 16]));
                 }
-                mask &= pass;
-                if (mask) {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if ((mask >> j) & 1u) scr[j * TC_M + tid] = __uint_as_float(v[j]);
-                    do {
-                        const int j = __ffs(mask) - 1;
+                for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+                    for (int j = 0; j < w; ++j) m[j] = MET == M_L2 ? fminf(m[j], m[j + w]) : fmaxf(m[j], m[j + w]);
+                const float tmin = MET == M_L2 ? m[0] : -m[0];
+                // flagged candidates of this chunk; ids at or past n are zero padding rows of the last tile
+                uint32_t mask = 0;
+                if (tmin < thr) {
+                    if (id0 < a.n) mask = a.n - id0 >= 32 ? kFull : (1u << uint32_t(a.n - id0)) - 1u;
+                    uint32_t pass = 0;
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const float tj =
+                            MET == M_L2 ? fmaf(-2.0f, __uint_as_float(v[j]), bn[j]) : -__uint_as_float(v[j]);
+                        pass |= uint32_t(tj < thr) << j;
+                    }
+                    mask &= pass;
+                }
+                // Queue them; when some thread's queue would overflow, the warp drains every
+                // queue (older ids first) and replays this chunk directly.  Admissions then
+                // cost the warp about the largest per-thread count, not one round per chunk.
+                if (__any_sync(kFull, qlen + __popc(mask) > TC_QUEUE)) {
+                    for (uint32_t e = 0; e < qlen; ++e) {
+                        const float tj = MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tid], a.bnorm[qi[e * TC_M + tid]])
+                                                     : -qv[e * TC_M + tid];
+                        if (!(tj < thr)) continue;  // the bound fell since the chunk test
+                        const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+                        thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
+                    }
+                    qlen = 0;
+                    while (mask) {
+                        const uint32_t j = __ffs(mask) - 1;
                         mask &= mask - 1;
-                        const uint32_t id = uint32_t(id0) + j;
-                        const float acc = scr[j * TC_M + tid];
-                        const float du = MET == M_L2 ? qn + fmaf(-2.0f, acc, a.bnorm[id]) : -acc;
-                        const float dist = du * scale;
-                        float B;
-                        if (!a.exact) {
-                            // CompGT.cpp:71-95
-                            if (cnt < k) {
-                                if (dist > topdist) { topdist = dist; toppos = cnt; }
-                                lmax = fmaxf(lmax, dist);
-                                tk_d[cnt * TC_M + tid] = dist;
-                                tk_i[cnt * TC_M + tid] = id;
-                                ++cnt;
-                            } else if (dist < topdist) {
-                                // overwrite toppos, rescan seeded with topk[0] read before the write
-                                const float old0 = tk_d[tid];
-                                tk_d[toppos * TC_M + tid] = dist;
-                                tk_i[toppos * TC_M + tid] = id;
-                                float nt = old0, mx = tk_d[tid];
-                                uint32_t np = 0;
-                                for (uint32_t l = 1; l < k; ++l) {
-                                    const float x = tk_d[l * TC_M + tid];
-                                    if (x > nt) { nt = x; np = l; }
-                                    mx = fmaxf(mx, x);
-                                }
-                                topdist = nt;
-                                toppos = np;
-                                lmax = mx;
-                            }
-                            B = cnt < k ? kInf : fmaxf(topdist, lmax);
-                        } else {
-                            // sorted insert; a later id never wins a tie
-                            if (cnt < k || dist < tk_d[(k - 1) * TC_M + tid]) {
-                                uint32_t pos = cnt < k ? cnt : k - 1;
-                                while (pos > 0 && dist < tk_d[(pos - 1) * TC_M + tid]) {
-                                    tk_d[pos * TC_M + tid] = tk_d[(pos - 1) * TC_M + tid];
-                                    tk_i[pos * TC_M + tid] = tk_i[(pos - 1) * TC_M + tid];
-                                    --pos;
-                                }
-                                tk_d[pos * TC_M + tid] = dist;
-                                tk_i[pos * TC_M + tid] = id;
-                                if (cnt < k) ++cnt;
-                            }
-                            B = cnt < k ? kInf : tk_d[(k - 1) * TC_M + tid];
-                        }
-                        thr = accum_threshold<MET>(B, inv_scale, qn);
-                    } while (mask);
+                        const float acc = __uint_as_float(pick32(v, j));
+                        const float tj = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
+                        if (!(tj < thr)) continue;
+                        const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+                        thr = tk_offer(L, S, dist, uint32_t(id0) + j) * inv_scale - (MET == M_L2 ? qn : 0.0f);
+                    }
+                } else {
+                    while (mask) {
+                        const uint32_t j = __ffs(mask) - 1;
+                        mask &= mask - 1;
+                        qv[qlen * TC_M + tid] = __uint_as_float(pick32(v, j));
+                        qi[qlen * TC_M + tid] = uint32_t(id0) + j;
+                        ++qlen;
+                    }
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             mbar_arrive(bar_tempty + 8 * s);
         }
+        for (uint32_t e = 0; e < qlen; ++e) {
+            const float tj =
+                MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tid], a.bnorm[qi[e * TC_M + tid]]) : -qv[e * TC_M + tid];
+            if (!(tj < thr)) continue;
+            const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+            thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
+        }
         // output sorted by (dist, id) (CompGT.cpp:107-124)
-        if (live && cnt == k) {
-            if (!a.exact) {
-                for (uint32_t i = 1; i < k; ++i) {
-                    const float dv = tk_d[i * TC_M + tid];
-                    const uint32_t iv = tk_i[i * TC_M + tid];
-                    const uint64_t key = make_key(dv, iv);
-                    int32_t j = int32_t(i) - 1;
-                    while (j >= 0 && make_key(tk_d[j * TC_M + tid], tk_i[j * TC_M + tid]) > key) {
-                        tk_d[(j + 1) * TC_M + tid] = tk_d[j * TC_M + tid];
-                        tk_i[(j + 1) * TC_M + tid] = tk_i[j * TC_M + tid];
-                        --j;
-                    }
-                    tk_d[(j + 1) * TC_M + tid] = dv;
-                    tk_i[(j + 1) * TC_M + tid] = iv;
+        if (live && S.cnt == k) {
+            // sort (dist, id) in place: distances in shared memory, ids in the output row
+            uint32_t *ids = L.id;
+            for (uint32_t i = 1; i < k; ++i) {
+                const float dv = tk_d[i * TC_M + tid];
+                const uint32_t iv = ids[i];
+                int32_t j = int32_t(i) - 1;
+                while (j >= 0) {
+                    const float dj = tk_d[j * TC_M + tid];
+                    if (!(dj > dv || (dj == dv && ids[j] > iv))) break;
+                    tk_d[(j + 1) * TC_M + tid] = dj;
+                    ids[j + 1] = ids[j];
+                    --j;
                 }
+                tk_d[(j + 1) * TC_M + tid] = dv;
+                ids[j + 1] = iv;
             }
-            for (uint32_t l = 0; l < k; ++l) {
-                const float dv = tk_d[l * TC_M + tid];
-                a.out_ids[size_t(q) * k + l] = tk_i[l * TC_M + tid];
-                a.out_dists[size_t(q) * k + l] = output_dist<MET>(dv);
-            }
+            for (uint32_t l = 0; l < k; ++l) a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 4) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
     }
 }
 
@@ -443,13 +607,22 @@ static bool make_map(CUtensorMap *m, void *base, uint64_t rows, uint32_t K)
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Dynamic shared memory of one CTA.  At least 80 KB, so that no more than two CTAs
-// share an SM and their TMEM allocations (256 columns each) fit the SM's 512 columns.
-size_t gt_tc_smem(uint32_t katoms, uint32_t k)
+// Dynamic shared memory of one CTA with a ring of `stages` base tiles.  At least 120 KB,
+// so that one CTA holds an SM and its TMEM allocation (all 512 columns) never waits
+// for another's.
+size_t gt_tc_smem(uint32_t katoms, uint32_t k, uint32_t stages)
 {
-    const size_t need = 1024 + size_t(katoms) * TC_M * 128 * (1 + TC_STAGES) + 32 * TC_M * 4 + 16 * 8 + 16 +
-                        size_t(k) * TC_M * 8;
-    return need > 80 * 1024 ? need : 80 * 1024;
+    const size_t need = 1024 + size_t(katoms) * TC_M * 128 * (1 + stages) + TC_M * TC_M + TC_QUEUE * TC_M * 8 +
+                        24 * 8 + 16 + size_t(k) * TC_M * 4;
+    return need > 120 * 1024 ? need : 120 * 1024;
+}
+
+// deepest ring that fits, 0 if even two stages do not
+static uint32_t gt_tc_stages(uint32_t katoms, uint32_t k, size_t smem_optin)
+{
+    for (uint32_t st = TC_MAX_STAGES; st >= 2; --st)
+        if (gt_tc_smem(katoms, k, st) <= smem_optin) return st;
+    return 0;
 }
 
 // Whether the tensor-core path applies: D up to 128 elements after nibble expansion,
@@ -459,7 +632,7 @@ bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_opti
     const uint32_t elems = (dtype == NBPG_U4 || dtype == NBPG_I4) ? 2 * dims : dims;
     if (dtype > NBPG_I4 || elems == 0 || elems > 128 || k == 0 || k > 100) return false;
     const uint32_t katoms = (elems + TC_KATOM - 1) / TC_KATOM;
-    return gt_tc_smem(katoms, k) <= smem_optin;
+    return gt_tc_stages(katoms, k, smem_optin) != 0;
 }
 
 // Workspace of the tensor engine: bf16 rows of base and queries (K = codes rounded up to
@@ -542,13 +715,21 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
         set_error("nbpg_gt: tensor map encoding failed");
         s = NBPG_ERR_CUDA;
     }
-    const size_t smem = gt_tc_smem(l.katoms, k);
+    int dev = 0, optin = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const uint32_t stages = gt_tc_stages(l.katoms, k, size_t(optin));
+    if (e == cudaSuccess && stages == 0) {
+        set_error("nbpg_gt: the tensor engine's shared memory does not fit this k and row length");
+        s = NBPG_ERR_UNSUPPORTED;
+    }
+    const size_t smem = gt_tc_smem(l.katoms, k, stages ? stages : 2);
     if (e == cudaSuccess && s == NBPG_OK)
         e = cudaFuncSetAttribute(metric == NBPG_L2 ? gt_tc_kernel<M_L2> : gt_tc_kernel<M_IP>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e == cudaSuccess && s == NBPG_OK) {
         TcArgs a{qn, bn, n, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, nib ? 256u : 1u, l.katoms,
-                 uint32_t(n_pad / TC_N), d_ids, d_dists, err};
+                 uint32_t(n_pad / TC_N), stages, d_ids, d_dists, err};
         if (metric == NBPG_L2) gt_tc_kernel<M_L2><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
         else gt_tc_kernel<M_IP><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
         e = cudaGetLastError();
