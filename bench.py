@@ -66,7 +66,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -213,13 +213,15 @@ def run_reference(args):
                                dynamic_prune=CFG["dynamic_prune"], min_alpha=CFG["min_alpha"],
                                max_alpha=CFG["max_alpha"], sp_seed=0, threads=threads)
     log(f"[bench/ref] CPU build {time.time() - t:.1f}s on {threads} threads")
+    # L chosen on all 10k queries, as the GPU arm does (the two builds give the same graph);
+    # the timed steps then run a 2,000-query sample at that L
     sample = q[:2000]
     t = time.time()
-    gi, gd = O.gt("u8", "l2", base, sample, k=CFG["gt_k"], exact=False, threads=threads)
-    log(f"[bench/ref] CPU ground truth for {len(sample)} queries {time.time() - t:.1f}s")
+    gi, gd = O.gt("u8", "l2", base, q, k=CFG["gt_k"], exact=False, threads=threads)
+    log(f"[bench/ref] CPU ground truth for {len(q)} queries {time.time() - t:.1f}s")
     L_op = None
     for L in L_SWEEP:
-        ids = O.search("u8", "l2", base, g, sample, L=L, k=CFG["k"], cut=CFG["cut"], threads=threads)[0]
+        ids = O.search("u8", "l2", base, g, q, L=L, k=CFG["k"], cut=CFG["cut"], threads=threads)[0]
         r = recall_at_k(ids, gi, gd, CFG["k"])
         if r >= CFG["recall_target"]:
             L_op, rec = L, r

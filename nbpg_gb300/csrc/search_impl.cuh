@@ -77,7 +77,7 @@ struct SearchArgs {
 // ---------------------------------------------------------------------------
 // Distances of `cnt` rows (ids[0..cnt)) to the query held in registers.
 // Lanes are grouped lpr per row; each lane loads vpl uint4 (16-byte, coalesced
-// within the group).  Row-passes covering 32 rows are issued before any arithmetic so their
+// within the group).  Several row-passes are issued before any arithmetic so their
 // loads are in flight together.  Result keys go to out[0..cnt).
 // ---------------------------------------------------------------------------
 template <int DT, int MET, int VPL, bool FILTER>
@@ -86,7 +86,7 @@ __device__ __forceinline__ uint32_t warp_row_keys_impl(const SearchArgs &a, cons
 {
     const uint32_t lpr = a.lpr, rows_per = 32u / lpr;
     const uint32_t grp = uint32_t(lane) / lpr, lq = uint32_t(lane) % lpr;
-    constexpr int P = VPL == 1 ? 8 : VPL == 2 ? 4 : 2;  // 32 rows in flight per pass group
+    constexpr int P = VPL == 4 ? 2 : 4;  // 16 (lane width 1) or 32 rows in flight per pass group
     uint32_t stored = 0;
     for (uint32_t r0 = 0; r0 < cnt; r0 += rows_per * P) {
         uint4 bv[P][VPL];
