@@ -28,7 +28,9 @@ static const SearchOps *ops_for(uint32_t dtype, uint32_t vpl)
 void row_geometry(uint32_t row_stride, uint32_t want, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl)
 {
     vecs = row_stride / 16;
-    vpl = vecs <= 32 ? 1 : 4;
+    // default: two 16-byte words per lane for rows of 64-512 bytes (fastest on 1M x 128 u8
+    // at every beam width measured), one for shorter rows, four beyond 512 bytes
+    vpl = vecs > 32 ? 4 : (vecs >= 4 ? 2 : 1);
     if ((want == 2 || want == 4) && want <= vecs && (vecs + want - 1) / want <= 32) vpl = want;
     if (want == 1 && vecs <= 32) vpl = 1;
     const uint32_t need = (vecs + vpl - 1) / vpl;

@@ -558,9 +558,11 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     __syncwarp();
 }
 
-// Persistent form: warps pull queries from a device queue until it runs dry.
+// Persistent form: warps pull queries from a device queue until it runs dry.  Capped at
+// 80 registers (the one-warp form settles at 72 unconstrained): at the 128 that a
+// 512-thread bound allows, only 16 warps fit per SM; at 80, 24 do (a few bytes spill).
 template <int DT, int MET, bool LIST, int VPL>
-__global__ void __launch_bounds__(512) search_batched_kernel(SearchArgs a)
+__global__ void __maxnreg__(80) search_batched_kernel(SearchArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
