@@ -254,6 +254,31 @@ nbpg_status nbpg_gt_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint3
                            size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * PCA encode.  Replaces PCACompress's matmul + compress (data_tools/ANNs/data_proc/
+ * base/matrix.h:86-125, driven by PCACompress.cpp:21-83): values[j] = bias[j] + mat[j] . x,
+ * summed in index order in fp32 with separately rounded products, then quantised:
+ * out_dtype NBPG_F32 writes the values; NBPG_U8 / NBPG_I8 write one code per value;
+ * NBPG_U4 / NBPG_I4 pack two (high nibble = element 2i+1), d_out even.
+ * in_dtype: NBPG_F32, NBPG_U8 or NBPG_I8 rows of d_in elements (d_in <= 576); mat is
+ * d_out x d_in row-major, bias d_out floats (NULL = zeros).  Out rows are d_out values
+ * or codes (d_out / 2 bytes for 4-bit).  Codes equal the reference's bit for bit when
+ * it is built without fast-math reassociation.
+ * ------------------------------------------------------------------------- */
+nbpg_status nbpg_pca_encode(uint32_t in_dtype, const void *rows, uint64_t n, uint32_t d_in, const float *mat,
+                            const float *bias, uint32_t d_out, uint32_t out_dtype, void *out, int32_t device);
+/* device buffers, enqueued on `stream` (a cudaStream_t); bias required */
+nbpg_status nbpg_pca_encode_device(uint32_t in_dtype, const void *d_rows, uint64_t n, uint32_t d_in,
+                                   const float *d_mat, const float *d_bias, uint32_t d_out, uint32_t out_dtype,
+                                   void *d_out_rows, void *stream);
+
+/* FmtConv u8bin2u4bin (FmtConv.cpp:95-131): out byte j = (row[2j+1] & 0xF0) + (row[2j] >> 4),
+ * rows of dims >> 1 bytes. */
+nbpg_status nbpg_u8_to_u4(const uint8_t *rows, uint64_t n, uint32_t dims, uint8_t *out, int32_t device);
+/* FmtConv fbin2u8bin (FmtConv.cpp:63-93): truncation of values in [0, 256); any other
+ * value returns NBPG_ERR_INVALID_ARG (the reference asserts). */
+nbpg_status nbpg_f32_to_u8(const float *rows, uint64_t n, uint32_t dims, uint8_t *out, int32_t device);
+
+/* ---------------------------------------------------------------------------
  * Build.  Replaces build_vamana (algorithms/nsw.h:547-663) with NSWIndex::batch_insert
  * (nsw.h:110-286), RobustPrune (algorithms/utils/Graph/prune.h:159-209), reverse-edge
  * merging (merge_edges.h:23-148, nsw.h:463-511), popularity-driven alpha

@@ -109,6 +109,12 @@ def lib() -> C.CDLL:
                                          C.POINTER(C.c_size_t)]
     L.nbpg_gt_device.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.nbpg_pca_encode.argtypes = [C.c_uint32, _vp, C.c_uint64, C.c_uint32, _f32p, _f32p, C.c_uint32, C.c_uint32, _vp,
+                                  C.c_int32]
+    L.nbpg_pca_encode_device.argtypes = [C.c_uint32, _vp, C.c_uint64, C.c_uint32, _vp, _vp, C.c_uint32, C.c_uint32,
+                                         _vp, _vp]
+    L.nbpg_u8_to_u4.argtypes = [_vp, C.c_uint64, C.c_uint32, _vp, C.c_int32]
+    L.nbpg_f32_to_u8.argtypes = [_f32p, C.c_uint64, C.c_uint32, _vp, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
     _lib = L
     return L

@@ -62,7 +62,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
-CLI = {"nbpg_vamana": "vamana.cpp", "nbpg_compgt": "compgt.cpp"}
+CLI = {"nbpg_vamana": "vamana.cpp", "nbpg_compgt": "compgt.cpp", "nbpg_pcacompress": "pcacompress.cpp",
+       "nbpg_fmtconv": "fmtconv.cpp"}
 
 
 def _build_cli() -> None:

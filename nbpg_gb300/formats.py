@@ -95,3 +95,41 @@ def write_gt(path: str, ids: np.ndarray, dists: np.ndarray) -> None:
         np.array(ids.shape, dtype=np.uint32).tofile(f)
         ids.tofile(f)
         np.ascontiguousarray(dists, dtype=np.float32).tofile(f)
+
+
+def read_matrix(path: str) -> tuple[np.ndarray, np.ndarray]:
+    """A `.mat` projection (matrix.h:59-84): [d_out u32][d_in u32][has_bias u8][d_out x d_in f32][d_out f32 if bias].
+    Returns (mat, bias); bias is zeros when the file has none."""
+    with open(path, "rb") as f:
+        d_out, d_in = (int(x) for x in np.fromfile(f, dtype=np.uint32, count=2))
+        has_bias = bool(np.fromfile(f, dtype=np.uint8, count=1)[0])
+        mat = np.fromfile(f, dtype=np.float32, count=d_out * d_in).reshape(d_out, d_in)
+        bias = np.fromfile(f, dtype=np.float32, count=d_out) if has_bias else np.zeros(d_out, np.float32)
+    return mat, bias
+
+
+def write_matrix(path: str, mat: np.ndarray, bias: np.ndarray | None) -> None:
+    mat = np.ascontiguousarray(mat, dtype=np.float32)
+    with open(path, "wb") as f:
+        np.array(mat.shape, dtype=np.uint32).tofile(f)
+        np.array([0 if bias is None else 1], dtype=np.uint8).tofile(f)
+        mat.tofile(f)
+        if bias is not None:
+            np.ascontiguousarray(bias, dtype=np.float32).tofile(f)
+
+
+def read_fvecs(path: str) -> np.ndarray:
+    """`.fvecs` rows of [dims u32][dims f32], the input of FmtConv vec2bin (FmtConv.cpp:18-61)."""
+    raw = np.fromfile(path, dtype=np.uint32)
+    if raw.size == 0:
+        return np.zeros((0, 0), np.float32)
+    d = int(raw[0])
+    return raw.reshape(-1, d + 1)[:, 1:].copy().view(np.float32)
+
+
+def write_fvecs(path: str, x: np.ndarray) -> None:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    rows = np.empty((x.shape[0], x.shape[1] + 1), np.uint32)
+    rows[:, 0] = x.shape[1]
+    rows[:, 1:] = x.view(np.uint32)
+    rows.tofile(path)

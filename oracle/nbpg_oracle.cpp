@@ -795,4 +795,96 @@ int nbpg_oracle_gt(int dtype, int metric, uint32_t dims, const void *base, uint6
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// PCA projection and quantisation, as PCACompress.cpp:21-83 drives matrix.h.
+//   in_kind  0 float rows, 1 u8 rows, 2 i8 rows (loadFloatPoint, matrix.h:25-54: (float)v)
+//   out_kind 0 float, 1 u8 ("uint", chunk 1), 2 i8 ("int", chunk 1),
+//            3 u4 ("uint", chunk 2), 4 i4 ("int", chunk 2)      (PCACompress.cpp:24-38)
+// values[j] = bias[j] - mips_distance(mat[j], x) (matmul, matrix.h:86-97), the dot
+// product summed in index order in float with separately rounded products
+// (point.h:148-156 as written); then compress (matrix.h:99-125): for output byte i the
+// chunk's elements are taken from the highest index down, ti = int((v + 1) * 0.5 * 255)
+// evaluated as float + 1, then double products, truncated; clamped to [0, 255]; minus
+// 128 for "int"; arithmetic shift right by 8 - 8/chunk; masked and packed.  The
+// reference's (int) of a double outside int's range is undefined; here it saturates.
+// ---------------------------------------------------------------------------
+static inline int quant_code(float v)
+{
+    double t = double(v + 1.0f) * 0.5 * 255.0;
+    if (!(t > -2147483648.0)) t = -2147483648.0;  // also maps NaN to the low end
+    if (t > 2147483647.0) t = 2147483647.0;
+    return int(t);
+}
+
+int nbpg_oracle_pca_encode(int in_kind, const void *x, uint64_t n, uint32_t d_in, const float *mat, const float *bias,
+                           uint32_t d_out, int out_kind, void *out, int threads)
+{
+    if (in_kind < 0 || in_kind > 2 || out_kind < 0 || out_kind > 4 || d_in == 0 || d_out == 0) return -1;
+    const uint32_t chunk = out_kind >= 3 ? 2 : 1;
+    if (out_kind != 0 && d_out % chunk) return -1;
+    const uint32_t out_dims = d_out / chunk;
+    const int delta = (out_kind == 2 || out_kind == 4) ? 128 : 0;
+    const int offset = 8 - 8 / int(chunk);
+    const int mask = (1 << (8 / chunk)) - 1;
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (long long p = 0; p < (long long)n; ++p) {
+        std::vector<float> xf(d_in), v(d_out);
+        for (uint32_t i = 0; i < d_in; ++i) {
+            if (in_kind == 0) xf[i] = static_cast<const float *>(x)[size_t(p) * d_in + i];
+            else if (in_kind == 1) xf[i] = float(static_cast<const uint8_t *>(x)[size_t(p) * d_in + i]);
+            else xf[i] = float(static_cast<const int8_t *>(x)[size_t(p) * d_in + i]);
+        }
+        for (uint32_t j = 0; j < d_out; ++j) {
+            float r = 0.0f;
+            const float *m = mat + size_t(j) * d_in;
+            for (uint32_t i = 0; i < d_in; ++i) {
+                const float prod = m[i] * xf[i];
+                r = r + prod;
+            }
+            v[j] = bias[j] - (-r);
+        }
+        if (out_kind == 0) {
+            std::memcpy(static_cast<float *>(out) + size_t(p) * d_out, v.data(), d_out * sizeof(float));
+            continue;
+        }
+        uint8_t *o = static_cast<uint8_t *>(out) + size_t(p) * out_dims;
+        for (uint32_t i = 0; i < out_dims; ++i) {
+            uint8_t res = 0;
+            for (uint32_t j = 0; j < chunk; ++j) {
+                const float val = v[(i + 1) * chunk - 1 - j];
+                res = uint8_t(res << (8 / chunk));
+                int ti = quant_code(val);
+                ti = ((std::clamp(ti, 0, 255) - delta) >> offset);
+                res = uint8_t(res + uint8_t(ti & mask));
+            }
+            o[i] = res;
+        }
+    }
+    return 0;
+}
+
+// FmtConv u8bin2u4bin (FmtConv.cpp:95-131): byte jj = (row[2jj+1] & 0xF0) + (row[2jj] >> 4);
+// an odd last element is dropped (half_dims = dims >> 1).
+int nbpg_oracle_u8_to_u4(const uint8_t *rows, uint64_t n, uint32_t dims, uint8_t *out)
+{
+    const uint32_t half = dims >> 1;
+    for (uint64_t p = 0; p < n; ++p)
+        for (uint32_t j = 0; j < half; ++j)
+            out[p * half + j] = uint8_t((rows[p * dims + 2 * j + 1] & 0xF0) + (rows[p * dims + 2 * j] >> 4));
+    return 0;
+}
+
+// FmtConv fbin2u8bin (FmtConv.cpp:63-93): static_cast<unsigned char>(v), defined for
+// 0 <= v < 256 (the reference asserts that range); -1 if a value falls outside it.
+int nbpg_oracle_f32_to_u8(const float *rows, uint64_t n, uint32_t dims, uint8_t *out)
+{
+    for (uint64_t i = 0; i < n * dims; ++i) {
+        const float v = rows[i];
+        if (!(v >= 0.0f && v < 256.0f)) return -1;
+        out[i] = static_cast<unsigned char>(v);
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -67,6 +67,14 @@ class CpuLib:
                                C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.c_double, C.c_double,
                                C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint64, _u32p, _u32p, _u32p,
                                _u64p, C.c_int]
+        if hasattr(self.lib, prefix + "pca_encode"):
+            f("pca_encode").restype = C.c_int
+            f("pca_encode").argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_uint32, _f32p, _f32p, C.c_uint32, C.c_int,
+                                        C.c_void_p, C.c_int]
+            f("u8_to_u4").restype = C.c_int
+            f("u8_to_u4").argtypes = [_u8p, C.c_uint64, C.c_uint32, _u8p]
+            f("f32_to_u8").restype = C.c_int
+            f("f32_to_u8").argtypes = [_f32p, C.c_uint64, C.c_uint32, _u8p]
         if hasattr(self.lib, prefix + "gt"):
             f("gt").restype = C.c_int
             f("gt").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, _u8p, C.c_uint32, C.c_uint32, C.c_int,
@@ -167,6 +175,40 @@ class CpuLib:
         if rc != 0:
             raise ValueError("gt rejected its arguments")
         return ids, ds
+
+
+    # -- PCA encode and format conversions (PCACompress / FmtConv) -----------------
+    PCA_IN = {"f32": 0, "u8": 1, "i8": 2}
+    PCA_OUT = {"f32": 0, "u8": 1, "i8": 2, "u4": 3, "i4": 4}
+
+    def pca_encode(self, x, mat, bias, out, threads=0):
+        """Project rows x (f32/u8/i8) with mat (d_out x d_in) and bias, quantise to `out`."""
+        x = np.ascontiguousarray(x)
+        mat = np.ascontiguousarray(mat, dtype=np.float32)
+        bias = np.ascontiguousarray(bias, dtype=np.float32)
+        kin = {np.dtype(np.float32): "f32", np.dtype(np.uint8): "u8", np.dtype(np.int8): "i8"}[x.dtype]
+        n, d_in = x.shape
+        d_out = mat.shape[0]
+        width = d_out if out in ("f32", "u8", "i8") else d_out // 2
+        res = np.empty((n, width), np.float32 if out == "f32" else np.uint8)
+        rc = self._f("pca_encode")(self.PCA_IN[kin], x.ctypes.data, n, d_in, _p(mat, _f32p), _p(bias, _f32p), d_out,
+                                   self.PCA_OUT[out], res.ctypes.data, threads)
+        if rc != 0:
+            raise ValueError("pca_encode rejected its arguments")
+        return res
+
+    def u8_to_u4(self, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.uint8)
+        out = np.empty((rows.shape[0], rows.shape[1] // 2), np.uint8)
+        self._f("u8_to_u4")(_p(rows, _u8p), rows.shape[0], rows.shape[1], _p(out, _u8p))
+        return out
+
+    def f32_to_u8(self, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.float32)
+        out = np.empty(rows.shape, np.uint8)
+        if self._f("f32_to_u8")(_p(rows, _f32p), rows.shape[0], rows.shape[1], _p(out, _u8p)) != 0:
+            raise ValueError("values outside [0, 256)")
+        return out
 
 
 _oracle = None

@@ -8,7 +8,12 @@ Inputs are small seeded synthetic sets.  Outputs, stored as tests/golden/*.npz:
                   (--num_split 0, and --num_split 1 which runs the split stage, a popularity
                   pass and the dynamic-prune pass), kept as raw bytes;
   * search_*.npz  per-query ids, dists, counts, expansions and distance counts from the
-                  harness over the reference headers (qsearchAll's body) on those graphs.
+                  harness over the reference headers (qsearchAll's body) on those graphs;
+  * pca.npz       PCACompress outputs (.u4bin/.i4bin/.u8bin/.i8bin/.fbin) for float rows and
+                  a .mat with bias; for u8/i8 input rows (whose path in the reference only
+                  works on whole 100,000-row blocks) the seed of the rows and the SHA-256 of
+                  the reference's output instead of the rows themselves;
+  * fmtconv.npz   FmtConv fbin2u8bin, u8bin2u4bin (odd row length) and vec2bin outputs.
 
 Usage: make -C oracle ref && python tests/golden/make_golden.py
 """
@@ -26,6 +31,56 @@ sys.path.insert(0, ROOT)
 from nbpg_gb300 import formats, synth  # noqa: E402
 from oracle.oracle import REF_COMPGT, REF_VAMANA, reference  # noqa: E402
 
+REF_DIR = os.path.dirname(REF_COMPGT)
+
+
+def pca_rows_u8in(seed):
+    """Rows for the u8/i8-input PCACompress pins: 100,000 x 48 (one reference block)."""
+    r = np.random.default_rng(seed)
+    return r.integers(0, 256, (100000, 48)).astype(np.uint8), r.integers(-128, 128, (100000, 48)).astype(np.int8)
+
+
+def pca_golden(tmp):
+    import hashlib
+    r = np.random.default_rng(13)
+    x = (r.normal(size=(600, 32)) * 0.6).astype(np.float32)
+    mat = (r.normal(size=(16, 32)) * 0.3).astype(np.float32)
+    bias = (r.normal(size=16) * 0.1).astype(np.float32)
+    formats.write_vectors(f"{tmp}/x.fbin", x)
+    formats.write_matrix(f"{tmp}/m.mat", mat, bias)
+    out = {"x": x, "mat": mat, "bias": bias}
+    for kind, ext in [("u4", ".u4bin"), ("i4", ".i4bin"), ("u8", ".u8bin"), ("i8", ".i8bin"), ("f32", ".fbin")]:
+        subprocess.run([f"{REF_DIR}/PCACompress", "--ifile", f"{tmp}/x.fbin", "--ofile", f"{tmp}/o{ext}", "--matFile",
+                        f"{tmp}/m.mat"], check=True, stdout=subprocess.DEVNULL)
+        out["out_" + kind] = np.fromfile(f"{tmp}/o{ext}", dtype=np.uint8)
+    m2 = (r.normal(size=(16, 48)) * 0.3 / 200).astype(np.float32)
+    formats.write_matrix(f"{tmp}/m2.mat", m2, bias)
+    xu, xi = pca_rows_u8in(29)
+    for name, rows, ext in [("u8in", xu, ".u8bin"), ("i8in", xi, ".i8bin")]:
+        formats.write_vectors(f"{tmp}/r{ext}", rows)
+        subprocess.run([f"{REF_DIR}/PCACompress", "--ifile", f"{tmp}/r{ext}", "--ofile", f"{tmp}/r_{name}.u4bin",
+                        "--matFile", f"{tmp}/m2.mat"], check=True, stdout=subprocess.DEVNULL)
+        out["sha_" + name] = np.array(hashlib.sha256(open(f"{tmp}/r_{name}.u4bin", "rb").read()).hexdigest())
+    out["mat_u8in"] = m2
+    out["seed_u8in"] = np.array(29)
+    np.savez_compressed(f"{HERE}/pca.npz", **out)
+
+    xf = r.uniform(0, 255.99, (300, 24)).astype(np.float32)
+    formats.write_vectors(f"{tmp}/f.fbin", xf)
+    subprocess.run([f"{REF_DIR}/FmtConv", "fbin2u8bin", "--ifile", f"{tmp}/f.fbin", "--ofile", f"{tmp}/f.u8bin"],
+                   check=True, stdout=subprocess.DEVNULL)
+    xu8 = r.integers(0, 256, (300, 25)).astype(np.uint8)
+    formats.write_vectors(f"{tmp}/g.u8bin", xu8)
+    subprocess.run([f"{REF_DIR}/FmtConv", "u8bin2u4bin", "--ifile", f"{tmp}/g.u8bin", "--ofile", f"{tmp}/g.u4bin"],
+                   check=True, stdout=subprocess.DEVNULL)
+    formats.write_fvecs(f"{tmp}/v.fvecs", xf[:40])
+    subprocess.run([f"{REF_DIR}/FmtConv", "vec2bin", "--ifile", f"{tmp}/v.fvecs", "--ofile", f"{tmp}/v.fbin"],
+                   check=True, stdout=subprocess.DEVNULL)
+    np.savez_compressed(f"{HERE}/fmtconv.npz", f32=xf, f32_to_u8=np.fromfile(f"{tmp}/f.u8bin", dtype=np.uint8),
+                        u8=xu8, u8_to_u4=np.fromfile(f"{tmp}/g.u4bin", dtype=np.uint8),
+                        fvecs=np.fromfile(f"{tmp}/v.fvecs", dtype=np.uint8),
+                        vec2bin=np.fromfile(f"{tmp}/v.fbin", dtype=np.uint8))
+
 
 def datasets():
     b, q = synth.u8_mixture(3000, 40, dim=32, n_centres=12, seed=7)
@@ -40,6 +95,10 @@ def main():
         sys.exit("build the reference first: make -C oracle ref")
     ref = reference()
     tmp = tempfile.mkdtemp()
+    pca_golden(tmp)
+    if "--pca-only" in sys.argv:
+        print("PCA/FmtConv golden vectors written to", HERE)
+        return
     for name, (dt, ext, b, q) in datasets().items():
         bp, qp = f"{tmp}/{name}_b{ext}", f"{tmp}/{name}_q{ext}"
         formats.write_vectors(bp, b)
