@@ -254,6 +254,28 @@ nbpg_status nbpg_gt_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint3
                            size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Re-ranking with raw vectors.  Replaces beam_search_rerank (algorithms/utils/Graph/
+ * beamSearch.h:183-247) called with Base_Points (raw) beside Q_Base_Points (quantised),
+ * the Vamana driver's --base_path / --rerank_factor / --cache_raw (Vamana.cpp:91-122, 212-231).
+ * nbpg_index_set_raw_points stores raw rows (raw_dtype NBPG_U8/I8/U4/I4/F32; raw_dims
+ * elements, bytes for 4-bit rows) on the device beside the index's quantised rows.
+ * nbpg_search_rerank searches with the quantised queries and then:
+ *   no raw rows, or raw rows of the quantised row size: the plain search (beamSearch.h:23-26);
+ *   rerank_factor > 0: exact distances of frontier[0 : min(k * rerank_factor, frontier)],
+ *     sorted by (dist, id), first k (counts: the search's own distances);
+ *   rerank_factor == 0 (filtering): exact distances of the visited list (counted), sorted,
+ *     cut to min(frontier size, visited size), first k.
+ * k <= 256; the re-rank set (min(k * rerank_factor, L), or visited_factor * L) <= 4096.
+ * raw_queries: nq rows of raw_dims elements.  Outputs as nbpg_search (exact distances).
+ * ------------------------------------------------------------------------- */
+nbpg_status nbpg_index_set_raw_points(nbpg_index *idx, uint32_t raw_dtype, uint32_t raw_dims, const void *rows,
+                                      uint64_t first, uint64_t count);
+nbpg_status nbpg_search_rerank(nbpg_index *idx, const void *queries, const void *raw_queries, uint32_t nq,
+                               const nbpg_search_params *params, uint32_t rerank_factor, const uint32_t *start_points,
+                               uint32_t n_start, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
+                               uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps);
+
+/* ---------------------------------------------------------------------------
  * PCA encode.  Replaces PCACompress's matmul + compress (data_tools/ANNs/data_proc/
  * base/matrix.h:86-125, driven by PCACompress.cpp:21-83): values[j] = bias[j] + mat[j] . x,
  * summed in index order in fp32 with separately rounded products, then quantised:

@@ -62,6 +62,7 @@ extern "C" nbpg_status nbpg_index_destroy(nbpg_index *idx)
     if (idx->stream) cudaStreamSynchronize(idx->stream);
     if (idx->d_points) cudaFree(idx->d_points);
     if (idx->d_graph) cudaFree(idx->d_graph);
+    if (idx->d_raw) cudaFree(idx->d_raw);
     idx->scratch.release();
     for (DevBuf *b : {&idx->qbuf, &idx->obuf, &idx->ghash, &idx->order_buf}) b->release();
     if (idx->stream) cudaStreamDestroy(idx->stream);

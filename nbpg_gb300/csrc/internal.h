@@ -77,6 +77,22 @@ struct SearchScratch {
     }
 };
 
+// What a search writes besides the usual top k, for a re-rank with raw vectors
+// (beam_search_rerank, beamSearch.h:183-247): `factor` > 0 emits frontier[0 : min(k *
+// factor, fs)]; `visited` forces LIST mode and emits the final visited list (adding its
+// insertions to the distance count); `d_fs` receives each query's final frontier size.
+struct SearchEmit {
+    uint32_t factor = 0;
+    bool visited = false;
+    uint32_t *d_fs = nullptr;
+};
+
+nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
+                               const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
+                               const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
+                               uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st,
+                               const SearchEmit *emit = nullptr);
+
 }  // namespace nbpg
 
 struct nbpg_index {
@@ -86,6 +102,9 @@ struct nbpg_index {
     uint32_t gstride = 0;     // u32 per graph row on device: round_up(R+1, 4)
     uint8_t *d_points = nullptr;
     uint32_t *d_graph = nullptr;
+    // raw (exact) vectors for re-ranking: Base_Points beside Q_Base_Points
+    uint8_t *d_raw = nullptr;
+    uint32_t raw_dtype = 0, raw_dims = 0, raw_row_bytes = 0;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     size_t smem_optin = 0;

@@ -23,8 +23,8 @@ static const SearchOps *ops_for(uint32_t dtype, uint32_t vpl)
 }
 
 // Lane geometry of the distance passes: vpl uint4 per lane (1, 2 or 4), lpr lanes per
-// row (a power of two, lpr * vpl >= row words).  want = 0 picks 1 for rows up to 512
-// bytes and 4 above; an unusable request falls back to that default.
+// row (a power of two, lpr * vpl >= row words).  want = 0 picks the default below; an
+// unusable request falls back to it.
 void row_geometry(uint32_t row_stride, uint32_t want, uint32_t &vecs, uint32_t &lpr, uint32_t &vpl)
 {
     vecs = row_stride / 16;
@@ -110,7 +110,8 @@ static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, 
 nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
                                const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
                                const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
-                               uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st)
+                               uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st,
+                               const SearchEmit *emit)
 {
     NBPG_CHECK_ARG(idx && P && d_ids, "null argument");
     NBPG_CHECK_ARG(idx->d_points && idx->d_graph, "index has no points/graph");
@@ -139,8 +140,12 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     const int metric = int(idx->desc.metric);
     const bool plain = P->kernel == NBPG_KERNEL_PLAIN;
     const uint32_t vf = P->visited_factor ? P->visited_factor : 8;
-    // inner product: the cut rule routinely keeps <= k entries, so go straight to LIST
-    const bool flag_first = metric == M_L2;
+    // inner product: the cut rule routinely keeps <= k entries, so go straight to LIST;
+    // filtering mode needs the visited list itself
+    const bool flag_first = metric == M_L2 && !(emit && emit->visited);
+    if (emit && emit->visited)
+        NBPG_CHECK_ARG(k_stride >= (P->visited_factor ? P->visited_factor : 8) * P->L,
+                       "k_stride must hold the visited list (visited_factor * L)");
 
     PassCfg main{}, rerun{};
     nbpg_status s = plan_pass(idx, ops, metric, !flag_first, plain, P->L, vf, P->warps_per_cta, main);
@@ -200,6 +205,11 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     a.out_cmps = d_cmps;
     a.err = q + 2;
     a.prefetch = plain ? 0 : (P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u));
+    if (emit) {
+        a.emit_factor = emit->factor;
+        a.emit_visited = emit->visited ? 1u : 0u;
+        a.out_fs = emit->d_fs;
+    }
 
     // main pass (queries in the caller's order, or longest beam first when given)
     SearchArgs m = a;

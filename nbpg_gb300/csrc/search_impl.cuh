@@ -71,6 +71,11 @@ struct SearchArgs {
     uint32_t g_vis_cap;
     uint32_t prefetch;  // unvisited entries whose adjacency rows are prefetched to L2
     uint32_t *err;      // set to 1 when a query's (L, k) is rejected
+    // outputs for a re-rank with raw vectors (beam_search_rerank, beamSearch.h:183-247);
+    // zero / null for a plain search
+    uint32_t emit_factor;   // emit frontier[0 : min(k * emit_factor, fs)] instead of [0 : k)
+    uint32_t emit_visited;  // LIST mode: emit the final visited list, count its insertions
+    uint32_t *out_fs;       // frontier size at the end of each query (may be null)
     SlotLayout lay;
 };
 
@@ -258,6 +263,7 @@ struct SearchState {
     uint32_t *H;
     int b;
     uint32_t fs, vs, cmps, smask;
+    uint32_t ins;  // LIST mode: expansions inserted into the capped visited list
     uint64_t nvis;
     bool taint;
     __device__ uint64_t *frontier() const { return b ? fr1 : fr0; }
@@ -325,7 +331,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     uint32_t cmps = nsp;
     uint64_t nvis = 0;
     uint32_t vs = 0;
-    uint32_t remain = nsp, offset = 0, cs = 0;
+    uint32_t remain = nsp, offset = 0, cs = 0, ins = 0;
     bool taint = false;
     const uint32_t R = a.R;
     const uint32_t nchunks = (R + 31) / 32;
@@ -409,6 +415,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
                 }
             }
             if (lane == 0 && pv < nvs) vis[pv] = ck;
+            ins += pv < nvs;  // filtering mode computes an exact distance exactly for these
             vs = nvs;
             __syncwarp();
         } else {
@@ -492,6 +499,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     st.fs = fs;
     st.vs = vs;
     st.cmps = cmps;
+    st.ins = ins;
     st.nvis = nvis;
     st.taint = taint;
     return st;
@@ -531,12 +539,25 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     const uint32_t cmps = st.cmps;
     const bool taint = st.taint;
 
-    // results: frontier[0:min(k, fs)] (beamSearch.h:249-254)
-    const uint32_t kk = k < fs ? k : fs;
+    // results: frontier[0:min(k, fs)] (beamSearch.h:249-254); for a re-rank, frontier[0 :
+    // min(k * rerank_factor, fs)] (beamSearch.h:219-222) or, in filtering mode, the visited
+    // list (beamSearch.h:236-243), whose exact distances a later pass computes
+    const uint64_t *src = frb;
+    uint32_t kk;
+    uint32_t cmps_out = cmps;
+    if (LIST && a.emit_visited) {
+        src = st.vis;
+        kk = st.vs < a.k_stride ? st.vs : a.k_stride;
+        cmps_out += st.ins;
+    } else {
+        uint64_t want = uint64_t(k) * (a.emit_factor ? a.emit_factor : 1u);
+        if (want > a.k_stride) want = a.k_stride;
+        kk = want < fs ? uint32_t(want) : fs;
+    }
     for (uint32_t j = lane; j < a.k_stride; j += 32) {
         const size_t o = size_t(qi) * a.k_stride + j;
         if (j < kk) {
-            const uint64_t key = frb[j];
+            const uint64_t key = src[j];
             a.out_ids[o] = key_id(key);
             if (a.out_dists) a.out_dists[o] = output_dist<MET>(key_dist(key));
         } else {
@@ -547,7 +568,8 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     if (lane == 0) {
         if (a.out_count) a.out_count[qi] = kk;
         if (a.out_visited) a.out_visited[qi] = uint32_t(nvis);
-        if (a.out_cmps) a.out_cmps[qi] = cmps;
+        if (a.out_cmps) a.out_cmps[qi] = cmps_out;
+        if (a.out_fs) a.out_fs[qi] = fs;
         if constexpr (!LIST) {
             if (taint && a.taint) {
                 const uint32_t t = atomicAdd(a.taint, 1u);

@@ -30,10 +30,6 @@
 namespace nbpg {
 
 SlotLayout make_slot_layout(uint32_t Lmax, uint32_t R, bool vis_smem, uint32_t Vcap, bool hash_smem, uint32_t Scap);
-nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
-                               const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
-                               const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
-                               uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st);
 
 static int64_t now_ns()
 {

@@ -131,6 +131,34 @@ class Index:
                                      _p(ids), _p(ds, _f32p), _p(cnt), _p(vis), _p(cmps)))
         return SearchResult(ids, ds, cnt, vis, cmps)
 
+    def set_raw_points(self, raw: np.ndarray) -> None:
+        """Raw rows (f32, u8, i8; 4-bit packed rows as u8 with dtype_hint) for re-ranking: the
+        reference's Base_Points beside the quantised Q_Base_Points."""
+        raw = np.ascontiguousarray(raw)
+        if raw.shape[0] != self.n:
+            raise ValueError("raw rows must match the index's row count")
+        dt = {np.dtype(np.float32): "f32", np.dtype(np.uint8): "u8", np.dtype(np.int8): "i8"}[raw.dtype]
+        check(_lib.lib().nbpg_index_set_raw_points(self._h, _lib.DTYPES[dt], raw.shape[1], raw.ctypes.data, 0,
+                                                   raw.shape[0]))
+
+    def search_rerank(self, queries: np.ndarray, raw_queries: np.ndarray, qp: QueryParams, rerank_factor: int,
+                      start_points=(0,), launch: "LaunchConfig | None" = None) -> SearchResult:
+        """beam_search_rerank (beamSearch.h:183-247): quantised search, then exact distances of
+        the raw rows; rerank_factor > 0 re-ranks the frontier head, 0 is filtering mode."""
+        q = np.ascontiguousarray(queries)
+        rq = np.ascontiguousarray(raw_queries)
+        nq = q.shape[0]
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        prm = (launch or LaunchConfig()).params(qp)
+        kst = int(qp.k)
+        ids = np.empty((nq, kst), np.uint32)
+        ds = np.empty((nq, kst), np.float32)
+        cnt, vis, cmps = (np.empty(nq, np.uint32) for _ in range(3))
+        check(_lib.lib().nbpg_search_rerank(self._h, q.ctypes.data, rq.ctypes.data, nq, C.byref(prm), rerank_factor,
+                                            _p(sp), len(sp), kst, _p(ids), _p(ds, _f32p), _p(cnt), _p(vis),
+                                            _p(cmps)))
+        return SearchResult(ids, ds, cnt, vis, cmps)
+
     def qsearch_all(self, queries: np.ndarray, qp: QueryParams, start_points=(0,)) -> list[np.ndarray]:
         """qsearchAll: list of neighbour-id arrays, one per query."""
         r = self.search(queries, qp, start_points)

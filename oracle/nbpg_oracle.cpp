@@ -122,6 +122,7 @@ struct Cell {
     std::vector<Node> frontier, new_frontier, unvisited, candidates, visited, pool;
     std::vector<uint32_t> table, filtered;
     size_t fs = 0, vs = 0, num_visited = 0;
+    size_t inserted = 0;  // expansions that entered the capped visited list
 
     void reset(uint32_t L_, uint32_t max_visited_, uint32_t R)
     {
@@ -138,7 +139,7 @@ struct Cell {
         if (filtered.size() < R + 1) filtered.resize(R + 1);
         if (table.size() < slots) table.resize(slots);
         std::fill_n(table.begin(), slots, 0xFFFFFFFFu);
-        fs = vs = num_visited = 0;
+        fs = vs = num_visited = inserted = 0;
     }
 
     bool seen(uint32_t a)
@@ -195,7 +196,10 @@ size_t beam_search(Cell &c, const GraphView &G, DistTo dist_to, int64_t self, ui
         ++c.num_visited;
         if (c.vs < c.max_visited) ++c.vs;
         if (pos + 1 < c.vs) std::memmove(&c.visited[pos + 1], &c.visited[pos], (c.vs - 1 - pos) * sizeof(Node));
-        if (pos < c.vs) c.visited[pos] = cur;
+        if (pos < c.vs) {
+            c.visited[pos] = cur;
+            ++c.inserted;
+        }
 
         // deferred merge (beamSearch.h:119-125)
         if (cs == 0 || (limit >= uint64_t(uint32_t(2 * L)) && cs < L / 8 && offset + 1 < remain)) {
@@ -618,6 +622,90 @@ int nbpg_oracle_search(int dtype, int metric, uint32_t dims, const void *base, u
                 out_dists[size_t(qi) * k_stride + j] = j < kk ? c.frontier[j].d : std::numeric_limits<float>::infinity();
             }
             if (out_count) out_count[qi] = uint32_t(kk);
+            if (out_visited) out_visited[qi] = uint32_t(c.num_visited);
+            if (out_cmps) out_cmps[qi] = uint32_t(cmps);
+        }
+    }
+    return 0;
+}
+
+// beam_search_rerank (beamSearch.h:183-247) with raw rows of raw_dtype (U8/I8/U4/I4 = 0..3,
+// F32 = 4) beside the quantised rows searched.  Without exact storage (equal row sizes,
+// beamSearch.h:23-26) this is the plain search.  rerank_factor > 0: exact distances of
+// frontier[0 : min(k * rerank_factor, fs)] sorted by (dist, id), first k; only the search's
+// distances are counted.  rerank_factor == 0 (filtered_beam_search with track_exact_dist,
+// beamSearch.h:95-115, 162-168): the same search; each expansion inserted into the visited
+// list gets an exact distance (counted), the list is sorted by (exact, id), cut to
+// min(fs, visited size) (beamSearch.h:217), first k.  Float rows: point.h:137-156 in index order.
+static float raw_dist(int raw_dtype, int metric, const uint8_t *a, const uint8_t *b, uint32_t raw_dims)
+{
+    if (raw_dtype != 4) return dist_rows(raw_dtype, metric, a, b, raw_dims);
+    const float *p = reinterpret_cast<const float *>(a), *q = reinterpret_cast<const float *>(b);
+    float r = 0.0f;
+    for (uint32_t i = 0; i < raw_dims; ++i) {
+        if (metric == 0) {
+            const float d = p[i] - q[i];
+            const float sq = d * d;
+            r = r + sq;
+        } else {
+            const float pr = p[i] * q[i];
+            r = r + pr;
+        }
+    }
+    return metric == 0 ? r : -r;
+}
+
+int nbpg_oracle_search_rerank(int dtype, int raw_dtype, int metric, uint32_t dims, uint32_t raw_dims,
+                              const void *base, const void *raw_base, uint64_t n, const uint32_t *graph, uint32_t R,
+                              const void *queries, const void *raw_queries, uint32_t nq, uint32_t L, uint32_t k,
+                              uint32_t rerank_factor, double cut, uint32_t visited_factor, const uint32_t *sp,
+                              uint32_t nsp, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
+                              uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps, int threads)
+{
+    if (k > L || nsp > L || k > k_stride || L == 0) return 1;
+    const size_t rb = row_bytes(dtype, dims);
+    const size_t rrb = raw_dtype == 4 ? size_t(raw_dims) * 4 : row_bytes(raw_dtype, raw_dims);
+    const bool exact = rrb != rb;
+    const uint8_t *B = static_cast<const uint8_t *>(base), *RB = static_cast<const uint8_t *>(raw_base);
+    const uint8_t *Q = static_cast<const uint8_t *>(queries), *RQ = static_cast<const uint8_t *>(raw_queries);
+    GraphView gv{graph, R};
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel num_threads(threads)
+    {
+        Cell c;
+        std::vector<Node> pts;
+#pragma omp for schedule(dynamic, 16)
+        for (long long qi = 0; qi < (long long)nq; ++qi) {
+            const uint8_t *q = Q + size_t(qi) * rb, *rq = RQ + size_t(qi) * rrb;
+            auto dist_to = [&](uint32_t a) { return dist_rows(dtype, metric, B + size_t(a) * rb, q, dims); };
+            c.reset(L, visited_factor * L, R);
+            seed_frontier(c, sp, nsp, dist_to);
+            size_t cmps = beam_search(c, gv, dist_to, -1, k, cut, n, R);
+            pts.clear();
+            if (!exact) {
+                pts.assign(c.frontier.begin(), c.frontier.begin() + std::min<size_t>(k, c.fs));
+            } else if (rerank_factor > 0) {
+                const size_t num_check = std::min<size_t>(size_t(k) * rerank_factor, c.fs);
+                for (size_t i = 0; i < num_check; ++i) {
+                    const uint32_t j = c.frontier[i].id;
+                    pts.push_back(Node{j, raw_dist(raw_dtype, metric, RB + size_t(j) * rrb, rq, raw_dims)});
+                }
+                std::sort(pts.begin(), pts.end(), node_less);
+                pts.resize(std::min<size_t>(k, pts.size()));
+            } else {
+                for (size_t i = 0; i < c.vs; ++i) {
+                    const uint32_t j = c.visited[i].id;
+                    pts.push_back(Node{j, raw_dist(raw_dtype, metric, RB + size_t(j) * rrb, rq, raw_dims)});
+                }
+                std::sort(pts.begin(), pts.end(), node_less);
+                pts.resize(std::min<size_t>(k, std::min(c.fs, c.vs)));
+                cmps += c.inserted;
+            }
+            for (size_t j = 0; j < k_stride; ++j) {
+                out_ids[size_t(qi) * k_stride + j] = j < pts.size() ? pts[j].id : 0xFFFFFFFFu;
+                out_dists[size_t(qi) * k_stride + j] = j < pts.size() ? pts[j].d : std::numeric_limits<float>::infinity();
+            }
+            if (out_count) out_count[qi] = uint32_t(pts.size());
             if (out_visited) out_visited[qi] = uint32_t(c.num_visited);
             if (out_cmps) out_cmps[qi] = uint32_t(cmps);
         }

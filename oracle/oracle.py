@@ -67,6 +67,13 @@ class CpuLib:
                                C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.c_double, C.c_double,
                                C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint64, _u32p, _u32p, _u32p,
                                _u64p, C.c_int]
+        if hasattr(self.lib, prefix + "search_rerank"):
+            f("search_rerank").restype = C.c_int
+            f("search_rerank").argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                           C.c_uint64, _u32p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                           C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, C.c_uint32, _u32p,
+                                           C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p, _u32p, _u32p] + \
+                ([C.c_int] if prefix == "nbpg_oracle_" else [])
         if hasattr(self.lib, prefix + "pca_encode"):
             f("pca_encode").restype = C.c_int
             f("pca_encode").argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_uint32, _f32p, _f32p, C.c_uint32, C.c_int,
@@ -176,6 +183,29 @@ class CpuLib:
             raise ValueError("gt rejected its arguments")
         return ids, ds
 
+
+    def search_rerank(self, dtype, metric, base, raw_base, graph, queries, raw_queries, L, k, rerank_factor,
+                      cut=1.35, visited_factor=8, start_points=(0,)):
+        """beam_search_rerank with raw rows (f32, u8 or i8) beside the quantised rows;
+        returns (ids, dists, count, visited, cmps)."""
+        base, raw_base = np.ascontiguousarray(base), np.ascontiguousarray(raw_base)
+        queries, raw_queries = np.ascontiguousarray(queries), np.ascontiguousarray(raw_queries)
+        graph = np.ascontiguousarray(graph, dtype=np.uint32)
+        raw_dt = {np.dtype(np.float32): 4, np.dtype(np.uint8): 0, np.dtype(np.int8): 1}[raw_base.dtype]
+        n, nq = base.shape[0], queries.shape[0]
+        sp = np.array(start_points, np.uint32)
+        ids = np.empty((nq, k), np.uint32)
+        ds = np.empty((nq, k), np.float32)
+        cnt, vis, cmps = (np.empty(nq, np.uint32) for _ in range(3))
+        args = [DTYPES[dtype], raw_dt, METRICS[metric], base.shape[1], raw_base.shape[1], base.ctypes.data,
+                raw_base.ctypes.data, n, _p(graph, _u32p), graph.shape[1] - 1, queries.ctypes.data,
+                raw_queries.ctypes.data, nq, L, k, rerank_factor, cut, visited_factor, _p(sp, _u32p), len(sp), k,
+                _p(ids, _u32p), _p(ds, _f32p), _p(cnt, _u32p), _p(vis, _u32p), _p(cmps, _u32p)]
+        if self.prefix == "nbpg_oracle_":
+            args.append(0)
+        if self._f("search_rerank")(*args) != 0:
+            raise ValueError("search_rerank rejected its arguments")
+        return ids, ds, cnt, vis, cmps
 
     # -- PCA encode and format conversions (PCACompress / FmtConv) -----------------
     PCA_IN = {"f32": 0, "u8": 1, "i8": 2}

@@ -76,6 +76,44 @@ int search_t(uint32_t dims, int metric, const void *base, uint64_t n, const uint
     return 0;
 }
 
+// beam_search_rerank (beamSearch.h:183-247) with raw rows (Base_Points) of type TR beside
+// the quantised rows (Q_Base_Points) of type T; QP.rerank_factor selects rerank (> 0) or
+// filtering (0) mode.
+template <typename T, typename TR>
+int search_rerank_t(uint32_t dims, uint32_t raw_dims, int metric, const void *base, const void *raw_base, uint64_t n,
+                    const uint32_t *graph, uint32_t R, const void *queries, const void *raw_queries, uint32_t nq,
+                    uint32_t L, uint32_t k, uint32_t rerank_factor, double cut, uint32_t visited_factor,
+                    const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
+                    uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    auto Q = make_points<T>(queries, nq, dims, metric);
+    auto RB = make_points<TR>(raw_base, n, raw_dims, metric);
+    auto RQ = make_points<TR>(raw_queries, nq, raw_dims, metric);
+    auto G = make_graph(graph, n, R);
+    QueryStatic stats(nq);
+    std::vector<uint32_t> spv(sp, sp + nsp);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long i = 0; i < (long long)nq; ++i) {
+        QueryParams QP(k, L, cut, n, R);
+        QP.rerank_factor = rerank_factor;
+        BeamSearchMemoryTable<uint32_t> table(1, 1, QP.beamSize, size_t(QP.beamSize) * visited_factor, G.max_degree());
+        auto cell = table.getCell(0, 0, QP.beamSize, size_t(QP.beamSize) * visited_factor);
+        cell.init_starting_points(Q[i], B, spv.data(), nsp);
+        auto res = beam_search_rerank(cell, RQ[i], Q[i], G, RB, B, stats, QP, uint32_t(i));
+        for (uint32_t j = 0; j < k_stride; ++j) {
+            out_ids[size_t(i) * k_stride + j] = j < res.size() ? res[j].first : 0xFFFFFFFFu;
+            out_dists[size_t(i) * k_stride + j] = j < res.size() ? res[j].second : std::numeric_limits<float>::infinity();
+        }
+        if (out_count) out_count[i] = uint32_t(res.size());
+    }
+    for (uint32_t i = 0; i < nq; ++i) {
+        if (out_visited) out_visited[i] = stats.visited[i];
+        if (out_cmps) out_cmps[i] = stats.distances[i];
+    }
+    return 0;
+}
+
 template <typename T>
 int prune_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t p, uint32_t *ids, float *dists,
             uint32_t *cnt, uint32_t R, double alpha, double cos_angle, float dir_bias_scale, const uint32_t *degrees,
@@ -214,6 +252,36 @@ int nbpg_ref_search(int dtype, int metric, uint32_t dims, const void *base, uint
     default: return 1;
     }
 #undef NBPG_REF_SEARCH
+}
+
+int nbpg_ref_search_rerank(int dtype, int raw_dtype, int metric, uint32_t dims, uint32_t raw_dims, const void *base,
+                           const void *raw_base, uint64_t n, const uint32_t *graph, uint32_t R, const void *queries,
+                           const void *raw_queries, uint32_t nq, uint32_t L, uint32_t k, uint32_t rerank_factor,
+                           double cut, uint32_t visited_factor, const uint32_t *sp, uint32_t nsp, uint32_t k_stride,
+                           uint32_t *out_ids, float *out_dists, uint32_t *out_count, uint32_t *out_visited,
+                           uint32_t *out_cmps)
+{
+    if (k > L || nsp > L || k > k_stride) return 1;
+#define NBPG_REF_RR(T, TR)                                                                                            \
+    return search_rerank_t<T, TR>(dims, raw_dims, metric, base, raw_base, n, graph, R, queries, raw_queries, nq, L, k, \
+                                  rerank_factor, cut, visited_factor, sp, nsp, k_stride, out_ids, out_dists, out_count,  \
+                                  out_visited, out_cmps)
+#define NBPG_REF_RR_RAW(T)                                                                                            \
+    switch (raw_dtype) {                                                                                              \
+    case 0: NBPG_REF_RR(T, uint8_t);                                                                                  \
+    case 1: NBPG_REF_RR(T, int8_t);                                                                                   \
+    case 4: NBPG_REF_RR(T, float);                                                                                    \
+    default: return 1;                                                                                                \
+    }
+    switch (dtype) {
+    case 0: NBPG_REF_RR_RAW(uint8_t);
+    case 1: NBPG_REF_RR_RAW(int8_t);
+    case 2: NBPG_REF_RR_RAW(uint4_2);
+    case 3: NBPG_REF_RR_RAW(int4_2);
+    default: return 1;
+    }
+#undef NBPG_REF_RR_RAW
+#undef NBPG_REF_RR
 }
 
 int nbpg_ref_prune(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t p, uint32_t *ids,

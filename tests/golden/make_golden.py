@@ -13,9 +13,12 @@ Inputs are small seeded synthetic sets.  Outputs, stored as tests/golden/*.npz:
                   a .mat with bias; for u8/i8 input rows (whose path in the reference only
                   works on whole 100,000-row blocks) the seed of the rows and the SHA-256 of
                   the reference's output instead of the rows themselves;
-  * fmtconv.npz   FmtConv fbin2u8bin, u8bin2u4bin (odd row length) and vec2bin outputs.
+  * fmtconv.npz   FmtConv fbin2u8bin, u8bin2u4bin (odd row length) and vec2bin outputs;
+  * rerank_*.npz  beam_search_rerank through the harness with raw float rows beside 4-bit
+                  (L2) and u8 (inner product) quantised rows: rerank factors 100, 3 and 0
+                  (filtering mode), on a graph built by the oracle.
 
-Usage: make -C oracle ref && python tests/golden/make_golden.py
+Usage: make -C oracle ref && python tests/golden/make_golden.py [--only pca,rerank]
 """
 import os
 import subprocess
@@ -90,14 +93,38 @@ def datasets():
     return {"mix": ("u8", ".u8bin", b, q), "tie": ("u8", ".u8bin", tb, tq), "i8": ("i8", ".i8bin", ib, iq)}
 
 
+def rerank_golden():
+    from oracle.oracle import oracle
+    ref = reference()
+    r = np.random.default_rng(17)
+    n, nq, d = 1500, 40, 16
+    raw = r.normal(size=(n, d)).astype(np.float32)
+    rq = r.normal(size=(nq, d)).astype(np.float32)
+    cb = np.clip(np.round((raw + 3) * 40), 0, 255).astype(np.uint8)
+    cq = np.clip(np.round((rq + 3) * 40), 0, 255).astype(np.uint8)
+    for name, dtype, metric, qb, qq in [("u4_l2", "u4", "l2", synth.pack_u4(cb >> 4), synth.pack_u4(cq >> 4)),
+                                        ("u8_ip", "u8", "ip", cb, cq)]:
+        g, _, _, _ = oracle().build_graph(dtype, metric, qb, R=16, L=32, VL=48, num_split=0, num_passes=1)
+        out = {"base": qb, "queries": qq, "raw": raw, "raw_queries": rq, "graph": g}
+        for L, k, rf in [(32, 10, 100), (40, 5, 3), (32, 10, 0)]:
+            ids, ds, cnt, vis, cmps = ref.search_rerank(dtype, metric, qb, raw, g, qq, rq, L, k, rf)
+            out.update({f"ids_{L}_{k}_{rf}": ids, f"dists_{L}_{k}_{rf}": ds, f"count_{L}_{k}_{rf}": cnt,
+                        f"visited_{L}_{k}_{rf}": vis, f"cmps_{L}_{k}_{rf}": cmps})
+        np.savez_compressed(f"{HERE}/rerank_{name}.npz", **out)
+
+
 def main():
     if not (os.path.exists(REF_COMPGT) and os.path.exists(REF_VAMANA) and reference()):
         sys.exit("build the reference first: make -C oracle ref")
     ref = reference()
     tmp = tempfile.mkdtemp()
-    pca_golden(tmp)
-    if "--pca-only" in sys.argv:
-        print("PCA/FmtConv golden vectors written to", HERE)
+    only = sys.argv[sys.argv.index("--only") + 1].split(",") if "--only" in sys.argv else None
+    if only is None or "pca" in only:
+        pca_golden(tmp)
+    if only is None or "rerank" in only:
+        rerank_golden()
+    if only is not None:
+        print("golden vectors written to", HERE)
         return
     for name, (dt, ext, b, q) in datasets().items():
         bp, qp = f"{tmp}/{name}_b{ext}", f"{tmp}/{name}_q{ext}"
