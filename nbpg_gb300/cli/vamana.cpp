@@ -7,7 +7,8 @@
 // recall@k with distance-tie extension (check_nn_recall.h:84-184), QPS, and the CSV of
 // best-QPS rows per recall bucket (check_nn_recall.h:12-48, parse_results.h:142-180).
 // Extra flag: --sp_seed (seed of the merge-pass start points, which the reference draws
-// from std::random_device).  Re-ranking with raw vectors (--base_path) is not supported.
+// from std::random_device).  With --base_path (raw rows) and --query_path the search re-ranks
+// through nbpg_search_rerank (--rerank_factor > 0, or 0 for filtering mode).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -63,14 +64,15 @@ static void read_head(const std::string &p, uint32_t &n, uint32_t &d)
     f.read(reinterpret_cast<char *>(&d), 4);
 }
 
-static std::vector<uint8_t> read_rows(const std::string &p, uint32_t &n, uint32_t &d, uint32_t limit = 0)
+static std::vector<uint8_t> read_rows(const std::string &p, uint32_t &n, uint32_t &d, uint32_t limit = 0,
+                                      size_t elem = 1)
 {
     std::ifstream f(p, std::ios::binary);
     if (!f) die("cannot open " + p);
     f.read(reinterpret_cast<char *>(&n), 4);
     f.read(reinterpret_cast<char *>(&d), 4);
     if (limit && limit < n) n = limit;
-    std::vector<uint8_t> v(size_t(n) * d);
+    std::vector<uint8_t> v(size_t(n) * d * elem);
     f.read(reinterpret_cast<char *>(v.data()), v.size());
     if (!f) die("truncated " + p);
     return v;
@@ -106,9 +108,24 @@ static void write_graph(const std::string &p, const std::vector<uint32_t> &g, ui
         w.write(reinterpret_cast<const char *>(&g[size_t(i) * (R + 1) + 1]), size_t(g[size_t(i) * (R + 1)]) * 4);
 }
 
-// host distance for the recall's tie check (point.h:35-135)
+// host distance for the recall's tie check (point.h:35-156); float rows in index order
 static float host_dist(uint32_t dtype, bool mips, const uint8_t *a, const uint8_t *b, uint32_t d)
 {
+    if (dtype == NBPG_F32) {
+        const float *x = reinterpret_cast<const float *>(a), *y = reinterpret_cast<const float *>(b);
+        float r = 0.0f;
+        for (uint32_t i = 0; i < d; ++i) {
+            if (mips) {
+                const float pr = x[i] * y[i];
+                r = r + pr;
+            } else {
+                const float df = x[i] - y[i];
+                const float sq = df * df;
+                r = r + sq;
+            }
+        }
+        return mips ? -r : r;
+    }
     int32_t r = 0;
     for (uint32_t i = 0; i < d; ++i) {
         if (dtype == NBPG_U8 || dtype == NBPG_I8) {
@@ -235,10 +252,31 @@ int main(int argc, char **argv)
 
     // ---- query evaluation (Vamana.cpp:234-280, check_nn_recall.h)
     if (a.quant_query_path.empty() || a.gt_path.empty()) return 0;
-    if (!a.base_path.empty()) die("nbpg_vamana: re-ranking with raw vectors (--base_path) is not supported");
     uint32_t nq, qd;
     std::vector<uint8_t> Q = read_rows(a.quant_query_path, nq, qd, a.q_num);
     if (qd != dims) die("query and base dimensions differ");
+    // raw rows for re-ranking (Vamana.cpp:212-231, 253-275): --base_path of any vector type
+    // with --query_path of the same type; --cache_raw only chooses host memory over a file
+    // mapping in the reference, here the raw rows live on the device either way
+    uint32_t raw_dtype = dtype, raw_dims = dims, rn = n, rqn = nq;
+    std::vector<uint8_t> raw_base, raw_q;
+    const bool raw = !a.base_path.empty();
+    if (raw) {
+        if (ends_with(a.base_path, ".u8bin")) raw_dtype = NBPG_U8;
+        else if (ends_with(a.base_path, ".u4bin")) raw_dtype = NBPG_U4;
+        else if (ends_with(a.base_path, ".i8bin")) raw_dtype = NBPG_I8;
+        else if (ends_with(a.base_path, ".i4bin")) raw_dtype = NBPG_I4;
+        else if (ends_with(a.base_path, ".fbin") || ends_with(a.base_path, ".bin")) raw_dtype = NBPG_F32;
+        else return 0;  // the reference runs no query for other extensions
+        const size_t elem = raw_dtype == NBPG_F32 ? 4 : 1;
+        raw_base = read_rows(a.base_path, rn, raw_dims, 0, elem);
+        uint32_t rqd = 0;
+        raw_q = read_rows(a.query_path, rqn, rqd, a.q_num, elem);
+        if (rn != n || rqn != nq || rqd != raw_dims) die("raw base/query files do not match the quantised ones");
+    }
+    const std::vector<uint8_t> &tie_base = raw ? raw_base : base, &tie_q = raw ? raw_q : Q;
+    const uint32_t tie_dtype = raw ? raw_dtype : dtype, tie_dims = raw ? raw_dims : dims;
+    const size_t tie_row = size_t(tie_dims) * (tie_dtype == NBPG_F32 ? 4 : 1);
     std::ifstream gf(a.gt_path, std::ios::binary);
     if (!gf) die("cannot open " + a.gt_path);
     uint32_t gnq, gk;
@@ -255,23 +293,30 @@ int main(int argc, char **argv)
     check(nbpg_index_create(&d, &idx));
     check(nbpg_index_set_points(idx, base.data(), 0, n));
     check(nbpg_index_set_graph(idx, G.data(), 0, n));
+    if (raw) check(nbpg_index_set_raw_points(idx, raw_dtype, raw_dims, raw_base.data(), 0, n));
 
     auto run_check = [&](uint32_t r, uint32_t qk, uint32_t beam, double cut, uint64_t limit, uint32_t dl) {
         nbpg_search_params sp{qk, beam, cut, limit, dl, 8, NBPG_KERNEL_BATCHED, 0, 0, -1};
         const uint32_t start = 0;
         std::vector<uint32_t> ids(size_t(nq) * qk), cnt(nq), vis(nq), cmps(nq);
         auto t0 = std::chrono::steady_clock::now();
-        check(nbpg_search(idx, Q.data(), nq, &sp, nullptr, nullptr, &start, 1, qk, ids.data(), nullptr, cnt.data(),
-                          vis.data(), cmps.data()));
+        if (raw)
+            check(nbpg_search_rerank(idx, Q.data(), raw_q.data(), nq, &sp, a.rerank_factor, &start, 1, qk, ids.data(),
+                                     nullptr, cnt.data(), vis.data(), cmps.data()));
+        else
+            check(nbpg_search(idx, Q.data(), nq, &sp, nullptr, nullptr, &start, 1, qk, ids.data(), nullptr, cnt.data(),
+                              vis.data(), cmps.data()));
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         long correct = 0;
         for (uint32_t i = 0; i < nq; ++i) {
             std::vector<uint32_t> with_ties(gt.begin() + size_t(i) * gk, gt.begin() + size_t(i) * gk + r);
-            const uint8_t *qp = &Q[size_t(i) * dims];
-            const float last = host_dist(dtype, a.use_mips, &base[size_t(gt[size_t(i) * gk + r - 1]) * dims], qp, dims);
+            const uint8_t *qp = &tie_q[size_t(i) * tie_row];
+            const float last =
+                host_dist(tie_dtype, a.use_mips, &tie_base[size_t(gt[size_t(i) * gk + r - 1]) * tie_row], qp, tie_dims);
             for (uint32_t l = r; l < gk; ++l) {
                 const uint32_t id = gt[size_t(i) * gk + l];
-                if (host_dist(dtype, a.use_mips, &base[size_t(id) * dims], qp, dims) == last) with_ties.push_back(id);
+                if (host_dist(tie_dtype, a.use_mips, &tie_base[size_t(id) * tie_row], qp, tie_dims) == last)
+                    with_ties.push_back(id);
                 else break;
             }
             std::set<uint32_t> rep;

@@ -60,3 +60,31 @@ def test_vamana_drop_in_writes_identical_graph_and_evaluates(gpu_lib, tmp_path, 
                         "--quant_query_path", str(qf), "--gt_path", str(gtf), "--Q", "5", "--k", "10"],
                        capture_output=True, text=True)
     assert r.returncode != 0 and "same size or smaller than k" in r.stderr
+
+
+@pytest.mark.parametrize("rf", [100, 0])
+def test_vamana_drop_in_reranks_with_raw_vectors(gpu_lib, tmp_path, rf):
+    """--base_path/--query_path raw float rows beside 4-bit codes: the recall nbpg_vamana
+    reports equals the recall of the reference's beam_search_rerank results (golden)."""
+    import re
+    from nbpg_gb300 import formats
+    z = np.load(os.path.join(GOLDEN, "rerank_u4_l2.npz"))
+    qb, rb, qq, rq = (tmp_path / n for n in ("b.u4bin", "b.fbin", "q.u4bin", "q.fbin"))
+    formats.write_vectors(str(qb), z["base"])
+    formats.write_vectors(str(rb), z["raw"])
+    formats.write_vectors(str(qq), z["queries"])
+    formats.write_vectors(str(rq), z["raw_queries"])
+    idx = tmp_path / "idx"
+    formats.write_graph(str(idx) + ".graph", z["graph"])
+    raw, rqv = z["raw"].astype(np.float64), z["raw_queries"].astype(np.float64)
+    gt = np.argsort(((rqv[:, None, :] - raw[None, :, :]) ** 2).sum(-1), axis=1, kind="stable")[:, :50].astype(np.uint32)
+    formats.write_gt(str(tmp_path / "g.gt"), gt, np.zeros(gt.shape, np.float32))
+    r = subprocess.run([_exe("nbpg_vamana"), "--quant_base_path", str(qb), "--index_path", str(idx),
+                        "--base_path", str(rb), "--query_path", str(rq), "--quant_query_path", str(qq),
+                        "--gt_path", str(tmp_path / "g.gt"), "--Q", "32", "--k", "10", "--rerank_factor", str(rf),
+                        "--cache_raw"], check=True, capture_output=True, text=True)
+    got = [float(m) for m in re.findall(r"recall = ([0-9.eE+-]+)", r.stdout)]
+    ids = z[f"ids_32_10_{rf}"]
+    correct = sum(len(set(ids[i, :10].tolist()) & set(gt[i, :10].tolist())) for i in range(len(ids)))
+    want = float(np.float32(correct) / np.float32(10 * len(ids)))
+    assert len(got) == 5 and all(abs(g - want) < 1e-5 for g in got), (got, want)
