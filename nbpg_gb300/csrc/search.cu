@@ -92,7 +92,21 @@ static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, 
         return NBPG_OK;
     }
     uint32_t fit = uint32_t(idx->smem_optin / pc.lay.bytes);
-    uint32_t w = want_warps ? want_warps : std::min<uint32_t>(16, fit);
+    uint32_t w = want_warps;
+    if (!w) {
+        // default: the CTA size with the most resident warps per SM (registers or shared
+        // memory, whichever binds), the larger CTA on a tie
+        int best = -1;
+        for (uint32_t c : {16u, 8u, 4u, 2u}) {
+            if (c > fit) continue;
+            const size_t sm = size_t(c) * pc.lay.bytes;
+            int b = 0;
+            NBPG_CUDA_TRY(ops->set_attr(metric, list, false, sm));
+            NBPG_CUDA_TRY(ops->occ(metric, list, false, int(c) * 32, sm, &b));
+            if (int(c) * b > best) { best = int(c) * b; w = c; }
+        }
+        if (!w) w = 1;
+    }
     w = std::max<uint32_t>(1, std::min<uint32_t>(w, std::min<uint32_t>(16, fit)));
     pc.warps = w;
     pc.smem = size_t(w) * pc.lay.bytes;
