@@ -282,7 +282,7 @@ static cudaError_t launch_gt(const GtArgs &a, size_t smem, cudaStream_t st)
 bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_optin);
 nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t stride, const uint8_t *d_base,
                          uint64_t n, const uint8_t *d_q, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *d_ids,
-                         float *d_dists, void *ws, cudaStream_t st);
+                         float *d_dists, void *ws, cudaStream_t st, bool withhold = false);
 size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq);
 
 nbpg_status gt_device(uint32_t dtype, uint32_t metric, const GtArgs &a, cudaStream_t st, size_t smem_optin)

@@ -34,7 +34,8 @@ constexpr int TC_KATOM = 64;     // bf16 elements per 128-byte swizzled row
 constexpr uint32_t TC_MAX_STAGES = 4;  // shared-memory ring of base tiles: 2..4 deep as memory allows
 constexpr uint32_t TC_ACC = 4;         // TMEM accumulators of 128 columns: all 512 columns of the SM
 constexpr int TC_THREADS = 192;  // warps 0-3 epilogue, 4 TMA, 5 MMA
-constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+constexpr uint64_t TC_WAIT_NS = 2000000000ull;  // 2 s: far above any wait of a working pipeline
+constexpr uint32_t TC_WAIT_POLLS = 1u << 30;
 constexpr uint32_t TC_QUEUE = 8;  // flagged candidates queued per query before a drain
 
 struct TcArgs {
@@ -45,6 +46,7 @@ struct TcArgs {
     uint32_t katoms;               // K / 64
     uint32_t ntiles;
     uint32_t stages;               // depth of the base-tile ring
+    uint32_t withhold;             // test hook: the producer issues no base tiles
     uint32_t *out_ids;
     float *out_dists;
     uint32_t *err;
@@ -70,10 +72,20 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
-// bounded wait for the phase of the given parity; false (and *err set) on timeout
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the phase of the given parity; false (and *err set) when it has not
+// completed within TC_WAIT_NS of wall time (try_wait may itself suspend the thread for a
+// while, so the bound is on the clock, with a poll count as the last resort).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t *err)
 {
-    for (uint32_t it = 0; it < TC_WAIT_LIMIT; ++it) {
+    uint64_t t0 = 0;
+    for (uint32_t it = 0; it < TC_WAIT_POLLS; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -81,7 +93,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_
             : "r"(bar), "r"(parity)
             : "memory");
         if (done) return true;
-        if (it > 64) __nanosleep(64);
+        if (it == 64) t0 = global_ns();
+        if (it > 64) {
+            __nanosleep(64);
+            if ((it & 255) == 0 && global_ns() - t0 > TC_WAIT_NS) break;
+        }
     }
     atomicExch(err, 1u);
     return false;
@@ -349,7 +365,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (uint32_t c = 0; c < a.katoms; ++c)
                 tma_load_2d(smem_u32(sA + c * atom_bytes), &tmA, int32_t(c * TC_KATOM), int32_t(q0), bar_a);
             uint32_t issued = 0, s = 0, ph = 0;
-            for (uint32_t t = 0; t < T; ++t) {
+            for (uint32_t t = 0; t < (a.withhold ? 0u : T); ++t) {
                 if (!mbar_wait(bar_empty + 8 * s, ph ^ 1, a.err)) break;
                 mbar_expect_tx(bar_full + 8 * s, tile_bytes);
                 for (uint32_t c = 0; c < a.katoms; ++c)
@@ -670,7 +686,7 @@ size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq)
 // kernel has finished (the error flag of the bounded waits is read back).
 nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t stride, const uint8_t *d_base,
                          uint64_t n, const uint8_t *d_q, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *d_ids,
-                         float *d_dists, void *ws, cudaStream_t st)
+                         float *d_dists, void *ws, cudaStream_t st, bool withhold = false)
 {
     const bool nib = dtype == NBPG_U4 || dtype == NBPG_I4;
     const TcLayout l = tc_layout(dtype, dims, n, nq);
@@ -729,7 +745,7 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e == cudaSuccess && s == NBPG_OK) {
         TcArgs a{qn, bn, n, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, nib ? 256u : 1u, l.katoms,
-                 uint32_t(n_pad / TC_N), stages, d_ids, d_dists, err};
+                 uint32_t(n_pad / TC_N), stages, withhold ? 1u : 0u, d_ids, d_dists, err};
         if (metric == NBPG_L2) gt_tc_kernel<M_L2><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
         else gt_tc_kernel<M_IP><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
         e = cudaGetLastError();
@@ -753,3 +769,35 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
 }
 
 }  // namespace nbpg
+
+// Test hook for the failure path: the tensor kNN on a small problem with its base tiles
+// withheld, so the MMA and epilogue waits run out (nothing ever arrives on those barriers);
+// the kernel must record the timeout, tear down (final commit, TMEM freed) and return, and
+// the context must stay usable.  Returns NBPG_ERR_TIMEOUT on that path.
+extern "C" nbpg_status nbpg_test_gt_timeout(int32_t device)
+{
+    using namespace nbpg;
+    NBPG_CUDA_TRY(cudaSetDevice(device));
+    const uint32_t n = 512, nq = 128, dims = 64, k = 10;
+    uint8_t *db = nullptr, *dq = nullptr;
+    uint32_t *di = nullptr;
+    float *dd = nullptr;
+    cudaError_t e = cudaMalloc(&db, n * dims);
+    if (e == cudaSuccess) e = cudaMalloc(&dq, nq * dims);
+    if (e == cudaSuccess) e = cudaMalloc(&di, nq * k * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dd, nq * k * 4);
+    if (e == cudaSuccess) e = cudaMemset(db, 7, n * dims);
+    if (e == cudaSuccess) e = cudaMemset(dq, 3, nq * dims);
+    nbpg_status s = NBPG_ERR_CUDA;
+    if (e == cudaSuccess) s = gt_tc_device(NBPG_U8, NBPG_L2, dims, dims, db, n, dq, nq, k, NBPG_GT_COMPGT, di, dd,
+                                           nullptr, nullptr, true);
+    cudaFree(db);
+    cudaFree(dq);
+    cudaFree(di);
+    cudaFree(dd);
+    if (e != cudaSuccess) {
+        set_error(std::string("nbpg_test_gt_timeout: ") + cudaGetErrorString(e));
+        return NBPG_ERR_CUDA;
+    }
+    return s;
+}

@@ -114,3 +114,22 @@ def test_gt_device_entry(gpu_lib, oracle_lib, engine):
             oi, od = oracle_lib.gt("u8", "l2", b, q, k=k, exact=exact)
             assert np.array_equal(ids.cpu().numpy().view(np.uint32), oi), (use_ws, exact)
             assert np.array_equal(ds.cpu().numpy(), od), (use_ws, exact)
+
+
+def test_tensor_engine_timeout_path(gpu_lib, oracle_lib):
+    """The bounded waits of the tensor kNN, exercised without a fault: with its base tiles
+    withheld, the kernel's waits run out (2 s), it records the timeout, tears down and
+    returns NBPG_ERR_TIMEOUT; the context stays usable for the next call."""
+    import time
+    from nbpg_gb300 import synth
+    from nbpg_gb300._lib import lib
+    from nbpg_gb300.index import ground_truth
+    t = time.time()
+    status = lib().nbpg_test_gt_timeout(0)
+    took = time.time() - t
+    assert status == 4, (status, lib().nbpg_last_error())  # NBPG_ERR_TIMEOUT
+    assert 1.5 < took < 60, took
+    b, q = synth.u8_mixture(2000, 130, dim=64, n_centres=8)
+    ids, ds = ground_truth(b, q, "u8", "l2", k=10, engine="tensor")
+    oi, od = oracle_lib.gt("u8", "l2", b, q, k=10)
+    assert np.array_equal(ids, oi) and np.array_equal(ds, od)
