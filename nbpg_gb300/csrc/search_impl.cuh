@@ -431,6 +431,27 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         }
         offset = 0;
 
+        if (cst == 0) {
+            // Every candidate of this round lies at or past the full frontier's last key: the
+            // union truncated to L is the frontier itself, and the cut rule keeps at least the
+            // old size, so the merge changes nothing but the unvisited list (no taint either).
+            cs = 0;
+            remain = 0;
+            for (uint32_t base = 0; base < fs; base += 32) {
+                const uint32_t i = base + lane;
+                bool un = false;
+                if (i < fs) {
+                    if constexpr (LIST) un = !contains(vis, vs, frb[i]);
+                    else un = flb[i] == 0;
+                }
+                const unsigned m = __ballot_sync(kFull, un);
+                if (un) unv[remain + __popc(m & lanemask_lt())] = uint16_t(i);
+                remain += __popc(m);
+            }
+            __syncwarp();
+            continue;
+        }
+
         // sort + unique candidates, set_union with the frontier, truncate to L (beamSearch.h:128-138)
         const uint32_t cu = sort_unique_minus(cand, cst, frb, fs, lane);
         const int nb2 = b ^ 1;
@@ -601,9 +622,10 @@ __global__ void __maxnreg__(80) search_batched_kernel(SearchArgs a)
     }
 }
 
-// Plain form: one query per thread block of one warp; everything in shared memory.
+// Plain form: one query per thread block of one warp; everything in shared memory.  Held
+// to 72 registers so that 28 blocks (warps) fit per SM.
 template <int DT, int MET, bool LIST, int VPL>
-__global__ void __launch_bounds__(32) search_plain_kernel(SearchArgs a)
+__global__ void __launch_bounds__(32, 28) search_plain_kernel(SearchArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t total = a.only ? a.only[0] : a.nq;
