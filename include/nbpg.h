@@ -275,6 +275,16 @@ nbpg_status nbpg_search_rerank(nbpg_index *idx, const void *queries, const void 
                                uint32_t n_start, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
                                uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps);
 
+/* Recall with distance-tie extension on the device (calRecall, data_tools/ANNs/base/
+ * check_nn_recall.h:84-167): for each query, the first r ground-truth ids plus the
+ * following ids whose distance equals the r-th one's, counted against the first
+ * min(r, count) reported ids.  Distances use the raw rows (use_raw != 0, queries in raw
+ * rows) or the quantised rows (queries in quantised rows).  *correct receives the count;
+ * recall = correct / (r * nq) as the reference computes it. */
+nbpg_status nbpg_eval_recall(nbpg_index *idx, int32_t use_raw, const void *queries, uint32_t nq,
+                             const uint32_t *ids, const uint32_t *count, uint32_t k_stride, const uint32_t *gt,
+                             uint32_t gk, uint32_t r, uint64_t *correct);
+
 /* ---------------------------------------------------------------------------
  * PCA encode.  Replaces PCACompress's matmul + compress (data_tools/ANNs/data_proc/
  * base/matrix.h:86-125, driven by PCACompress.cpp:21-83): values[j] = bias[j] + mat[j] . x,

@@ -110,6 +110,8 @@ def lib() -> C.CDLL:
     L.nbpg_gt_device.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_uint64, _vp, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, _vp, _vp, _vp, C.c_size_t, _vp]
     L.nbpg_test_gt_timeout.argtypes = [C.c_int32]
+    L.nbpg_eval_recall.argtypes = [_vp, C.c_int32, _vp, C.c_uint32, _u32p, _u32p, C.c_uint32, _u32p, C.c_uint32,
+                                   C.c_uint32, C.POINTER(C.c_uint64)]
     L.nbpg_index_set_raw_points.argtypes = [_vp, C.c_uint32, C.c_uint32, _vp, C.c_uint64, C.c_uint64]
     L.nbpg_search_rerank.argtypes = [_vp, _vp, _vp, C.c_uint32, C.POINTER(SearchParams), C.c_uint32, _u32p,
                                      C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p, _u32p, _u32p]

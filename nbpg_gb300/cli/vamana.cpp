@@ -108,37 +108,6 @@ static void write_graph(const std::string &p, const std::vector<uint32_t> &g, ui
         w.write(reinterpret_cast<const char *>(&g[size_t(i) * (R + 1) + 1]), size_t(g[size_t(i) * (R + 1)]) * 4);
 }
 
-// host distance for the recall's tie check (point.h:35-156); float rows in index order
-static float host_dist(uint32_t dtype, bool mips, const uint8_t *a, const uint8_t *b, uint32_t d)
-{
-    if (dtype == NBPG_F32) {
-        const float *x = reinterpret_cast<const float *>(a), *y = reinterpret_cast<const float *>(b);
-        float r = 0.0f;
-        for (uint32_t i = 0; i < d; ++i) {
-            if (mips) {
-                const float pr = x[i] * y[i];
-                r = r + pr;
-            } else {
-                const float df = x[i] - y[i];
-                const float sq = df * df;
-                r = r + sq;
-            }
-        }
-        return mips ? -r : r;
-    }
-    int32_t r = 0;
-    for (uint32_t i = 0; i < d; ++i) {
-        if (dtype == NBPG_U8 || dtype == NBPG_I8) {
-            const int32_t x = dtype == NBPG_U8 ? int32_t(a[i]) : int32_t(int8_t(a[i]));
-            const int32_t y = dtype == NBPG_U8 ? int32_t(b[i]) : int32_t(int8_t(b[i]));
-            r += mips ? x * y : (x - y) * (x - y);
-        } else {
-            const int32_t ah = a[i] & 0xF0, al = uint8_t(a[i] << 4), bh = b[i] & 0xF0, bl = uint8_t(b[i] << 4);
-            r += mips ? ah * bh + al * bl : (ah - bh) * (ah - bh) + (al - bl) * (al - bl);
-        }
-    }
-    return mips ? -float(r) : float(r);
-}
 
 struct Result {
     double recall, qps;
@@ -274,9 +243,7 @@ int main(int argc, char **argv)
         raw_q = read_rows(a.query_path, rqn, rqd, a.q_num, elem);
         if (rn != n || rqn != nq || rqd != raw_dims) die("raw base/query files do not match the quantised ones");
     }
-    const std::vector<uint8_t> &tie_base = raw ? raw_base : base, &tie_q = raw ? raw_q : Q;
-    const uint32_t tie_dtype = raw ? raw_dtype : dtype, tie_dims = raw ? raw_dims : dims;
-    const size_t tie_row = size_t(tie_dims) * (tie_dtype == NBPG_F32 ? 4 : 1);
+    const std::vector<uint8_t> &tie_q = raw ? raw_q : Q;
     std::ifstream gf(a.gt_path, std::ios::binary);
     if (!gf) die("cannot open " + a.gt_path);
     uint32_t gnq, gk;
@@ -307,22 +274,11 @@ int main(int argc, char **argv)
             check(nbpg_search(idx, Q.data(), nq, &sp, nullptr, nullptr, &start, 1, qk, ids.data(), nullptr, cnt.data(),
                               vis.data(), cmps.data()));
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        long correct = 0;
-        for (uint32_t i = 0; i < nq; ++i) {
-            std::vector<uint32_t> with_ties(gt.begin() + size_t(i) * gk, gt.begin() + size_t(i) * gk + r);
-            const uint8_t *qp = &tie_q[size_t(i) * tie_row];
-            const float last =
-                host_dist(tie_dtype, a.use_mips, &tie_base[size_t(gt[size_t(i) * gk + r - 1]) * tie_row], qp, tie_dims);
-            for (uint32_t l = r; l < gk; ++l) {
-                const uint32_t id = gt[size_t(i) * gk + l];
-                if (host_dist(tie_dtype, a.use_mips, &tie_base[size_t(id) * tie_row], qp, tie_dims) == last)
-                    with_ties.push_back(id);
-                else break;
-            }
-            std::set<uint32_t> rep;
-            for (uint32_t l = 0; l < r && l < cnt[i]; ++l) rep.insert(ids[size_t(i) * qk + l]);
-            for (uint32_t id : with_ties) correct += rep.count(id);
-        }
+        // tie-extended recall on the device (check_nn_recall.h:84-167), over the raw rows when
+        // --base_path gave them, else the quantised rows
+        uint64_t correct = 0;
+        check(nbpg_eval_recall(idx, raw ? 1 : 0, tie_q.data(), nq, ids.data(), cnt.data(), qk, gt.data(), gk, r,
+                               &correct));
         Result res;
         res.recall = double(float(correct) / float(r * nq));
         res.qps = nq / secs;

@@ -250,3 +250,106 @@ extern "C" nbpg_status nbpg_search_rerank(nbpg_index *idx, const void *queries, 
     }
     return NBPG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Recall with distance-tie extension (calRecall, data_tools/ANNs/base/check_nn_recall.h:84-167),
+// on the device: per query, the first r ground-truth ids plus every further id whose distance
+// equals the r-th one's (stopping at the first that differs), counted against the set of the
+// first r reported ids.  Distances come from the index's raw rows when present (the reference
+// passes Base_Points and Query_Points), else from its quantised rows.
+// ---------------------------------------------------------------------------
+namespace nbpg {
+
+struct EvalArgs {
+    const uint8_t *rows;
+    uint32_t row_pitch, dims;
+    const uint8_t *q;
+    uint32_t q_pitch;
+    const uint32_t *ids, *cnt, *gt;
+    uint32_t k_stride, gk, nq, r;
+    unsigned long long *correct;
+};
+
+template <int RDT, int MET>
+__global__ void __launch_bounds__(256) recall_kernel(EvalArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t qi = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (qi >= a.nq) return;
+    const uint32_t *g = a.gt + size_t(qi) * a.gk;
+    const uint8_t *q = a.q + size_t(qi) * a.q_pitch;
+    uint32_t with = a.r;  // results_with_ties = g[0 : with)
+    if (lane == 0) {
+        const float last = raw_distance<RDT, MET>(a.rows + size_t(g[a.r - 1]) * a.row_pitch, q, a.dims);
+        while (with < a.gk && raw_distance<RDT, MET>(a.rows + size_t(g[with]) * a.row_pitch, q, a.dims) == last) ++with;
+    }
+    with = __shfl_sync(kFull, with, 0);
+    const uint32_t rep = a.cnt[qi] < a.r ? a.cnt[qi] : a.r;
+    const uint32_t *ids = a.ids + size_t(qi) * a.k_stride;
+    uint32_t hits = 0;
+    for (uint32_t l = lane; l < with; l += 32) {
+        const uint32_t id = g[l];
+        for (uint32_t j = 0; j < rep; ++j)
+            if (ids[j] == id) { ++hits; break; }
+    }
+    for (int o = 16; o > 0; o >>= 1) hits += __shfl_xor_sync(kFull, hits, o);
+    if (lane == 0 && hits) atomicAdd(a.correct, (unsigned long long)hits);
+}
+
+template <int RDT>
+static void launch_recall(int metric, const EvalArgs &a)
+{
+    const uint32_t grid = (a.nq + 7) / 8;
+    if (metric == M_L2) recall_kernel<RDT, M_L2><<<grid, 256>>>(a);
+    else recall_kernel<RDT, M_IP><<<grid, 256>>>(a);
+}
+
+}  // namespace nbpg
+
+extern "C" nbpg_status nbpg_eval_recall(nbpg_index *idx, int32_t use_raw, const void *queries, uint32_t nq,
+                                        const uint32_t *ids, const uint32_t *count, uint32_t k_stride,
+                                        const uint32_t *gt, uint32_t gk, uint32_t r, uint64_t *correct)
+{
+    NBPG_CHECK_ARG(idx && queries && ids && count && gt && correct, "null argument");
+    NBPG_CHECK_ARG(r >= 1 && r <= gk && r <= k_stride, "need 1 <= r <= min(gt width, k_stride)");
+    NBPG_CHECK_ARG(!use_raw || idx->d_raw, "no raw rows on this index");
+    *correct = 0;
+    if (nq == 0) return NBPG_OK;
+    for (uint64_t i = 0; i < uint64_t(nq) * gk; ++i) NBPG_CHECK_ARG(gt[i] < idx->desc.n, "ground-truth id out of range");
+    std::lock_guard<std::mutex> g(idx->mu);
+    NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
+    const uint32_t dtype = use_raw ? idx->raw_dtype : idx->desc.dtype;
+    const uint32_t dims = use_raw ? idx->raw_dims : idx->desc.dims;
+    const uint32_t qrow = use_raw ? idx->raw_row_bytes : idx->row_bytes;
+    DevBuf w;
+    const size_t qb = size_t(nq) * qrow, ib = size_t(nq) * k_stride * 4, gb = size_t(nq) * gk * 4;
+    nbpg_status s = w.ensure(qb + ib + gb + size_t(nq) * 4 + 1024);
+    if (s != NBPG_OK) return s;
+    uint8_t *p = static_cast<uint8_t *>(w.ptr);
+    auto take = [&](size_t b) { uint8_t *r0 = p; p += (b + 255) / 256 * 256; return r0; };
+    uint8_t *dq = take(qb);
+    uint32_t *di = reinterpret_cast<uint32_t *>(take(ib)), *dg = reinterpret_cast<uint32_t *>(take(gb));
+    uint32_t *dc = reinterpret_cast<uint32_t *>(take(size_t(nq) * 4));
+    unsigned long long *dcor = reinterpret_cast<unsigned long long *>(take(8));
+    NBPG_CUDA_TRY(cudaMemcpy(dq, queries, qb, cudaMemcpyHostToDevice));
+    NBPG_CUDA_TRY(cudaMemcpy(di, ids, ib, cudaMemcpyHostToDevice));
+    NBPG_CUDA_TRY(cudaMemcpy(dg, gt, gb, cudaMemcpyHostToDevice));
+    NBPG_CUDA_TRY(cudaMemcpy(dc, count, size_t(nq) * 4, cudaMemcpyHostToDevice));
+    NBPG_CUDA_TRY(cudaMemset(dcor, 0, 8));
+    EvalArgs a{use_raw ? idx->d_raw : idx->d_points, use_raw ? idx->raw_row_bytes : idx->row_stride, dims, dq, qrow,
+               di, dc, dg, k_stride, gk, nq, r, dcor};
+    const int metric = int(idx->desc.metric);
+    switch (dtype) {
+    case NBPG_U8: launch_recall<DT_U8>(metric, a); break;
+    case NBPG_I8: launch_recall<DT_I8>(metric, a); break;
+    case NBPG_U4:
+    case NBPG_I4: launch_recall<DT_U4>(metric, a); break;
+    default: launch_recall<DT_F32>(metric, a);
+    }
+    NBPG_CUDA_TRY(cudaGetLastError());
+    unsigned long long c = 0;
+    NBPG_CUDA_TRY(cudaMemcpy(&c, dcor, 8, cudaMemcpyDeviceToHost));
+    *correct = c;
+    return NBPG_OK;
+}
+

@@ -159,6 +159,19 @@ class Index:
                                             _p(cmps)))
         return SearchResult(ids, ds, cnt, vis, cmps)
 
+    def eval_recall(self, queries: np.ndarray, result: SearchResult, gt: np.ndarray, r: int,
+                    raw: bool = False) -> float:
+        """calRecall (check_nn_recall.h:84-167) on the device: tie-extended recall@r of a search
+        result against ground-truth ids, distances from the raw rows (raw=True) or the quantised rows."""
+        q = np.ascontiguousarray(queries)
+        gt = np.ascontiguousarray(gt, dtype=np.uint32)
+        ids = np.ascontiguousarray(result.ids, dtype=np.uint32)
+        cnt = np.ascontiguousarray(result.count, dtype=np.uint32)
+        out = C.c_uint64(0)
+        check(_lib.lib().nbpg_eval_recall(self._h, int(raw), q.ctypes.data, q.shape[0], _p(ids), _p(cnt), ids.shape[1],
+                                          _p(gt), gt.shape[1], r, C.byref(out)))
+        return float(np.float32(out.value) / np.float32(r * q.shape[0]))
+
     def qsearch_all(self, queries: np.ndarray, qp: QueryParams, start_points=(0,)) -> list[np.ndarray]:
         """qsearchAll: list of neighbour-id arrays, one per query."""
         r = self.search(queries, qp, start_points)
