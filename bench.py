@@ -173,6 +173,74 @@ def time_gt_device(base, q, k, local, reps=3):
     return out
 
 
+def time_next_rows(idx, base, q, gi, L_op, k, local, reps=5):
+    """The rows after the search: PCA encode on the device (1M x 128 float rows -> PCA-64
+    4-bit codes, the 4-bit configuration's encode), re-ranking with raw float rows at the
+    operating point (both modes), and the device recall of the operating point's results."""
+    import torch
+    from nbpg_gb300 import _lib
+    from nbpg_gb300.index import QueryParams
+    from nbpg_gb300.pca import fit
+    out = {}
+    dev = torch.device("cuda", local)
+    # PCA encode: float rows = the u8 rows as floats plus a small seeded perturbation
+    r = np.random.default_rng(12)
+    xf = base.astype(np.float32) + r.normal(size=base.shape).astype(np.float32) * 0.25
+    mat, bias = fit(xf[:200000], 64)
+    dx = torch.from_numpy(xf).to(dev)
+    dm, db = torch.from_numpy(mat).to(dev), torch.from_numpy(bias).to(dev)
+    dy = torch.empty((len(xf), 32), dtype=torch.uint8, device=dev)
+    st = torch.cuda.Stream(device=dev)
+    lib = _lib.lib()
+
+    def enc():
+        _lib.check(lib.nbpg_pca_encode_device(_lib.DTYPES["f32"], dx.data_ptr(), len(xf), xf.shape[1], dm.data_ptr(),
+                                              db.data_ptr(), 64, _lib.DTYPES["u4"], dy.data_ptr(), st.cuda_stream))
+    enc()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        enc()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    peak, _ = measured_peaks()
+    nbytes = xf.nbytes + len(xf) * 32
+    out["pca_encode"] = {"rows": len(xf), "d_in": int(xf.shape[1]), "d_out": 64, "out": "u4 (32 B/row)", "ms": ms,
+                         "rows_per_s": len(xf) / (ms * 1e-3), "hbm_gbs": nbytes / (ms * 1e-3) / 1e9,
+                         "frac_of_hbm": nbytes / (ms * 1e-3) / 1e9 / peak,
+                         "fp32_tflops": 2.0 * len(xf) * xf.shape[1] * 64 / (ms * 1e-3) / 1e12,
+                         "note": "index-order fp32 sums with separately rounded products (bit-exact codes): "
+                                 "bound by instruction issue and latency of the dependent sums, not HBM"}
+    del dx, dy
+    # re-ranking with raw float rows (Base_Points beside the u8 Q_Base_Points)
+    qf = q.astype(np.float32)
+    idx.set_raw_points(xf)
+    qp = QueryParams(k=k, beamSize=L_op, cut=CFG["cut"])
+    rr = {}
+    for name, rf in (("rerank_factor_100", 100), ("filtering_mode", 0)):
+        idx.search_rerank(q, qf, qp, rf)
+        t = time.perf_counter()
+        for _ in range(reps):
+            res = idx.search_rerank(q, qf, qp, rf)
+        sec = (time.perf_counter() - t) / reps
+        rr[name] = {"qps_host_api": len(q) / sec, "recall@10_vs_u8_gt": recall_of(res.ids, gi, k)}
+    out["rerank"] = dict(rr, L=L_op, raw="float32 x 128 (u8 rows as floats + N(0, 0.25^2))",
+                         note="host API, query copies included; exact distances of min(k * rerank_factor, L) "
+                              "frontier entries, or of the visited list in filtering mode")
+    # device recall of the operating point's results
+    res = idx.search(q, qp)
+    t = time.perf_counter()
+    rec = idx.eval_recall(q, res, gi, k)
+    out["eval_recall"] = {"ms_host_api": (time.perf_counter() - t) * 1e3, "recall@10": rec}
+    return out
+
+
+def recall_of(ids, gi, k):
+    return float(np.mean([len(set(a[:k].tolist()) & set(b[:k].tolist())) / k for a, b in zip(ids, gi)]))
+
+
 def traffic_per_query():
     p = os.path.join(ROOT, "profiles", "search_traffic.json")
     if os.path.exists(p):
@@ -500,6 +568,12 @@ def main():
     h2d = nq * CFG["dim"]
     d2h = nq * k * 8 + nq * 12 + 4
 
+    next_rows = time_next_rows(idx, base, q, gi, L_op, k, local) if rank == 0 else None
+    if next_rows:
+        log(f"[bench] PCA encode {next_rows['pca_encode']['ms']:.2f} ms per 1M rows; re-rank "
+            f"{next_rows['rerank']['rerank_factor_100']['qps_host_api']:.3g} QPS; device recall "
+            f"{next_rows['eval_recall']['recall@10']:.4f}")
+
     # serving: continuous batching with Poisson arrivals (requests admitted as batch slots
     # and working-set budget free up); latency from each request's arrival to completion
     serving = None
@@ -579,7 +653,7 @@ def main():
             "latency_ms": None if not serving else {"p50": serving["at_half_peak"]["p50_ms"],
                                                      "p99": serving["at_half_peak"]["p99_ms"],
                                                      "at_offered_qps": serving["at_half_peak"]["offered_qps"]},
-            "serving": serving, "ground_truth": gt_dev}
+            "serving": serving, "ground_truth": gt_dev, "next_rows": next_rows}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
