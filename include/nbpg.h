@@ -345,6 +345,16 @@ typedef struct nbpg_build_stats {
 nbpg_status nbpg_build(nbpg_index *idx, const nbpg_build_params *params, nbpg_build_stats *stats,
                        uint32_t *per_node_visited, uint32_t *per_node_dists);
 
+/* The FGIM build (data_tools/ANNs/FGIM/FGIM.cpp:157-265 with FIGM_NSWIndex, FGIM_nsw.h:12-175):
+ * with num_split > 1 two split passes on the index's graph G; then every pass but the last
+ * is pair_batch_insert, which searches G (start points 0 .. num_split-1 for every insert) and
+ * writes a second graph toG, with candidates = the node's neighbours in G plus the search's
+ * frontier; the last pass is batch_insert on toG; toG (after repair) becomes the index's
+ * graph.  Same parameters as nbpg_build (sp_seed unused: FGIM draws no random start points);
+ * num_split >= 1. */
+nbpg_status nbpg_build_fgim(nbpg_index *idx, const nbpg_build_params *params, nbpg_build_stats *stats,
+                            uint32_t *per_node_visited, uint32_t *per_node_dists);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,6 +122,7 @@ def lib() -> C.CDLL:
     L.nbpg_u8_to_u4.argtypes = [_vp, C.c_uint64, C.c_uint32, _vp, C.c_int32]
     L.nbpg_f32_to_u8.argtypes = [_f32p, C.c_uint64, C.c_uint32, _vp, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
+    L.nbpg_build_fgim.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
     _lib = L
     return L
 

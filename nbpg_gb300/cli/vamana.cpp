@@ -1,5 +1,7 @@
 // nbpg_vamana: drop-in for the reference's Vamana driver (data_tools/ANNs/Vamana.cpp) over
-// the C ABI.  Same flags (BuildArgs Vamana.cpp:14-85, QueryArgs :88-125), same files:
+// the C ABI; compiled with NBPG_FGIM it is nbpg_fgim, the drop-in for the FGIM driver
+// (data_tools/ANNs/FGIM/FGIM.cpp), whose flags are Vamana's without --min/--max_cos_angle
+// and whose build is nbpg_build_fgim.  Same flags (BuildArgs Vamana.cpp:14-85, QueryArgs :88-125), same files:
 // the index is <index_path>.graph (graph.h:339-379 layout), loaded instead of rebuilt
 // unless --rebuild (Vamana.cpp:165-169), continued from --pre_index_path (:174-177).
 // Query evaluation follows search_and_parse (check_nn_recall.h:187-359): a fixed --Q runs
@@ -146,8 +148,10 @@ int main(int argc, char **argv)
     f.flag("--rand_sp", a.rand_sp);
     f.opt("--max_alpha", a.max_alpha);
     f.opt("--min_alpha", a.min_alpha);
+#ifndef NBPG_FGIM
     f.opt("--max_cos_angle", a.max_cos);
     f.opt("--min_cos_angle", a.min_cos);
+#endif
     f.flag("--cache_raw", a.cache_raw);
     f.opt("--base_path", a.base_path);
     f.opt("--query_path", a.query_path);
@@ -159,7 +163,9 @@ int main(int argc, char **argv)
     f.opt("--Q", a.Q);
     f.opt("--rerank_factor", a.rerank_factor);
     f.opt("--q_num", a.q_num);
+#ifndef NBPG_FGIM
     f.opt("--sp_seed", a.sp_seed);
+#endif
     if (!f.parse(argc, argv)) return 106;
 
     uint32_t dtype;
@@ -193,7 +199,11 @@ int main(int argc, char **argv)
         nbpg_build_params bp{a.L, a.VL, a.top_degree, a.num_split, a.num_passes, a.limit, a.dir_bias_scale,
                              a.min_alpha, a.max_alpha, a.min_cos, a.max_cos, a.dynamic_prune, a.rand_sp, 1, a.sp_seed};
         nbpg_build_stats st{};
+#ifdef NBPG_FGIM
+        check(nbpg_build_fgim(idx, &bp, &st, nullptr, nullptr));  // FGIM.cpp:157-265
+#else
         check(nbpg_build(idx, &bp, &st, nullptr, nullptr));
+#endif
         check(nbpg_index_get_graph(idx, G.data(), 0, n));
         nbpg_index_destroy(idx);
         build_s = st.seconds;

@@ -135,7 +135,7 @@ struct DevArr {
 };
 
 static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_build_stats *stats, uint32_t *out_sv,
-                              uint32_t *out_sd)
+                              uint32_t *out_sd, bool fgim = false)
 {
     const auto t_start = std::chrono::steady_clock::now();
     const uint64_t n = idx->desc.n;
@@ -146,6 +146,8 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     NBPG_CHECK_ARG(P.top_degree <= R, "top_degree above R");
     NBPG_CHECK_ARG(P.num_split <= L && P.num_split <= 256, "num_split start points exceed L");
     NBPG_CHECK_ARG(n >= 1 && n < 0xFFFFFFFFull, "bad n");
+    NBPG_CHECK_ARG(!fgim || P.num_split >= 1, "the FGIM build needs num_split >= 1 (with none, the reference's "
+                                              "pair pass reads a stale visited list)");
     if (P.dir_bias_scale > 0) {
         set_error("dir_bias_scale > 0 is not supported by the GPU build");
         return NBPG_ERR_UNSUPPORTED;
@@ -241,8 +243,21 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     std::mt19937 sp_engine{uint32_t(P.sp_seed)};
     uint64_t batches = 0;
 
-    // one pass of batch_insert over `inserts` with nsp start points per insert
-    auto run_pass = [&](uint32_t nsp, Popular mode) -> nbpg_status {
+    // FGIM: the graph the pair passes write (toG), which becomes the index's graph
+    DevBuf d_tog;
+    uint32_t *tog = nullptr;
+    if (fgim) {
+        if ((s = d_tog.ensure(size_t(n) * idx->gstride * 4)) != NBPG_OK) return s;
+        tog = d_tog.as<uint32_t>();
+        NBPG_CUDA_TRY(cudaMemsetAsync(tog, 0, size_t(n) * idx->gstride * 4, st));
+    }
+
+    // one pass of batch_insert over `inserts` with nsp start points per insert; `sg` is the
+    // graph searched, `wg` the graph written (the same except in FGIM's pair passes, which
+    // run pair_batch_insert's searchNghAndPrune and finish popularity without propagation)
+    auto run_pass = [&](uint32_t nsp, Popular mode, uint32_t *sg, uint32_t *wg, bool pair) -> nbpg_status {
+        B.s.graph = sg;
+        B.pair = pair ? 1u : 0u;
         NBPG_CUDA_TRY(cudaMemcpyAsync(d_inserts.ptr, inserts.data(), n * 4, cudaMemcpyHostToDevice, st));
         NBPG_CUDA_TRY(cudaMemcpyAsync(d_sp.ptr, sp_host.data(), n * nsp * 4, cudaMemcpyHostToDevice, st));
         B.nsp_per = nsp;
@@ -294,25 +309,36 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
             NBPG_CUDA_TRY(cudaMemsetAsync(d_bump.ptr, 0, 16, st));
             const uint32_t g1 = std::min<uint32_t>(full_grid, (bs + W - 1) / W);
             kt.search(g1, W * 32, smem_search, B, st);
-            forward_write_kernel<<<bs, 64, 0, st>>>(B);
+            BuildArgs Wr = B;
+            Wr.s.graph = wg;
+            forward_write_kernel<<<bs, 64, 0, st>>>(Wr);
             const uint32_t ne = bs * R;
             const uint32_t eg = (ne + 255) / 256;
             rev_count_kernel<<<eg, 256, 0, st>>>(B);
             rev_alloc_kernel<<<eg, 256, 0, st>>>(B);
             rev_scatter_kernel<<<eg, 256, 0, st>>>(B);
-            BuildArgs M = B;
+            BuildArgs M = Wr;
             M.queue = d_queue.as<uint32_t>() + 1;
             const uint32_t gm = std::min<uint32_t>(uint32_t(idx->sm_count) * 8, (ne + MW - 1) / MW);
             kt.merge(gm, MW * 32, smem_merge, M, st);
             NBPG_CUDA_TRY(cudaGetLastError());
         }
         NBPG_CUDA_TRY(cudaStreamSynchronize(st));
-        if (mode == Popular::Cal) {
+        if (mode == Popular::Cal && pair) {
+            // FGIM_nsw.h:164-172: log(x + 1) of the visit counts, min/max, no propagation
+            popular.resize(n);
+            NBPG_CUDA_TRY(cudaMemcpyAsync(popular.data(), d_pop.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+            NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+            for (uint64_t i = 0; i < n; ++i) popular[i] = float(std::log(double(popular[i] + 1.0f)));
+            auto mm = std::minmax_element(popular.begin(), popular.end());
+            min_pop = *mm.first;
+            max_pop = *mm.second;
+        } else if (mode == Popular::Cal) {
             // nsw.h:255-278: one-hop propagation in node order, log(x + 1), min/max
             std::vector<float> pop(n);
             std::vector<uint32_t> G(size_t(n) * (R + 1));
             NBPG_CUDA_TRY(cudaMemcpyAsync(pop.data(), d_pop.ptr, n * 4, cudaMemcpyDeviceToHost, st));
-            NBPG_CUDA_TRY(cudaMemcpy2DAsync(G.data(), (R + 1) * 4, idx->d_graph, idx->gstride * 4, (R + 1) * 4, n,
+            NBPG_CUDA_TRY(cudaMemcpy2DAsync(G.data(), (R + 1) * 4, wg, idx->gstride * 4, (R + 1) * 4, n,
                                             cudaMemcpyDeviceToHost, st));
             NBPG_CUDA_TRY(cudaStreamSynchronize(st));
             std::vector<float> tmp(n, 0.0f);
@@ -332,12 +358,14 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
 
     Popular mode = Popular::FixedMax;
     const uint32_t ns = P.num_split;
-    if (ns >= 1) {
+    uint32_t *G0 = idx->d_graph;
+    // split stage (nsw.h:562-575; FGIM.cpp:201-220 runs it only for num_split > 1)
+    if (fgim ? ns > 1 : ns >= 1) {
         for (int i = 0; i < 2; ++i) {
             std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
             sp_host.resize(n);
             for (uint64_t j = 0; j < n; ++j) sp_host[j] = inserts[j] % ns;
-            if ((s = run_pass(1, mode)) != NBPG_OK) return s;
+            if ((s = run_pass(1, mode, G0, G0, false)) != NBPG_OK) return s;
         }
     }
     for (int i = 0; i < int(P.num_passes); ++i) {
@@ -345,8 +373,18 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
         if (i == int(P.num_passes) - 2 && P.dynamic_prune) mode = Popular::Cal;
         else if (i == int(P.num_passes) - 1)
             mode = (P.dynamic_prune && P.num_passes > 1) ? Popular::Prune : Popular::FixedMin;
+        else if (fgim) mode = Popular::FixedMax;
+        const bool last = i == int(P.num_passes) - 1;
+        if (fgim && !last) {
+            // FGIM.cpp:244-249: pair pass on (G -> toG) with start points 0 .. num_split-1
+            sp_host.resize(size_t(n) * ns);
+            for (uint64_t j = 0; j < n; ++j)
+                for (uint32_t k = 0; k < ns; ++k) sp_host[j * ns + k] = k;
+            if ((s = run_pass(ns, mode, G0, tog, true)) != NBPG_OK) return s;
+            continue;
+        }
         uint32_t nsp = 1;
-        if (i != int(P.num_passes) - 1 && ns > 1) {
+        if (!last && ns > 1) {
             nsp = ns;
             sp_host.resize(n * ns);
             std::uniform_int_distribution<uint32_t> u(0, uint32_t(n) - 1);
@@ -357,13 +395,20 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
                     if (v >= n) v -= ns;
                     sp_host[j * ns + k] = v;
                 }
-        } else if (i == int(P.num_passes) - 1 && P.rand_sp) {
+        } else if (last && P.rand_sp) {
             sp_host.resize(n);
             for (uint64_t j = 0; j < n; ++j) sp_host[j] = uint32_t(n - inserts[j] - 1);
         } else {
             sp_host.assign(n, 0u);
         }
-        if ((s = run_pass(nsp, mode)) != NBPG_OK) return s;
+        uint32_t *g = fgim ? tog : G0;  // FGIM's last pass is batch_insert on toG
+        if ((s = run_pass(nsp, mode, g, g, false)) != NBPG_OK) return s;
+    }
+    if (fgim) {
+        // toG is the FGIM result (FGIM.cpp:259-263)
+        NBPG_CUDA_TRY(cudaMemcpyAsync(idx->d_graph, tog, size_t(n) * idx->gstride * 4, cudaMemcpyDeviceToDevice, st));
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+        d_tog.release();
     }
 
     uint64_t iso = 0;
@@ -402,4 +447,13 @@ extern "C" nbpg_status nbpg_build(nbpg_index *idx, const nbpg_build_params *para
     std::lock_guard<std::mutex> g(idx->mu);
     cudaSetDevice(idx->desc.device);
     return build_impl(idx, *params, stats, per_node_visited, per_node_dists);
+}
+
+extern "C" nbpg_status nbpg_build_fgim(nbpg_index *idx, const nbpg_build_params *params, nbpg_build_stats *stats,
+                                       uint32_t *per_node_visited, uint32_t *per_node_dists)
+{
+    if (!idx || !params) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(idx->mu);
+    cudaSetDevice(idx->desc.device);
+    return build_impl(idx, *params, stats, per_node_visited, per_node_dists, true);
 }

@@ -43,6 +43,7 @@ struct BuildArgs {
     uint32_t *bump;        // [0] allocator, [1] group count
     uint32_t *grp_target;  // groups
     uint64_t *edges;       // grouped (dist, source) keys
+    uint32_t pair;         // FGIM pair pass (FGIM_nsw.h:45-109) instead of searchNghAndPrune
 };
 
 constexpr double kPruneEps = 1e-5;  // kEpsilon, prune.h:212
@@ -70,12 +71,17 @@ __device__ __forceinline__ void load_row_regs(const SearchArgs &a, uint32_t id, 
 }
 
 template <int DT, int MET, int VPL>
+__device__ void prune_and_emit(const BuildArgs &B, uint32_t t, uint32_t index, uint64_t *pool, uint32_t np,
+                               uint8_t *alive, uint32_t search_cmps, uint32_t nvis, const uint64_t *vis, uint32_t vs,
+                               int lane);
+
+template <int DT, int MET, int VPL>
 __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t gslot, int lane)
 {
     const SearchArgs &a = B.s;
     const SlotLayout &lay = a.lay;
     const uint32_t index = B.inserts[t];
-    const uint32_t R = B.R, VL = B.VL;
+    const uint32_t VL = B.VL;
     const uint8_t *prow = a.base + size_t(index) * a.row_stride;
 
     // beam search from the start points (beam_search with k = 0, cut = 0)
@@ -137,6 +143,78 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
     np = __shfl_sync(kFull, np, 0);
     __syncwarp();
 
+    prune_and_emit<DT, MET, VPL>(B, t, index, pool, np, alive, st.cmps + rp, uint32_t(st.nvis), st.vis, st.vs, lane);
+}
+
+// FGIM pair pass for one insert (FIGM_NSWIndex::pair_batch_insert's searchNghAndPrune,
+// FGIM_nsw.h:45-109): candidates are all neighbours of the node in the searched graph (with
+// their distances, not counted) and the frontier of a search from the nsp start points,
+// taken once per start point as the reference's loop repeats the same search (its counters
+// too); the sorted candidates go through std::unique with the order predicate
+// a.index < b.index, so an entry stays only when its id is not above the last kept id
+// (equal ids stay); the first VL are kept, then sort_candidates and RobustPrune.
+template <int DT, int MET, int VPL>
+__device__ void fgim_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t gslot, int lane)
+{
+    const SearchArgs &a = B.s;
+    const SlotLayout &lay = a.lay;
+    const uint32_t index = B.inserts[t];
+    const uint32_t VL = B.VL, ns = B.nsp_per;
+    const uint8_t *prow = a.base + size_t(index) * a.row_stride;
+    const SearchState st = search_core<DT, MET, true, VPL>(a, prow, B.L, 0, VL, B.sp + size_t(t) * ns, ns, slot,
+                                                      gslot, lane, index);
+    const uint64_t *fr = st.frontier();
+    uint64_t *nk = st.b ? st.fr0 : st.fr1;  // the other frontier buffer: neighbour keys
+    uint32_t *filt = reinterpret_cast<uint32_t *>(slot + lay.off_filt);
+    uint64_t *pool = reinterpret_cast<uint64_t *>(st.H);  // the visited filter is free after the search
+    uint8_t *alive = slot + lay.off_fl0;
+
+    const uint32_t *grow = a.graph + size_t(index) * a.gstride;
+    const uint32_t deg = __ldg(grow);
+    for (uint32_t i = lane; i < deg; i += 32) filt[i] = __ldg(grow + 1 + i);
+    __syncwarp();
+    uint4 qv[VPL];
+    load_row_regs<VPL>(a, index, qv, lane);
+    warp_row_keys<DT, MET, VPL>(a, qv, filt, deg, nk, lane);
+    sort_keys(nk, deg, lane);
+
+    // merge (neighbours, frontier x ns) in key order through the unique filter, first VL kept
+    uint32_t np = 0;
+    if (lane == 0) {
+        uint32_t i = 0, j = 0, rep = 0, last = 0;
+        const uint32_t fs = ns ? st.fs : 0u;
+        while ((i < deg || j < fs) && np < VL) {
+            uint64_t e;
+            if (j >= fs || (i < deg && nk[i] <= fr[j])) {
+                e = nk[i++];
+            } else {
+                e = fr[j];
+                if (++rep == ns) { rep = 0; ++j; }
+            }
+            if (np == 0 || !(last < key_id(e))) {
+                pool[np++] = e;
+                last = key_id(e);
+            }
+        }
+    }
+    np = __shfl_sync(kFull, np, 0);
+    __syncwarp();
+    prune_and_emit<DT, MET, VPL>(B, t, index, pool, np, alive, ns * st.cmps, ns * uint32_t(st.nvis), st.vis,
+                                 ns ? st.vs : 0u, lane);
+}
+
+// sort_candidates (prune.h:50-74) on pool[0, np), RobustPrune (limitedSimilarityPrune,
+// prune.h:159-209) with the node's alpha / cos, and the outputs of one insert: the pruned
+// list, the BuildStats counters (search_cmps + the prune's distances, nvis) and, in a
+// popularity pass, one visit per entry of the visited list vis[0, vs).
+template <int DT, int MET, int VPL>
+__device__ void prune_and_emit(const BuildArgs &B, uint32_t t, uint32_t index, uint64_t *pool, uint32_t np,
+                               uint8_t *alive, uint32_t search_cmps, uint32_t nvis, const uint64_t *vis, uint32_t vs,
+                               int lane)
+{
+    const SearchArgs &a = B.s;
+    const uint32_t R = B.R;
+    uint32_t rp = 0;
     // sort_candidates (prune.h:50-74): p forced last, sort, drop repeats, drop p
     const uint64_t pkey = (uint64_t(f2ord(3.402823466e38f)) << 32) | index;
     for (uint32_t i = lane; i < np; i += 32)
@@ -236,11 +314,11 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
     }
     if (lane == 0) {
         B.res_cnt[t] = sel;
-        if (B.stat_dist) B.stat_dist[index] += st.cmps + rp;
-        if (B.stat_vis) B.stat_vis[index] += uint32_t(st.nvis);
+        if (B.stat_dist) B.stat_dist[index] += search_cmps + rp;
+        if (B.stat_vis) B.stat_vis[index] += nvis;
     }
     if (B.popular)
-        for (uint32_t i = lane; i < st.vs; i += 32) atomicAdd(&B.popular[key_id(st.vis[i])], 1.0f);
+        for (uint32_t i = lane; i < vs; i += 32) atomicAdd(&B.popular[key_id(vis[i])], 1.0f);
     __syncwarp();
 }
 
@@ -256,7 +334,8 @@ __global__ void __launch_bounds__(512) build_search_prune_kernel(BuildArgs B)
         if (lane == 0) w = atomicAdd(B.queue, 1u);
         w = __shfl_sync(kFull, w, 0);
         if (w >= B.bs) break;
-        build_one<DT, MET, VPL>(B, w, slot, gslot, lane);
+        if (B.pair) fgim_one<DT, MET, VPL>(B, w, slot, gslot, lane);
+        else build_one<DT, MET, VPL>(B, w, slot, gslot, lane);
     }
 }
 

@@ -226,6 +226,19 @@ class Index:
         check(_lib.lib().nbpg_build(self._h, C.byref(prm), C.byref(st), _p(sv), _p(sd)))
         return st, sv, sd
 
+    def build_fgim(self, L: int = 70, VL: int = 140, top_degree: int = 0, num_split: int = 4, num_passes: int = 2,
+                   limit: int = 0, min_alpha: float = 1.0, max_alpha: float = 1.1, dynamic_prune: bool = False,
+                   rand_sp: bool = False, repair_isolate: bool = True, with_stats: bool = False):
+        """The FGIM build (FGIM.cpp:157-265): pair passes searching the current graph and writing a
+        second one, then batch_insert on that graph, which becomes the index's graph."""
+        prm = BuildParams(L, VL, top_degree, num_split, num_passes, limit, 0.0, min_alpha, max_alpha, 0.0, 0.0,
+                          int(dynamic_prune), int(rand_sp), int(repair_isolate), 0)
+        st = BuildStats()
+        sv = np.zeros(self.n, np.uint32) if with_stats else None
+        sd = np.zeros(self.n, np.uint32) if with_stats else None
+        check(_lib.lib().nbpg_build_fgim(self._h, C.byref(prm), C.byref(st), _p(sv), _p(sd)))
+        return st, sv, sd
+
 
 class SearchGraph:
     """A captured search request; launch() replays it on a stream."""

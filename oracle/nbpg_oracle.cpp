@@ -329,7 +329,8 @@ struct BuildCfg {
 
 struct Builder {
     BuildCfg cfg;
-    std::vector<uint32_t> &G;  // n*(R+1)
+    std::vector<uint32_t> &G;  // n*(R+1): the graph searched
+    std::vector<uint32_t> *T = nullptr;  // FGIM pair passes: the graph written (toG), else G
     std::vector<float> popular;
     float min_pop = 0.f, max_pop = 1.f;
     std::vector<uint32_t> stat_visited, stat_dist;
@@ -348,6 +349,7 @@ struct Builder {
     const uint8_t *pt(uint32_t v) const { return cfg.base + size_t(v) * cfg.row; }
     float dist(uint32_t a, uint32_t b) const { return dist_rows(cfg.dtype, cfg.metric, pt(a), pt(b), cfg.dims); }
     uint32_t *row(uint32_t v) { return &G[size_t(v) * (cfg.R + 1)]; }
+    uint32_t *row_out(uint32_t v) { return T ? &(*T)[size_t(v) * (cfg.R + 1)] : row(v); }
 
     std::pair<float, float> alpha_cos(uint32_t v, Popular mode) const
     {
@@ -400,6 +402,43 @@ struct Builder {
         res.vis.assign(c.visited.begin(), c.visited.begin() + c.vs);
     }
 
+    // FIGM_NSWIndex::pair_batch_insert's searchNghAndPrune (FGIM_nsw.h:45-109): candidates are
+    // the node's neighbours in the searched graph (all of them) plus the frontier of a search
+    // from the sp start points, repeated once per start point as the reference's loop does;
+    // sorted, then std::unique with the order predicate a.index < b.index (an element stays
+    // when its id is not above the last kept one's), cut to VL, sort_candidates, RobustPrune.
+    void search_and_prune_pair(Cell &c, uint32_t index, const std::vector<uint32_t> &sps, Popular mode,
+                               const std::vector<uint32_t> &degrees, Result &res)
+    {
+        auto [alpha, cos_angle] = alpha_cos(index, mode);
+        GraphView gv{G.data(), cfg.R};
+        auto dist_to = [&](uint32_t a) { return dist(a, index); };
+        std::vector<Node> cand;
+        const uint32_t deg = gv.degree(index);
+        for (uint32_t i = 0; i < deg; ++i) cand.push_back(Node{gv.nbr(index, i), dist(gv.nbr(index, i), index)});
+        for (size_t rep = 0; rep < sps.size(); ++rep) {
+            c.reset(cfg.L, cfg.VL, cfg.R);
+            seed_frontier(c, sps.data(), uint32_t(sps.size()), dist_to);
+            size_t cmps = beam_search(c, gv, dist_to, int64_t(index), 0, 0.0, cfg.limit, cfg.R);
+            stat_dist[index] += uint32_t(cmps);
+            stat_visited[index] += uint32_t(c.num_visited);
+            for (size_t j = 0; j < c.fs; ++j) cand.push_back(c.frontier[j]);
+        }
+        std::sort(cand.begin(), cand.end(), node_less);
+        size_t kept = 0;
+        for (size_t i = 0; i < cand.size(); ++i)
+            if (kept == 0 || !(cand[kept - 1].id < cand[i].id)) cand[kept++] = cand[i];
+        if (kept > cfg.VL) kept = cfg.VL;
+        std::copy(cand.begin(), cand.begin() + kept, c.pool.begin());
+        size_t np = kept;
+        sort_candidates(index, degrees.data(), bias.empty() ? nullptr : bias.data(), c.pool.data(), np);
+        size_t rp = robust_prune(index, c.pool.data(), np, cfg.R, double(alpha), double(cos_angle),
+                                 [&](uint32_t a, uint32_t b) { return dist(a, b); });
+        stat_dist[index] += uint32_t(rp);
+        res.prune.assign(c.pool.begin(), c.pool.begin() + np);
+        res.vis.assign(c.visited.begin(), c.visited.begin() + (sps.empty() ? 0 : c.vs));
+    }
+
     // nsw.h:329-355
     size_t fill_new_dists(uint32_t index, Node *c, size_t pre, size_t n) const
     {
@@ -423,7 +462,7 @@ struct Builder {
 
     void batch_insert(const std::vector<uint32_t> &inserts,
                       const std::function<void(std::vector<std::vector<uint32_t>> &, size_t, size_t)> &fill_sp,
-                      Popular mode, int threads)
+                      Popular mode, int threads, bool pair = false)
     {
         const uint64_t n = cfg.n;
         size_t eff = std::min<size_t>(size_t(0.02 * double(float(n))), 1000000ul);
@@ -455,7 +494,10 @@ struct Builder {
 
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 8)
             for (long long i = 0; i < (long long)bs; ++i)
-                search_and_prune(cells[omp_get_thread_num()], inserts[floor + i], sp[i], mode, degrees, res[i]);
+                if (pair)
+                    search_and_prune_pair(cells[omp_get_thread_num()], inserts[floor + i], sp[i], mode, degrees, res[i]);
+                else
+                    search_and_prune(cells[omp_get_thread_num()], inserts[floor + i], sp[i], mode, degrees, res[i]);
 
             if (mode == Popular::Cal)
                 for (size_t i = 0; i < bs; ++i)
@@ -463,7 +505,7 @@ struct Builder {
 
             // forward lists (nsw.h:416-429)
             for (size_t i = 0; i < bs; ++i) {
-                uint32_t *r = row(inserts[floor + i]);
+                uint32_t *r = row_out(inserts[floor + i]);
                 r[0] = uint32_t(res[i].prune.size());
                 for (size_t j = 0; j < res[i].prune.size(); ++j) r[1 + j] = res[i].prune[j].id;
             }
@@ -492,7 +534,7 @@ struct Builder {
                 size_t cs = 0;
                 for (size_t j = b; j < e; ++j) cand[cs++] = edges[j].src;
                 size_t pre = cs;
-                uint32_t *r = row(t);
+                uint32_t *r = row_out(t);
                 for (uint32_t i = 0; i < r[0]; ++i) {
                     uint32_t nb = r[1 + i];
                     bool dup = false;
@@ -515,7 +557,13 @@ struct Builder {
             ++inc;
         }
 
-        if (mode == Popular::Cal) {
+        if (mode == Popular::Cal && pair) {
+            // FGIM_nsw.h:164-172: log(x+1) of the visit counts, no propagation
+            for (uint64_t i = 0; i < n; ++i) popular[i] = float(std::log(double(popular[i] + 1.0f)));
+            auto mm = std::minmax_element(popular.begin(), popular.end());
+            min_pop = *mm.first;
+            max_pop = *mm.second;
+        } else if (mode == Popular::Cal) {
             // nsw.h:255-278 — one-hop propagation in node order, then log(x+1)
             std::vector<float> tmp(n, 0.0f);
             for (uint64_t i = 0; i < n; ++i) {
@@ -820,6 +868,80 @@ int nbpg_oracle_build(int dtype, int metric, uint32_t dims, const void *base, ui
     size_t iso = 0;
     if (repair_isolate) iso = repair_isolated(G, R, n, 0);
     std::copy(G.begin(), G.end(), graph);
+    if (out_stat_visited) std::copy(b.stat_visited.begin(), b.stat_visited.end(), out_stat_visited);
+    if (out_stat_dist) std::copy(b.stat_dist.begin(), b.stat_dist.end(), out_stat_dist);
+    if (out_isolated) *out_isolated = iso;
+    return 0;
+}
+
+// The FGIM build (data_tools/ANNs/FGIM/FGIM.cpp:157-265 with FGIM_nsw.h): with num_split > 1,
+// two split passes of batch_insert on G (start point id % num_split); then num_passes passes
+// over shuffled inserts: every pass but the last is pair_batch_insert searching G and writing
+// toG, with start points 0..num_split-1 for every insert; the last pass is batch_insert on toG
+// (start point 0, or n - id - 1 with rand_sp); popularity as in the Vamana build, except that
+// the pair pass's visit counts are not propagated; then repair on toG.  toG is the result.
+// num_split must be >= 1 (with none, the reference's pair pass reads a stale visited list).
+int nbpg_oracle_build_fgim(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t R, uint32_t L,
+                           uint32_t VL, uint32_t top_degree, uint32_t num_split, uint32_t num_passes, uint64_t limit,
+                           double min_alpha, double max_alpha, double min_cos, double max_cos, int dynamic_prune,
+                           int rand_sp, int repair_isolate, uint32_t *graph, uint32_t *out_stat_visited,
+                           uint32_t *out_stat_dist, uint64_t *out_isolated, int threads)
+{
+    if (n == 0 || R == 0 || L == 0 || num_split == 0 || num_split > L) return 1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    std::vector<uint32_t> G(graph, graph + size_t(n) * (R + 1));
+    std::vector<uint32_t> toG(size_t(n) * (R + 1), 0u);
+    BuildCfg cfg{dtype, metric, dims, static_cast<const uint8_t *>(base), row_bytes(dtype, dims), n, R, L, VL,
+                 top_degree, num_split, num_passes, limit == 0 ? n : limit, 0.0f, float(min_alpha), float(max_alpha),
+                 float(min_cos), float(max_cos)};
+    Builder b(cfg, G);
+    std::vector<uint32_t> inserts(n);
+    std::iota(inserts.begin(), inserts.end(), 0u);
+    Popular mode = Popular::FixedMax;
+    if (num_split > 1) {
+        auto fill = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+            for (size_t j = 0; j < hi - lo; ++j) sp[j].push_back(inserts[lo + j] % num_split);
+        };
+        for (int i = 0; i < 2; ++i) {
+            std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
+            b.batch_insert(inserts, fill, mode, threads);
+        }
+    }
+    auto fill_iota = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+        for (size_t j = 0; j < hi - lo; ++j)
+            for (uint32_t s = 0; s < num_split; ++s) sp[j].push_back(s);
+    };
+    auto fill_rand = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+        for (size_t j = 0; j < hi - lo; ++j) sp[j].push_back(uint32_t(inserts.size() - inserts[lo + j] - 1));
+    };
+    auto fill_default = [&](std::vector<std::vector<uint32_t>> &sp, size_t lo, size_t hi) {
+        for (size_t j = 0; j < hi - lo; ++j) sp[j].push_back(0);
+    };
+    for (int i = 0; i < int(num_passes); ++i) {
+        std::shuffle(inserts.begin(), inserts.end(), std::mt19937(i));
+        if (i == int(num_passes) - 2 && dynamic_prune) mode = Popular::Cal;
+        else if (i == int(num_passes) - 1) mode = (dynamic_prune && num_passes > 1) ? Popular::Prune : Popular::FixedMin;
+        else mode = Popular::FixedMax;
+        if (i != int(num_passes) - 1) {
+            b.T = &toG;
+            b.batch_insert(inserts, fill_iota, mode, threads, true);
+            b.T = nullptr;
+        } else {
+            Builder f(cfg, toG);
+            f.popular = b.popular;
+            f.min_pop = b.min_pop;
+            f.max_pop = b.max_pop;
+            f.stat_visited = b.stat_visited;
+            f.stat_dist = b.stat_dist;
+            f.batch_insert(inserts, rand_sp ? std::function<void(std::vector<std::vector<uint32_t>> &, size_t, size_t)>(fill_rand)
+                                            : fill_default, mode, threads);
+            b.stat_visited = f.stat_visited;
+            b.stat_dist = f.stat_dist;
+        }
+    }
+    size_t iso = 0;
+    if (repair_isolate) iso = repair_isolated(toG, R, n, 0);
+    std::copy(toG.begin(), toG.end(), graph);
     if (out_stat_visited) std::copy(b.stat_visited.begin(), b.stat_visited.end(), out_stat_visited);
     if (out_stat_dist) std::copy(b.stat_dist.begin(), b.stat_dist.end(), out_stat_dist);
     if (out_isolated) *out_isolated = iso;

@@ -14,11 +14,13 @@ Inputs are small seeded synthetic sets.  Outputs, stored as tests/golden/*.npz:
                   works on whole 100,000-row blocks) the seed of the rows and the SHA-256 of
                   the reference's output instead of the rows themselves;
   * fmtconv.npz   FmtConv fbin2u8bin, u8bin2u4bin (odd row length) and vec2bin outputs;
+  * fgim_*.npz    .graph files written by the FGIM binary (pair passes, split stage, dynamic
+                  prune, rand_sp), kept as raw bytes;
   * rerank_*.npz  beam_search_rerank through the harness with raw float rows beside 4-bit
                   (L2) and u8 (inner product) quantised rows: rerank factors 100, 3 and 0
                   (filtering mode), on a graph built by the oracle.
 
-Usage: make -C oracle ref && python tests/golden/make_golden.py [--only pca,rerank]
+Usage: make -C oracle ref && python tests/golden/make_golden.py [--only pca,rerank,fgim]
 """
 import os
 import subprocess
@@ -113,6 +115,25 @@ def rerank_golden():
         np.savez_compressed(f"{HERE}/rerank_{name}.npz", **out)
 
 
+def fgim_golden(tmp):
+    b, _ = synth.u8_mixture(3000, 1, dim=32, n_centres=12, seed=7)
+    formats.write_vectors(f"{tmp}/fb.u8bin", b)
+    builds = {
+        "split4": ["--num_split", "4", "--num_passes", "2"],
+        "dyn3": ["--num_split", "4", "--num_passes", "3", "--dynamic_prune", "--min_alpha", "1.05", "--max_alpha",
+                 "1.2"],
+        "randsp": ["--num_split", "2", "--num_passes", "2", "--rand_sp"],
+    }
+    for name, flags in builds.items():
+        ip = f"{tmp}/fidx_{name}"
+        subprocess.run([os.path.join(REF_DIR, "FGIM"), "--quant_base_path", f"{tmp}/fb.u8bin", "--index_path", ip,
+                        "--R", "16", "--L", "24", "--VL", "32", "--rebuild", *flags], check=True,
+                       stdout=subprocess.DEVNULL)
+        raw = open(ip + ".graph", "rb").read()
+        np.savez_compressed(f"{HERE}/fgim_{name}.npz", base=b, graph_file=np.frombuffer(raw, np.uint8),
+                            flags=np.array(" ".join(["--R 16 --L 24 --VL 32"] + flags)))
+
+
 def main():
     if not (os.path.exists(REF_COMPGT) and os.path.exists(REF_VAMANA) and reference()):
         sys.exit("build the reference first: make -C oracle ref")
@@ -123,6 +144,8 @@ def main():
         pca_golden(tmp)
     if only is None or "rerank" in only:
         rerank_golden()
+    if only is None or "fgim" in only:
+        fgim_golden(tmp)
     if only is not None:
         print("golden vectors written to", HERE)
         return
