@@ -237,6 +237,39 @@ def time_next_rows(idx, base, q, gi, L_op, k, local, reps=5):
     return out
 
 
+def time_fgim(base, q, gi, L_op, k, local, n_prefix=100_000):
+    """The FGIM builder (FGIM.cpp:157-265) at the build configuration's R/L/VL/passes/split:
+    on the GPU over all rows, with the recall of its graph at the operating L; and on a
+    prefix of n_prefix rows, the GPU build beside the oracle port's on all host cores, with
+    the two graphs compared."""
+    from nbpg_gb300.index import Index, QueryParams
+    kw = dict(L=CFG["L_build"], VL=CFG["VL"], num_split=CFG["num_split"], num_passes=CFG["num_passes"],
+              dynamic_prune=CFG["dynamic_prune"], min_alpha=CFG["min_alpha"], max_alpha=CFG["max_alpha"])
+    fi = Index(base, "u8", "l2", max_degree=CFG["R"], device=local)
+    st, _, _ = fi.build_fgim(**kw)
+    res = fi.search(q, QueryParams(k=k, beamSize=L_op, cut=CFG["cut"]))
+    out = {"n": len(base), "gpu_s": st.seconds, "isolated_repaired": int(st.isolated), "L": L_op,
+           "recall@10_at_L": recall_of(res.ids, gi, k)}
+    del fi
+    sub = np.ascontiguousarray(base[:n_prefix])
+    pi = Index(sub, "u8", "l2", max_degree=CFG["R"], device=local)
+    pst, _, _ = pi.build_fgim(**kw)
+    g_gpu = pi.get_graph()
+    del pi
+    from oracle.oracle import oracle
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    g_cpu, _, _, _ = oracle().build_fgim("u8", "l2", sub, R=CFG["R"], threads=threads, **kw)
+    cpu_s = time.perf_counter() - t
+    R = CFG["R"]
+    mask = np.arange(R)[None, :] < g_gpu[:, :1]
+    same = bool(np.array_equal(g_gpu[:, :1], g_cpu[:, :1]) and np.array_equal(g_gpu[:, 1:][mask], g_cpu[:, 1:][mask]))
+    out["prefix"] = {"n": n_prefix, "gpu_s": pst.seconds, "graph_equal_to_port": same,
+                     "cpu_baseline": {"seconds": cpu_s, "cores": threads, "kind": "port"},
+                     "gpu_over_cpu": cpu_s / pst.seconds}
+    return out
+
+
 def recall_of(ids, gi, k):
     return float(np.mean([len(set(a[:k].tolist()) & set(b[:k].tolist())) / k for a, b in zip(ids, gi)]))
 
@@ -570,6 +603,11 @@ def main():
 
     next_rows = time_next_rows(idx, base, q, gi, L_op, k, local) if rank == 0 else None
     if next_rows:
+        next_rows["fgim_build"] = time_fgim(base, q, gi, L_op, k, local)
+        fg = next_rows["fgim_build"]
+        log(f"[bench] FGIM build {fg['gpu_s']:.2f} s on the GPU, recall {fg['recall@10_at_L']:.4f} at L={L_op}; "
+            f"{fg['prefix']['n']} rows: GPU {fg['prefix']['gpu_s']:.2f} s vs port "
+            f"{fg['prefix']['cpu_baseline']['seconds']:.1f} s, graphs equal: {fg['prefix']['graph_equal_to_port']}")
         log(f"[bench] PCA encode {next_rows['pca_encode']['ms']:.2f} ms per 1M rows; re-rank "
             f"{next_rows['rerank']['rerank_factor_100']['qps_host_api']:.3g} QPS; device recall "
             f"{next_rows['eval_recall']['recall@10']:.4f}")
