@@ -81,6 +81,24 @@ def write_graph(path: str, g: np.ndarray) -> None:
         g[:, 1:][mask].tofile(f)
 
 
+def read_hid(path: str) -> tuple[int, int, int, np.ndarray]:
+    """An HNSW id mapping (HNSW/base/hier_idmapping.h:20-46): max_node_num, cur_node_num, entry
+    node, then id_in_pre_level for the cur_node_num nodes (int64; -1 - vector id at level 0)."""
+    with open(path, "rb") as f:
+        mx, cur, sp = (int(x) for x in np.fromfile(f, dtype=np.uint64, count=3))
+        pre = np.fromfile(f, dtype=np.int64, count=cur)
+    if pre.size != cur:
+        raise ValueError(f"{path}: malformed id mapping")
+    return mx, cur, sp, pre
+
+
+def write_hid(path: str, max_node: int, sp: int, pre: np.ndarray) -> None:
+    pre = np.ascontiguousarray(pre, dtype=np.int64)
+    with open(path, "wb") as f:
+        np.array([max_node, pre.size, sp], dtype=np.uint64).tofile(f)
+        pre.tofile(f)
+
+
 def read_gt(path: str) -> tuple[np.ndarray, np.ndarray]:
     with open(path, "rb") as f:
         nq, k = (int(x) for x in np.fromfile(f, dtype=np.uint32, count=2))

@@ -142,6 +142,15 @@ struct Cell {
         fs = vs = num_visited = inserted = 0;
     }
 
+    // a new search in the same cell without clearing the visited filter: the HNSW build's
+    // per-level searches (hnsw.h:179-190 resets only the sizes)
+    void restart(uint32_t L_, uint32_t max_visited_)
+    {
+        L = L_;
+        max_visited = max_visited_;
+        fs = vs = num_visited = inserted = 0;
+    }
+
     bool seen(uint32_t a)
     {
         uint32_t slot = uint32_t(splitmix_final(a) & (slots - 1));
@@ -167,9 +176,9 @@ void seed_frontier(Cell &c, const uint32_t *sp, uint32_t nsp, DistTo dist_to)
 // Greedy beam search: algorithms/utils/Graph/beamSearch.h:43-171 with
 // Points == Q_Points (the pure quantized path used by both query and build).
 // `self` is the node being inserted (Points[a].same_as(p), beamSearch.h:79) or -1.
-template <class DistTo>
-size_t beam_search(Cell &c, const GraphView &G, DistTo dist_to, int64_t self, uint32_t k, double cut,
-                   uint64_t limit, uint32_t degree_limit)
+template <class DistTo, class IsSelf>
+size_t beam_search_x(Cell &c, const GraphView &G, DistTo dist_to, IsSelf is_self, uint32_t k, double cut,
+                     uint64_t limit, uint32_t degree_limit)
 {
     const uint32_t L = c.L;
     size_t cmps = c.fs;
@@ -182,7 +191,7 @@ size_t beam_search(Cell &c, const GraphView &G, DistTo dist_to, int64_t self, ui
         size_t nf = 0;
         for (uint32_t i = 0; i < ne; ++i) {
             uint32_t a = G.nbr(cur.id, i);
-            if (c.seen(a) || int64_t(a) == self) continue;
+            if (c.seen(a) || is_self(a)) continue;
             c.filtered[nf++] = a;
         }
         for (size_t i = 0; i < nf; ++i) {
@@ -230,6 +239,14 @@ size_t beam_search(Cell &c, const GraphView &G, DistTo dist_to, int64_t self, ui
                      c.unvisited.begin());
     }
     return cmps;
+}
+
+template <class DistTo>
+size_t beam_search(Cell &c, const GraphView &G, DistTo dist_to, int64_t self, uint32_t k, double cut,
+                   uint64_t limit, uint32_t degree_limit)
+{
+    return beam_search_x(c, G, dist_to, [self](uint32_t a) { return int64_t(a) == self; }, k, cut, limit,
+                         degree_limit);
 }
 
 // ---------------------------------------------------------------------------
@@ -292,6 +309,53 @@ size_t robust_prune(uint32_t p, Node *c, size_t &n, uint32_t R, double alpha, do
     }
     n = sel;
     return cmps;
+}
+
+// Prune::maxAnglePrune (prune.h:92-154), step for step: each round takes the candidate at
+// `sel` (a reference into the array, so a later swap into that slot changes the distance the
+// rule reads), scores the rest by their largest cosine to a selected point, keeps those that
+// pass survives_prune_enhanced (prune.h:240-249) compacted after `sel`, and swaps a survivor
+// whose score is below the current slot's into that slot.  Returns false where the reference
+// aborts (a candidate equal to p or -1, or alpha and cos_angle both unset).
+template <class PairDist>
+bool max_angle_prune(uint32_t p, Node *c, size_t &n, uint32_t R, double alpha, double cos_angle, PairDist pair_dist,
+                     size_t &cmps)
+{
+    cmps = 0;
+    if (alpha <= kEps && cos_angle <= kEps) return false;
+    std::vector<float> score(n, -2.f);
+    size_t sel = 0;  // start_prune_id = 1
+    while (sel < R && sel < n) {
+        Node &cur = c[sel];
+        const uint32_t ps = cur.id;
+        if (ps == p || ps == 0xFFFFFFFFu) return false;
+        ++sel;
+        size_t se = sel;
+        for (size_t i = sel; i < n; ++i) {
+            const uint32_t pp = c[i].id;
+            ++cmps;
+            const float dsp = pair_dist(ps, pp);
+            const float dpp = c[i].d;
+            const float cv = cos_at_p(cur.d, dpp, dsp);
+            score[i] = std::max(score[i], cv);
+            bool keep = false;
+            if (alpha > kEps && alpha * dsp > dpp) keep = true;
+            else if (cos_angle > kEps && cv < cos_angle) keep = true;
+            if (!keep) continue;
+            if (i > se) {
+                std::swap(c[se], c[i]);
+                std::swap(score[se], score[i]);
+            }
+            if (score[se] < score[sel - 1]) {
+                std::swap(c[se], c[sel - 1]);
+                std::swap(score[se], score[sel - 1]);
+            }
+            ++se;
+        }
+        n = se;
+    }
+    n = sel;
+    return true;
 }
 
 // utilities.h:128-165 — two-pointer union; the first range need not be sorted.
@@ -622,6 +686,283 @@ size_t repair_isolated(std::vector<uint32_t> &G, uint32_t R, uint64_t n, uint32_
     return cnt;
 }
 
+// ---------------------------------------------------------------------------
+// HNSW build: data_tools/ANNs/HNSW/base/hnsw.h:42-279 (HNSWIndex::batch_insert),
+// hier_idmapping.h:9-107 (id_in_pre_level, levels, root ids), hier_utils.h:14-50 (entry
+// points between levels), dfs.h:138-262 (repair over the hierarchy); HNSW.cpp:62-72 (m_l
+// and node-count defaults).  Every (vector, level) pair is a node; a vector of level l takes
+// l + 1 consecutive ids from the top down, id_in_pre_level links each to the one below and
+// the level-0 node to -1 - vector id.
+// ---------------------------------------------------------------------------
+struct HnswBuild {
+    int dtype, metric;
+    uint32_t dims;
+    const uint8_t *base;
+    size_t row;
+    uint64_t n;
+    uint32_t R, L, VL, top_degree, hbs, PR;
+    double alpha, cos_angle, m_l;
+    size_t max_node, cur = 0;
+    std::vector<uint32_t> G;
+    std::vector<int64_t> pre;
+    std::vector<uint32_t> root, sv, sd;
+    uint64_t ep = 0;
+    uint32_t max_level = 0;
+    bool aborted = false;
+
+    const uint8_t *pt(uint32_t v) const { return base + size_t(root[v]) * row; }
+    float dist(uint32_t a, uint32_t b) const { return dist_rows(dtype, metric, pt(a), pt(b), dims); }
+    uint32_t *rw(size_t v) { return &G[v * (R + 1)]; }
+    uint32_t level(int64_t v) const
+    {
+        uint32_t l = 0;
+        for (int64_t q = pre[v]; q >= 0; q = pre[q]) ++l;
+        return l;
+    }
+
+    struct Layer {
+        uint32_t src;
+        std::vector<Node> nbrs;
+    };
+
+    // one insert across levels max_level .. 0 (hnsw.h:158-215 with searchNghAndPrune, :52-83)
+    void insert(Cell &c, uint32_t &node, uint32_t lvl, std::vector<uint32_t> &sp, uint64_t limit,
+                std::vector<Layer> &out)
+    {
+        c.reset(L, 2 * L, R);
+        for (int lc = int(max_level); lc >= 0; --lc) {
+            const uint32_t index = node;
+            const bool is_insert = lc <= int(lvl);
+            const uint32_t beam = is_insert ? L : hbs;
+            c.restart(beam, 2 * beam);
+            uint32_t nsp = 1;
+            while (nsp < hbs && sp[nsp] != 0xFFFFFFFFu) ++nsp;
+            auto dist_to = [&](uint32_t a) { return dist(a, index); };
+            seed_frontier(c, sp.data(), nsp, dist_to);
+            GraphView gv{G.data(), R};
+            const uint32_t rt = root[index];
+            size_t cmps = beam_search_x(c, gv, dist_to, [&](uint32_t a) { return root[a] == rt; }, 0, 0.0, limit, R);
+            sv[index] += uint32_t(c.num_visited);
+            sd[index] += uint32_t(cmps);
+            size_t np = merge_union(c.visited.data(), 0, c.visited.data(), c.vs, c.pool.data(), VL);
+            const double a = lc == 0 ? alpha : 1.0;
+            size_t rp = 0;
+            auto pd = [&](uint32_t x, uint32_t y) { return dist(x, y); };
+            if (PR > 0) {
+                if (!max_angle_prune(index, c.pool.data(), np, R, a, cos_angle, pd, rp)) {
+                    aborted = true;
+                    return;
+                }
+            } else {
+                rp = robust_prune(index, c.pool.data(), np, R, a, cos_angle, pd);
+            }
+            sd[index] += uint32_t(rp);
+            if (is_insert) {
+                uint32_t *r = rw(index);
+                r[0] = uint32_t(np);
+                for (size_t j = 0; j < np; ++j) r[1 + j] = c.pool[j].id;
+                out.push_back(Layer{index, std::vector<Node>(c.pool.begin(), c.pool.begin() + np)});
+                node = uint32_t(pre[index]);
+            }
+            if (lc > 0) {
+                // fill_next_level_entry_points (hier_utils.h:24-50)
+                std::fill(sp.begin(), sp.end(), 0xFFFFFFFFu);
+                const size_t m = std::min<size_t>(hbs, c.vs);
+                for (size_t j = 0; j < m; ++j) {
+                    const uint32_t near = c.visited[j].id;
+                    sp[j] = level(near) >= uint32_t(lc) ? uint32_t(pre[near]) : near;
+                }
+            }
+        }
+    }
+
+    // nsw.h:329-355 over hierarchical ids
+    size_t fill_new_dists(uint32_t index, Node *cd, size_t p0, size_t m) const
+    {
+        size_t rp = 0;
+        size_t td = top_degree == 0 ? R : top_degree;
+        size_t end = std::min(p0 + td, m);
+        for (size_t j = p0; j < end; ++j) { cd[j].d = dist(cd[j].id, index); ++rp; }
+        if (end < m) {
+            float a = cd[end - 1].d;
+            float b = dist(cd[m - 1].id, index);
+            cd[m - 1].d = b;
+            ++rp;
+            float delta = (a - b) / float(m - end);
+            for (size_t j = end; j < m - 1; ++j) {
+                float step = float(j - end + 1) * delta;
+                cd[j].d = a + step;
+            }
+        }
+        return rp;
+    }
+
+    int run(int threads)
+    {
+        G.assign(max_node * (R + 1), 0u);
+        pre.assign(max_node, 0);
+        root.assign(max_node, 0u);
+        sv.assign(max_node, 0u);
+        sd.assign(max_node, 0u);
+        size_t eff = std::min<size_t>(size_t(0.02 * double(float(max_node))), 1000000ul);
+        if (eff == 0) eff = 1;
+        std::vector<Cell> cells(std::max(1, threads));
+        size_t inc = 0, count = 0;
+        const size_t m = n;
+        std::vector<uint32_t> nodes, lv;
+        while (count < m) {
+            size_t floor, ceiling;
+            if (std::pow(2.0, double(inc)) <= double(eff)) {
+                floor = size_t(std::pow(2.0, double(inc))) - 1;
+                ceiling = std::min(size_t(std::pow(2.0, double(inc + 1))) - 1, m);
+                count = ceiling;
+            } else {
+                floor = count;
+                ceiling = std::min(count + eff, m);
+                count = count + (ceiling - floor);
+            }
+            const size_t bs = ceiling - floor;
+            nodes.assign(bs, 0u);
+            lv.assign(bs, 0u);
+            // levels (hnsw.h:118-127): srand(ceiling), -log(r) * m_l, capped at max_level + 1
+            srand(unsigned(ceiling));
+            for (size_t i = 0; i < bs; ++i) {
+                const double r = double(rand()) / RAND_MAX;
+                lv[i] = std::min(static_cast<unsigned>(-std::log(r) * m_l), max_level + 1);
+            }
+            // ids from the top down (hnsw.h:129-152)
+            for (size_t i = 0; i < bs; ++i) {
+                int l = int(lv[i]);
+                int64_t node = int64_t(cur);
+                nodes[i] = uint32_t(node);
+                while (l >= 0) {
+                    ++cur;
+                    if (cur > max_node) return 2;
+                    const int64_t p = l == 0 ? -1 - int64_t(floor + i) : int64_t(cur);
+                    pre[node] = p;
+                    root[node] = uint32_t(floor + i);
+                    node = p;
+                    --l;
+                }
+            }
+            // a new top level: its nodes linked among themselves, searches start one level down
+            // (hnsw.h:154-176)
+            std::vector<uint32_t> fresh;
+            for (size_t i = 0; i < bs; ++i)
+                if (lv[i] > max_level) {
+                    fresh.push_back(nodes[i]);
+                    nodes[i] = uint32_t(pre[nodes[i]]);
+                    --lv[i];
+                }
+            if (!fresh.empty()) {
+                const size_t lc = std::min<size_t>(fresh.size(), R);
+                for (size_t i = 0; i < fresh.size(); ++i)
+                    for (size_t j = 1; j < lc; ++j) {
+                        uint32_t *r = rw(fresh[i]);
+                        r[1 + r[0]] = fresh[(i + j) % fresh.size()];
+                        r[0] += 1;
+                    }
+            }
+            std::vector<std::vector<Layer>> layers(bs);
+            const uint64_t limit = cur;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 8)
+            for (long long i = 0; i < (long long)bs; ++i) {
+                std::vector<uint32_t> sp(hbs, 0xFFFFFFFFu);
+                sp[0] = uint32_t(ep);
+                uint32_t node = nodes[i];
+                insert(cells[omp_get_thread_num()], node, lv[i], sp, limit, layers[i]);
+            }
+            if (aborted) return 3;
+            // reverse edges of every layer (nsw.h:446-485, merge_edges.h:53-119)
+            struct Edge {
+                uint32_t target;
+                Node src;
+            };
+            std::vector<Edge> edges;
+            for (auto &ls : layers)
+                for (auto &ly : ls)
+                    for (const Node &e : ly.nbrs) edges.push_back(Edge{e.id, Node{ly.src, e.d}});
+            std::sort(edges.begin(), edges.end(), [](const Edge &a, const Edge &b) {
+                if (a.target != b.target) return a.target < b.target;
+                return node_less(a.src, b.src);
+            });
+            std::vector<size_t> starts;
+            for (size_t i = 0; i < edges.size(); ++i)
+                if (i == 0 || edges[i].target != edges[i - 1].target) starts.push_back(i);
+            starts.push_back(edges.size());
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+            for (long long g = 0; g < (long long)starts.size() - 1; ++g) {
+                size_t b = starts[g], e = std::min(starts[g + 1], b + size_t(VL));
+                uint32_t t = edges[b].target;
+                std::vector<Node> cand(VL + R);
+                size_t cs = 0;
+                for (size_t j = b; j < e; ++j) cand[cs++] = edges[j].src;
+                size_t p0 = cs;
+                uint32_t *r = rw(t);
+                for (uint32_t i = 0; i < r[0]; ++i) {
+                    uint32_t nb = r[1 + i];
+                    bool dup = false;
+                    for (size_t j = 0; j < cs; ++j)
+                        if (cand[j].id == nb) { dup = true; break; }
+                    if (dup || cs >= size_t(VL) + R) continue;
+                    cand[cs++].id = nb;
+                }
+                sd[t] += uint32_t(fill_new_dists(t, cand.data(), p0, cs));
+                if (cs <= R) {
+                    std::sort(cand.begin(), cand.begin() + cs, node_less);
+                } else {
+                    dedupe_by_id(cand.data(), cs);
+                    std::sort(cand.begin(), cand.begin() + cs, node_less);
+                    if (cs > R) cs = R;
+                }
+                r[0] = uint32_t(cs);
+                for (size_t j = 0; j < cs; ++j) r[1 + j] = cand[j].id;
+            }
+            if (!fresh.empty()) {
+                ep = fresh[0];
+                ++max_level;
+            }
+            ++inc;
+        }
+        return 0;
+    }
+
+    // DFS::repair_isolate_node over the hierarchy (dfs.h:138-177, 217-262): reachability from
+    // the entry follows edges and the link to the level below; only level-0 nodes are repaired.
+    size_t repair()
+    {
+        const size_t nn = cur;
+        std::vector<int> flag(nn, 0);
+        std::queue<size_t> q;
+        flag[ep] = 1;
+        q.push(ep);
+        while (!q.empty()) {
+            size_t v = q.front();
+            q.pop();
+            const int64_t low = pre[v];
+            if (low >= 0 && !flag[size_t(low)]) { flag[size_t(low)] = 1; q.push(size_t(low)); }
+            const uint32_t *r = rw(v);
+            for (uint32_t j = 0; j < r[0]; ++j)
+                if (!flag[r[1 + j]]) { flag[r[1 + j]] = 1; q.push(r[1 + j]); }
+        }
+        size_t cnt = 0;
+        for (size_t i = 0; i < nn; ++i) {
+            if (flag[i] || level(int64_t(i)) > 0) continue;
+            ++cnt;
+            const uint32_t *r = rw(i);
+            bool done = false;
+            for (uint32_t j = 0; j < r[0] && !done; ++j)
+                if (flag[r[1 + j]] == 1 && add_edge_if_possible(G, R, r[1 + j], i)) done = true;
+            for (uint32_t j = 0; j < r[0] && !done; ++j)
+                if (add_edge_if_possible(G, R, r[1 + j], i)) done = true;
+            if (!done && flag[ep] == 1 && add_edge_if_possible(G, R, ep, i)) done = true;
+            for (size_t x = 0; x < nn && !done; ++x)
+                if (flag[x] == 1 && add_edge_if_possible(G, R, x, i)) done = true;
+        }
+        return cnt;
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -951,6 +1292,134 @@ int nbpg_oracle_build_fgim(int dtype, int metric, uint32_t dims, const void *bas
 // Brute-force kNN: CompGT.cpp:29-134.  exact == 0 replays CompGT's replace-max
 // rule, including its stale read of topk[0] (CompGT.cpp:80-95); exact != 0 keeps
 // the true (dist, id) top-k.  Output rows sorted by (dist, id).  Requires n >= k.
+// HNSW build (HNSW.cpp:166-208 with hnsw.h): graph and id_in_pre_level for the first
+// *out_cur nodes (buffers of max_node entries; max_node == 0 and m_l <= 1e-5 take
+// HNSW.cpp:62-72's defaults, *out_max_node returns the value used), entry node, per-node
+// BuildStats.  Returns 1 on bad arguments, 2 when the node count passes max_node, 3 where the
+// reference aborts in maxAnglePrune (PR > 0 with a candidate equal to the node itself).
+int nbpg_oracle_build_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t R, uint32_t L,
+                           uint32_t VL, uint32_t top_degree, uint32_t hbs, double alpha, double cos_angle, double m_l,
+                           uint64_t max_node, uint32_t PR, int repair_isolate, uint32_t *graph, int64_t *pre,
+                           uint64_t *out_cur, uint64_t *out_sp, uint32_t *out_sv, uint32_t *out_sd,
+                           uint64_t *out_iso, int threads)
+{
+    if (n == 0 || R == 0 || L == 0 || hbs == 0 || hbs > L || 2 * uint64_t(L) > VL) return 1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    HnswBuild h{};
+    h.dtype = dtype;
+    h.metric = metric;
+    h.dims = dims;
+    h.base = static_cast<const uint8_t *>(base);
+    h.row = row_bytes(dtype, dims);
+    h.n = n;
+    h.R = R;
+    h.L = L;
+    h.VL = VL;
+    h.top_degree = top_degree;
+    h.hbs = hbs;
+    h.PR = PR;
+    h.alpha = alpha;
+    h.cos_angle = cos_angle;
+    h.m_l = m_l < 1e-5 ? 1.0f / std::log(double(R)) : m_l;
+    h.max_node = max_node ? max_node : size_t((std::exp(-1.0f / h.m_l) * 2 + 1) * double(uint32_t(n)));
+    int rc = h.run(threads);
+    if (rc) return rc;
+    size_t iso = repair_isolate ? h.repair() : 0;
+    std::copy(h.G.begin(), h.G.begin() + h.cur * (R + 1), graph);
+    std::copy(h.pre.begin(), h.pre.begin() + h.cur, pre);
+    *out_cur = h.cur;
+    *out_sp = h.ep;
+    if (out_sv) std::copy(h.sv.begin(), h.sv.begin() + h.cur, out_sv);
+    if (out_sd) std::copy(h.sd.begin(), h.sd.begin() + h.cur, out_sd);
+    if (out_iso) *out_iso = iso;
+    return 0;
+}
+
+// hier_qsearchAll (HNSW/base/hier_beamSearch.h:9-92): from the entry, each level above 0 runs
+// a search of beam hbs (the query's k and cut, visited cap 8L, a fresh filter sized by L) whose
+// visited list gives the next level's entry points; level 0 is the plain search of beam L
+// (visited and distance counts of that search only); the frontier's first k become vector ids.
+int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n,
+                            const uint32_t *graph, uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp,
+                            const void *queries, uint32_t nq, uint32_t L, uint32_t k, double cut, uint32_t hbs,
+                            uint32_t k_stride, uint32_t *out_ids, uint32_t *out_count, uint32_t *out_visited,
+                            uint32_t *out_cmps, int threads)
+{
+    if (k == 0 || k > L || hbs == 0 || hbs > L || sp >= cur) return 1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    const size_t row = row_bytes(dtype, dims);
+    const uint8_t *B = static_cast<const uint8_t *>(base);
+    const uint8_t *Q = static_cast<const uint8_t *>(queries);
+    std::vector<uint32_t> rootv(cur), lvl(cur);
+    for (uint64_t v = 0; v < cur; ++v) {
+        int64_t q = int64_t(v);
+        uint32_t l = 0;
+        while (pre[q] >= 0) { q = pre[q]; ++l; }
+        rootv[v] = uint32_t(-pre[q] - 1);
+        lvl[v] = l;
+    }
+    GraphView gv{graph, R};
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 4)
+    for (long long i = 0; i < (long long)nq; ++i) {
+        Cell c;
+        const uint8_t *qr = Q + size_t(i) * row;
+        auto dist_to = [&](uint32_t a) { return dist_rows(dtype, metric, B + size_t(rootv[a]) * row, qr, dims); };
+        std::vector<uint32_t> spv(hbs, 0xFFFFFFFFu);
+        spv[0] = uint32_t(sp);
+        while (true) {
+            const uint32_t lv = lvl[spv[0]];
+            uint32_t nsp = 1;
+            while (nsp < hbs && spv[nsp] != 0xFFFFFFFFu) ++nsp;
+            if (lv > 0) {
+                c.reset(L, 8 * L, R);
+                c.restart(hbs, 8 * L);
+                seed_frontier(c, spv.data(), nsp, dist_to);
+                beam_search(c, gv, dist_to, -1, k, cut, cur, R);
+                std::fill(spv.begin(), spv.end(), 0xFFFFFFFFu);
+                const size_t m = std::min<size_t>(hbs, c.vs);
+                for (size_t j = 0; j < m; ++j) {
+                    const uint32_t near = c.visited[j].id;
+                    spv[j] = lvl[near] >= lv ? uint32_t(pre[near]) : near;
+                }
+                continue;
+            }
+            c.reset(L, 8 * L, R);
+            seed_frontier(c, spv.data(), nsp, dist_to);
+            size_t cmps = beam_search(c, gv, dist_to, -1, k, cut, cur, R);
+            const size_t kk = std::min<size_t>(k, c.fs);
+            for (uint32_t j = 0; j < k_stride; ++j)
+                out_ids[size_t(i) * k_stride + j] = j < kk ? rootv[c.frontier[j].id] : 0xFFFFFFFFu;
+            if (out_count) out_count[i] = uint32_t(kk);
+            if (out_visited) out_visited[i] = uint32_t(c.num_visited);
+            if (out_cmps) out_cmps[i] = uint32_t(cmps);
+            break;
+        }
+    }
+    return 0;
+}
+
+// Prune::maxAnglePrune (prune.h:92-154) on one candidate list as given; 3 where the
+// reference aborts.
+int nbpg_oracle_max_angle_prune(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t p,
+                                uint32_t *ids, float *dists, uint32_t *cnt, uint32_t R, uint32_t PR, double alpha,
+                                double cos_angle, uint32_t *out_cmps)
+{
+    if (PR < *cnt) return 1;
+    const size_t row = row_bytes(dtype, dims);
+    const uint8_t *B = static_cast<const uint8_t *>(base);
+    std::vector<Node> c(*cnt);
+    for (uint32_t i = 0; i < *cnt; ++i) c[i] = Node{ids[i], dists[i]};
+    size_t m = *cnt, cmps = 0;
+    if (!max_angle_prune(p, c.data(), m, R, alpha, cos_angle,
+                         [&](uint32_t a, uint32_t b) { return dist_rows(dtype, metric, B + size_t(a) * row, B + size_t(b) * row, dims); },
+                         cmps))
+        return 3;
+    for (size_t i = 0; i < m; ++i) { ids[i] = c[i].id; dists[i] = c[i].d; }
+    *cnt = uint32_t(m);
+    if (out_cmps) *out_cmps = uint32_t(cmps);
+    return 0;
+}
+
 int nbpg_oracle_gt(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, const void *queries,
                    uint32_t nq, uint32_t k, int exact, uint32_t *out_ids, float *out_dists, int threads)
 {

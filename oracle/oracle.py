@@ -10,6 +10,7 @@ timed CPU baseline; the product never imports it.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -28,6 +29,7 @@ _u8p = C.c_void_p
 _u32p = C.POINTER(C.c_uint32)
 _f32p = C.POINTER(C.c_float)
 _u64p = C.POINTER(C.c_uint64)
+_i64p = C.POINTER(C.c_int64)
 
 
 def build(ref_root: str | None = None) -> None:
@@ -73,6 +75,20 @@ class CpuLib:
                                         C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_double,
                                         C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _u32p, _u32p,
                                         _u32p, _u64p, C.c_int]
+        if hasattr(self.lib, prefix + "build_hnsw"):
+            f("build_hnsw").restype = C.c_int
+            f("build_hnsw").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, C.c_uint32,
+                                        C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                        C.c_uint64, C.c_uint32, C.c_int, _u32p, _i64p, _u64p, _u64p, _u32p, _u32p,
+                                        _u64p, C.c_int]
+            f("search_hnsw").restype = C.c_int
+            f("search_hnsw").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, _u32p, C.c_uint32, _i64p,
+                                         C.c_uint64, C.c_uint64, _u8p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double,
+                                         C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p, _u32p] + \
+                ([C.c_int] if prefix == "nbpg_oracle_" else [])
+            f("max_angle_prune").restype = C.c_int
+            f("max_angle_prune").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, _u32p,
+                                             _f32p, _u32p, C.c_uint32, C.c_uint32, C.c_double, C.c_double, _u32p]
         if hasattr(self.lib, prefix + "search_rerank"):
             f("search_rerank").restype = C.c_int
             f("search_rerank").argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -206,6 +222,70 @@ class CpuLib:
         if rc != 0:
             raise ValueError("build_fgim rejected its arguments")
         return g, sv, sd, int(iso[0])
+
+    @staticmethod
+    def hnsw_sizes(n, R, m_l=0.0, max_node=0):
+        """m_l and the node capacity the HNSW driver derives when they are unset (HNSW.cpp:62-72)."""
+        if m_l < 1e-5:
+            m_l = 1.0 / math.log(R)
+        if max_node == 0:
+            max_node = int((math.exp(-1.0 / m_l) * 2 + 1) * n)
+        return m_l, max_node
+
+    def build_hnsw(self, dtype, metric, base, R, L=70, VL=140, top_degree=0, hier_beam=1, alpha=1.1, cos_angle=0.0,
+                   m_l=0.0, max_node=0, PR=0, repair_isolate=True, threads=0):
+        """The HNSW build (HNSW.cpp:166-208); returns (graph[cur, R+1], id_in_pre_level[cur], entry,
+        stat_visited[cur], stat_dist[cur], isolated).  Raises RuntimeError(code) on a refusal."""
+        base = np.ascontiguousarray(base)
+        n, dims = base.shape
+        _, mn = self.hnsw_sizes(n, R, m_l, max_node)
+        g = np.zeros((mn, R + 1), np.uint32)
+        pre = np.zeros(mn, np.int64)
+        sv, sd = np.zeros(mn, np.uint32), np.zeros(mn, np.uint32)
+        cur, sp, iso = np.zeros(1, np.uint64), np.zeros(1, np.uint64), np.zeros(1, np.uint64)
+        rc = self._f("build_hnsw")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, R, L, VL, top_degree,
+                                   hier_beam, alpha, cos_angle, m_l, max_node, PR, int(repair_isolate), _p(g, _u32p),
+                                   _p(pre, _i64p), _p(cur, _u64p), _p(sp, _u64p), _p(sv, _u32p), _p(sd, _u32p),
+                                   _p(iso, _u64p), threads)
+        if rc != 0:
+            raise RuntimeError(rc)
+        c = int(cur[0])
+        return g[:c], pre[:c], int(sp[0]), sv[:c], sd[:c], int(iso[0])
+
+    def search_hnsw(self, dtype, metric, base, graph, pre, sp, queries, L, k, cut=1.35, hier_beam=1, threads=0):
+        """hier_qsearchAll (hier_beamSearch.h:9-92); returns (ids, count, visited, cmps)."""
+        base = np.ascontiguousarray(base)
+        queries = np.ascontiguousarray(queries)
+        graph = np.ascontiguousarray(graph, dtype=np.uint32)
+        pre = np.ascontiguousarray(pre, dtype=np.int64)
+        n, dims = base.shape
+        nq = queries.shape[0]
+        ids = np.zeros((nq, k), np.uint32)
+        cnt, vis, cm = (np.zeros(nq, np.uint32) for _ in range(3))
+        extra = [threads] if self.prefix == "nbpg_oracle_" else []
+        rc = self._f("search_hnsw")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, _p(graph, _u32p),
+                                    graph.shape[1] - 1, _p(pre, _i64p), graph.shape[0], sp, queries.ctypes.data, nq,
+                                    L, k, cut, hier_beam, k, _p(ids, _u32p), _p(cnt, _u32p), _p(vis, _u32p),
+                                    _p(cm, _u32p), *extra)
+        if rc != 0:
+            raise ValueError("search_hnsw rejected its arguments")
+        return ids, cnt, vis, cm
+
+    def max_angle_prune(self, dtype, metric, base, p, ids, dists, R, PR, alpha, cos_angle=0.0):
+        """Prune::maxAnglePrune (prune.h:92-154) on a candidate list; returns (ids, dists, cmps)
+        or raises RuntimeError(3) where the reference aborts."""
+        base = np.ascontiguousarray(base)
+        ids = np.ascontiguousarray(ids, dtype=np.uint32).copy()
+        dists = np.ascontiguousarray(dists, dtype=np.float32).copy()
+        cnt = np.array([len(ids)], np.uint32)
+        cm = np.zeros(1, np.uint32)
+        rc = self._f("max_angle_prune")(DTYPES[dtype], METRICS[metric], base.shape[1], base.ctypes.data,
+                                        base.shape[0], p, _p(ids, _u32p), _p(dists, _f32p), _p(cnt, _u32p), R, PR,
+                                        alpha, cos_angle, _p(cm, _u32p))
+        if rc != 0:
+            raise RuntimeError(rc)
+        c = int(cnt[0])
+        return ids[:c], dists[:c], int(cm[0])
 
     def search_rerank(self, dtype, metric, base, raw_base, graph, queries, raw_queries, L, k, rerank_factor,
                       cut=1.35, visited_factor=8, start_points=(0,)):

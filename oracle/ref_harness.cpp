@@ -21,6 +21,8 @@
 #include "utils/Graph/beamSearch.h"
 #include "utils/Graph/prune.h"
 #include "nsw.h"
+#include "HNSW/base/hnsw.h"
+#include "HNSW/base/hier_beamSearch.h"
 
 using namespace ant;
 
@@ -210,6 +212,92 @@ int build_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t R,
     return 0;
 }
 
+// HNSW build (data_tools/ANNs/HNSW/HNSW.cpp:166-208 with hnsw.h): m_l <= 1e-5 and max_node == 0
+// take HNSW.cpp:62-72's defaults.  Outputs the first cur_node_num rows of the hierarchical graph,
+// id_in_pre_level and the entry node.  PR > 0 selects maxAnglePrune, which aborts the process
+// when a candidate is the node itself: callers check that case with the oracle first.
+template <typename T>
+int hnsw_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t R, uint32_t L, uint32_t VL,
+           uint32_t top_degree, uint32_t hbs, double alpha, double cos_angle, double m_l, uint64_t max_node, uint32_t PR,
+           int repair_isolate, uint32_t *graph, int64_t *pre, uint64_t *out_cur, uint64_t *out_sp, uint32_t *out_sv,
+           uint32_t *out_sd, uint64_t *out_iso)
+{
+    using PR_t = PointRange<Point<T>>;
+    auto QPoints = make_points<T>(base, n, dims, metric);
+    if (m_l < 1e-5) m_l = 1.0f / log(R);
+    if (max_node == 0) max_node = (exp(-1.0f / m_l) * 2 + 1) * uint32_t(n);
+    QueryStatic stats(max_node);
+    Graph<uint32_t> G(R, max_node);
+    HIdMapping hid(max_node);
+    auto prune = Prune(G.max_degree(), omp_get_max_threads(), PR);
+    HNSWIndex<uint32_t> h(prune, L, hbs, VL, omp_get_max_threads(), G.max_degree(),
+                          NSWIndex<uint32_t>::getMaxBatchSize(G), top_degree, cos_angle);
+    h.batch_insert(G, hid, QPoints, alpha, m_l, &stats, 2, .02, false);
+    size_t iso = 0;
+    if (repair_isolate) iso = DFS::repair_isolate_node(G, hid.get_sp(), 1000, &hid);
+    const size_t cur = hid.cur_node_num;
+    for (size_t i = 0; i < cur; ++i) {
+        std::memcpy(graph + i * (R + 1), G[i].data(), (R + 1) * sizeof(uint32_t));
+        pre[i] = hid.get_id_in_pre_level(int64_t(i));
+    }
+    *out_cur = cur;
+    *out_sp = hid.get_sp();
+    if (out_sv) std::memcpy(out_sv, stats.visited.data(), cur * sizeof(uint32_t));
+    if (out_sd) std::memcpy(out_sd, stats.distances.data(), cur * sizeof(uint32_t));
+    if (out_iso) *out_iso = iso;
+    return 0;
+}
+
+// hier_qsearchAll (HNSW/base/hier_beamSearch.h:9-92) over a hierarchical graph with entry sp:
+// root ids of frontier[0:k], the level-0 search's visited and distance counts.
+template <typename T>
+int hnsw_search_t(uint32_t dims, int metric, const void *base, uint64_t n, const uint32_t *graph, uint32_t R,
+                  const int64_t *pre, uint64_t cur, uint64_t sp, const void *queries, uint32_t nq, uint32_t L,
+                  uint32_t k, double cut, uint32_t hbs, uint32_t k_stride, uint32_t *out_ids, uint32_t *out_count,
+                  uint32_t *out_visited, uint32_t *out_cmps)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    auto Q = make_points<T>(queries, nq, dims, metric);
+    auto G = make_graph(graph, cur, R);
+    HIdMapping hid(cur);
+    hid.cur_node_num = cur;
+    for (uint64_t i = 0; i < cur; ++i) hid.id_in_pre_level[i] = pre[i];
+    hid.set_sp(sp);
+    QueryStatic stats(nq);
+    uint32_t spv = uint32_t(sp);
+    std::function<std::pair<uint32_t *, uint32_t>(uint32_t)> get_sp = [&](uint32_t) {
+        return std::make_pair(&spv, uint32_t(1));
+    };
+    QueryParams QP(k, L, cut, cur, R);
+    auto res = hier_qsearchAll<uint32_t>(Q, Q, G, hid, B, B, stats, get_sp, QP, hbs);
+    for (uint32_t i = 0; i < nq; ++i) {
+        for (uint32_t j = 0; j < k_stride; ++j)
+            out_ids[size_t(i) * k_stride + j] = j < res[i].size() ? res[i][j] : 0xFFFFFFFFu;
+        if (out_count) out_count[i] = uint32_t(res[i].size());
+        if (out_visited) out_visited[i] = stats.visited[i];
+        if (out_cmps) out_cmps[i] = stats.distances[i];
+    }
+    return 0;
+}
+
+// Prune::maxAnglePrune (prune.h:92-154) on one candidate list, as given (no sort_candidates).
+template <typename T>
+int max_angle_prune_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t p, uint32_t *ids,
+                      float *dists, uint32_t *cnt, uint32_t R, uint32_t PR, double alpha, double cos_angle,
+                      uint32_t *out_cmps)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    std::vector<QueryNode<uint32_t>> c(*cnt);
+    for (uint32_t i = 0; i < *cnt; ++i) c[i] = QueryNode<uint32_t>(ids[i], dists[i]);
+    Prune pr(R, 1, PR);
+    size_t m = *cnt;
+    size_t cmps = pr.robustPrune(p, c.data(), m, B, alpha, cos_angle, 1);
+    for (size_t i = 0; i < m; ++i) { ids[i] = c[i].index; dists[i] = c[i].dist; }
+    *cnt = uint32_t(m);
+    if (out_cmps) *out_cmps = uint32_t(cmps);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -316,6 +404,57 @@ int nbpg_ref_build(int dtype, int metric, uint32_t dims, const void *base, uint6
     default: return 1;
     }
 #undef NBPG_REF_BUILD
+}
+
+int nbpg_ref_build_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t R, uint32_t L,
+                        uint32_t VL, uint32_t top_degree, uint32_t hbs, double alpha, double cos_angle, double m_l,
+                        uint64_t max_node, uint32_t PR, int repair_isolate, uint32_t *graph, int64_t *pre,
+                        uint64_t *out_cur, uint64_t *out_sp, uint32_t *out_sv, uint32_t *out_sd, uint64_t *out_iso,
+                        int threads)
+{
+    if (threads > 0) omp_set_num_threads(threads);
+#define NBPG_REF_HNSW(T)                                                                                        \
+    return hnsw_t<T>(dims, metric, base, n, R, L, VL, top_degree, hbs, alpha, cos_angle, m_l, max_node, PR,      \
+                     repair_isolate, graph, pre, out_cur, out_sp, out_sv, out_sd, out_iso)
+    switch (dtype) {
+    case 0: NBPG_REF_HNSW(uint8_t);
+    case 1: NBPG_REF_HNSW(int8_t);
+    case 2: NBPG_REF_HNSW(uint4_2);
+    case 3: NBPG_REF_HNSW(int4_2);
+    default: return 1;
+    }
+#undef NBPG_REF_HNSW
+}
+
+int nbpg_ref_search_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, const uint32_t *graph,
+                         uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp, const void *queries, uint32_t nq,
+                         uint32_t L, uint32_t k, double cut, uint32_t hbs, uint32_t k_stride, uint32_t *out_ids,
+                         uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps)
+{
+#define NBPG_REF_HS(T)                                                                                          \
+    return hnsw_search_t<T>(dims, metric, base, n, graph, R, pre, cur, sp, queries, nq, L, k, cut, hbs, k_stride, \
+                            out_ids, out_count, out_visited, out_cmps)
+    switch (dtype) {
+    case 0: NBPG_REF_HS(uint8_t);
+    case 1: NBPG_REF_HS(int8_t);
+    case 2: NBPG_REF_HS(uint4_2);
+    case 3: NBPG_REF_HS(int4_2);
+    default: return 1;
+    }
+#undef NBPG_REF_HS
+}
+
+int nbpg_ref_max_angle_prune(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t p,
+                             uint32_t *ids, float *dists, uint32_t *cnt, uint32_t R, uint32_t PR, double alpha,
+                             double cos_angle, uint32_t *out_cmps)
+{
+    switch (dtype) {
+    case 0: return max_angle_prune_t<uint8_t>(dims, metric, base, n, p, ids, dists, cnt, R, PR, alpha, cos_angle, out_cmps);
+    case 1: return max_angle_prune_t<int8_t>(dims, metric, base, n, p, ids, dists, cnt, R, PR, alpha, cos_angle, out_cmps);
+    case 2: return max_angle_prune_t<uint4_2>(dims, metric, base, n, p, ids, dists, cnt, R, PR, alpha, cos_angle, out_cmps);
+    case 3: return max_angle_prune_t<int4_2>(dims, metric, base, n, p, ids, dists, cnt, R, PR, alpha, cos_angle, out_cmps);
+    default: return 1;
+    }
 }
 
 }  // extern "C"

@@ -20,7 +20,7 @@ Inputs are small seeded synthetic sets.  Outputs, stored as tests/golden/*.npz:
                   (L2) and u8 (inner product) quantised rows: rerank factors 100, 3 and 0
                   (filtering mode), on a graph built by the oracle.
 
-Usage: make -C oracle ref && python tests/golden/make_golden.py [--only pca,rerank,fgim]
+Usage: make -C oracle ref && python tests/golden/make_golden.py [--only pca,rerank,fgim,hnsw]
 """
 import os
 import subprocess
@@ -134,6 +134,60 @@ def fgim_golden(tmp):
                             flags=np.array(" ".join(["--R 16 --L 24 --VL 32"] + flags)))
 
 
+def hnsw_golden(tmp, ref):
+    """.graph/.hid files written by the reference HNSW driver, the harness's per-node counters for
+    the same build, its hier_qsearchAll results on 200 queries, and Prune::maxAnglePrune on
+    candidate lists drawn from those builds."""
+    b, q = synth.u8_mixture(3000, 200, dim=32, n_centres=12, seed=7)
+    formats.write_vectors(f"{tmp}/hb.u8bin", b)
+    builds = {
+        "default": dict(flags=[], kw={}),
+        "hb3": dict(flags=["--hier_beamSize", "3", "--m_l", "0.6", "--alpha", "1.2"],
+                    kw=dict(hier_beam=3, m_l=0.6, alpha=1.2)),
+        "pr": dict(flags=["--PR", "48", "--m_l", "6", "--max_node_num", "40000"], kw=dict(PR=48, m_l=6.0,
+                                                                                        max_node=40000)),
+    }
+    for name, spec in builds.items():
+        ip = f"{tmp}/hidx_{name}"
+        subprocess.run([os.path.join(REF_DIR, "HNSW"), "--quant_base_path", f"{tmp}/hb.u8bin", "--index_path", ip,
+                        "--R", "16", "--L", "24", "--VL", "48", "--rebuild", *spec["flags"]], check=True,
+                       stdout=subprocess.DEVNULL)
+        graph_raw = open(ip + ".graph", "rb").read()
+        hid_raw = open(ip + ".hid", "rb").read()
+        g, pre, sp, sv, sd, iso = ref.build_hnsw("u8", "l2", b, R=16, L=24, VL=48, **spec["kw"])
+        hb = spec["kw"].get("hier_beam", 1)
+        ids, cnt, vis, cm = ref.search_hnsw("u8", "l2", b, g, pre, sp, q, L=24, k=10, hier_beam=hb)
+        np.savez_compressed(f"{HERE}/hnsw_{name}.npz", base=b, queries=q, graph_file=np.frombuffer(graph_raw, np.uint8),
+                            hid_file=np.frombuffer(hid_raw, np.uint8), stat_visited=sv, stat_dist=sd, isolated=iso,
+                            q_ids=ids, q_count=cnt, q_visited=vis, q_cmps=cm, hier_beam=hb,
+                            flags=np.array(" ".join(["--R 16 --L 24 --VL 48"] + spec["flags"])))
+    # maxAnglePrune on the visited-like lists of a search over the default build's level-0 rows
+    r = np.random.default_rng(5)
+    cases = []
+    for t in range(60):
+        p = int(r.integers(0, len(b)))
+        m = int(r.integers(1, 48))
+        cand = r.choice(np.delete(np.arange(len(b)), p), size=m, replace=False).astype(np.uint32)
+        d = np.array([ref.distance("u8", "l2", b[p], b[c]) for c in cand], np.float32)
+        o = np.lexsort((cand, d))
+        cand, d = cand[o], d[o]
+        alpha, cosa = [(1.2, 0.0), (1.0, 0.5), (1.1, 0.8), (0.0, 0.6)][t % 4]
+        R = [8, 16, 32][t % 3]
+        oi, od, oc = ref.max_angle_prune("u8", "l2", b, p, cand, d, R, 48, alpha, cosa)
+        cases.append((p, cand, d, alpha, cosa, R, oi, od, oc))
+    np.savez_compressed(f"{HERE}/max_angle_prune.npz", base=b,
+                        p=np.array([c[0] for c in cases], np.uint32),
+                        alpha=np.array([c[3] for c in cases]), cos=np.array([c[4] for c in cases]),
+                        R=np.array([c[5] for c in cases], np.uint32),
+                        cmps=np.array([c[8] for c in cases], np.uint32),
+                        cand=np.array([np.pad(c[1], (0, 48 - len(c[1])), constant_values=0xFFFFFFFF) for c in cases]),
+                        dist=np.array([np.pad(c[2], (0, 48 - len(c[2]))) for c in cases]),
+                        n_cand=np.array([len(c[1]) for c in cases], np.uint32),
+                        out=np.array([np.pad(c[6], (0, 48 - len(c[6])), constant_values=0xFFFFFFFF) for c in cases]),
+                        out_d=np.array([np.pad(c[7], (0, 48 - len(c[7]))) for c in cases]),
+                        n_out=np.array([len(c[6]) for c in cases], np.uint32))
+
+
 def main():
     if not (os.path.exists(REF_COMPGT) and os.path.exists(REF_VAMANA) and reference()):
         sys.exit("build the reference first: make -C oracle ref")
@@ -146,6 +200,8 @@ def main():
         rerank_golden()
     if only is None or "fgim" in only:
         fgim_golden(tmp)
+    if only is None or "hnsw" in only:
+        hnsw_golden(tmp, ref)
     if only is not None:
         print("golden vectors written to", HERE)
         return

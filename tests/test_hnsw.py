@@ -1,0 +1,85 @@
+"""The HNSW oracle (build, hierarchical search, maxAnglePrune) against the golden vectors:
+.graph/.hid files written by the reference's HNSW driver, and the reference's per-node
+counters, hier_qsearchAll results and Prune::maxAnglePrune outputs through its own code."""
+import os
+
+import numpy as np
+import pytest
+
+from nbpg_gb300 import formats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+G = os.path.join(HERE, "golden")
+
+
+def _kw(flags: str) -> dict:
+    t = flags.split()
+    kw = {}
+    names = {"--hier_beamSize": ("hier_beam", int), "--m_l": ("m_l", float), "--alpha": ("alpha", float),
+             "--PR": ("PR", int), "--max_node_num": ("max_node", int), "--cos_angle": ("cos_angle", float),
+             "--top_degree": ("top_degree", int)}
+    for i, a in enumerate(t):
+        if a in names:
+            k, f = names[a]
+            kw[k] = f(t[i + 1])
+    return kw
+
+
+def _files(tmp_path, g, pre, sp, max_node):
+    gp, hp = str(tmp_path / "x.graph"), str(tmp_path / "x.hid")
+    formats.write_graph(gp, g)
+    formats.write_hid(hp, max_node, sp, pre)
+    return open(gp, "rb").read(), open(hp, "rb").read()
+
+
+@pytest.mark.parametrize("name", ["default", "hb3", "pr"])
+def test_oracle_hnsw_build_writes_reference_files(oracle_lib, tmp_path, name):
+    z = np.load(os.path.join(G, f"hnsw_{name}.npz"))
+    kw = _kw(str(z["flags"]))
+    g, pre, sp, sv, sd, iso = oracle_lib.build_hnsw("u8", "l2", z["base"], R=16, L=24, VL=48, **kw)
+    _, mn = oracle_lib.hnsw_sizes(len(z["base"]), 16, kw.get("m_l", 0.0), kw.get("max_node", 0))
+    graph_raw, hid_raw = _files(tmp_path, g, pre, sp, mn)
+    assert graph_raw == z["graph_file"].tobytes()
+    assert hid_raw == z["hid_file"].tobytes()
+    assert np.array_equal(sv, z["stat_visited"]) and np.array_equal(sd, z["stat_dist"])
+    assert iso == int(z["isolated"])
+
+
+@pytest.mark.parametrize("name", ["default", "hb3", "pr"])
+def test_oracle_hnsw_search_matches_reference(oracle_lib, tmp_path, name):
+    z = np.load(os.path.join(G, f"hnsw_{name}.npz"))
+    gp, hp = str(tmp_path / "g.graph"), str(tmp_path / "g.hid")
+    open(gp, "wb").write(z["graph_file"].tobytes())
+    open(hp, "wb").write(z["hid_file"].tobytes())
+    g = formats.read_graph(gp)
+    _, cur, sp, pre = formats.read_hid(hp)
+    assert g.shape[0] == cur
+    ids, cnt, vis, cm = oracle_lib.search_hnsw("u8", "l2", z["base"], g, pre, sp, z["queries"], L=24, k=10,
+                                               hier_beam=int(z["hier_beam"]))
+    assert np.array_equal(ids, z["q_ids"]) and np.array_equal(cnt, z["q_count"])
+    assert np.array_equal(vis, z["q_visited"]) and np.array_equal(cm, z["q_cmps"])
+
+
+def test_oracle_max_angle_prune_matches_reference(oracle_lib):
+    z = np.load(os.path.join(G, "max_angle_prune.npz"))
+    for i in range(len(z["p"])):
+        m = int(z["n_cand"][i])
+        ids, d, cm = oracle_lib.max_angle_prune("u8", "l2", z["base"], int(z["p"][i]), z["cand"][i][:m],
+                                                z["dist"][i][:m], int(z["R"][i]), 48, float(z["alpha"][i]),
+                                                float(z["cos"][i]))
+        no = int(z["n_out"][i])
+        assert np.array_equal(ids, z["out"][i][:no]) and np.array_equal(d, z["out_d"][i][:no]), i
+        assert cm == int(z["cmps"][i]), i
+
+
+def test_oracle_hnsw_refusals(oracle_lib):
+    z = np.load(os.path.join(G, "hnsw_default.npz"))
+    # the reference aborts in maxAnglePrune: the first insert's only candidate is itself
+    with pytest.raises(RuntimeError, match="3"):
+        oracle_lib.build_hnsw("u8", "l2", z["base"], R=16, L=24, VL=48, PR=48)
+    # more nodes than the capacity (the reference writes past its arrays)
+    with pytest.raises(RuntimeError, match="2"):
+        oracle_lib.build_hnsw("u8", "l2", z["base"], R=16, L=24, VL=48, m_l=8.0)
+    # a visited cap of 2L above VL overruns the reference's per-cell buffers
+    with pytest.raises(RuntimeError, match="1"):
+        oracle_lib.build_hnsw("u8", "l2", z["base"], R=16, L=30, VL=48)
