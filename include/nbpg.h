@@ -355,6 +355,61 @@ nbpg_status nbpg_build(nbpg_index *idx, const nbpg_build_params *params, nbpg_bu
 nbpg_status nbpg_build_fgim(nbpg_index *idx, const nbpg_build_params *params, nbpg_build_stats *stats,
                             uint32_t *per_node_visited, uint32_t *per_node_dists);
 
+/* ---------------------------------------------------------------------------
+ * HNSW (data_tools/ANNs/HNSW): a hierarchy of graphs over the index's vectors in which every
+ * (vector, level) pair is a node with its own adjacency row.  A vector of level l takes l + 1
+ * consecutive node ids from the top down; id_in_pre_level links each node to the one below it
+ * and the level-0 node to -1 - vector id (HIdMapping, HNSW/base/hier_idmapping.h:9-107).
+ * ------------------------------------------------------------------------- */
+typedef struct nbpg_hnsw nbpg_hnsw;
+
+/* The HNSW driver's build flags (HNSW.cpp:12-72). */
+typedef struct nbpg_hnsw_params {
+    uint32_t L;             /* --L: beam on the levels an insert joins */
+    uint32_t VL;            /* --VL: candidate cap and reverse-edge group cap; 2 * L <= VL */
+    uint32_t top_degree;    /* --top_degree: 0 = R */
+    uint32_t hier_beam;     /* --hier_beamSize: beam above an insert's level and entry points per level */
+    uint32_t PR;            /* --PR: > 0 selects maxAnglePrune (prune.h:92-154); PR >= 2 * L */
+    double alpha;           /* --alpha at level 0 (1 above) */
+    double cos_angle;       /* --cos_angle: 0 = off */
+    double m_l;             /* --m_l: level factor; <= 1e-5 = 1 / ln(R) */
+    uint64_t max_node_num;  /* --max_node_num: node capacity; 0 = (exp(-1 / m_l) * 2 + 1) * n */
+    int32_t repair_isolate; /* DFS::repair_isolate_node over the hierarchy (dfs.h:217-262) */
+} nbpg_hnsw_params;
+
+/* m_l and the node capacity the driver derives when they are unset (HNSW.cpp:62-72). */
+nbpg_status nbpg_hnsw_sizes(uint64_t n, uint32_t max_degree, double m_l, uint64_t max_node_num, double *out_m_l,
+                            uint64_t *out_max_node_num);
+
+/* HNSWIndex::batch_insert (HNSW/base/hnsw.h:42-279) over all of idx's vectors, then the
+ * repair; replaces HNSW.cpp:184-197.  per_node_visited / per_node_dists (node-capacity
+ * entries each, may be NULL) receive the BuildStats counters of the nodes.  idx must outlive
+ * the result.  INVALID_ARG where the reference aborts (maxAnglePrune meeting the node itself,
+ * which with PR > 0 happens on the first insert unless m_l lifts it to level 1). */
+nbpg_status nbpg_hnsw_build(nbpg_index *idx, const nbpg_hnsw_params *params, nbpg_hnsw **out,
+                            nbpg_build_stats *stats, uint32_t *per_node_visited, uint32_t *per_node_dists);
+
+/* Node capacity, node count, entry node (HIdMapping::sp) and top level. */
+nbpg_status nbpg_hnsw_info(const nbpg_hnsw *h, uint64_t *max_node_num, uint64_t *node_count, uint64_t *entry,
+                           uint32_t *max_level);
+
+/* The node_count adjacency rows ([degree, ids...], R + 1 u32 each: the .graph rows) and
+ * id_in_pre_level (the .hid body); either may be NULL. */
+nbpg_status nbpg_hnsw_get(nbpg_hnsw *h, uint32_t *rows, int64_t *id_in_pre_level);
+
+/* A hierarchy read back from .graph / .hid files (HNSW.cpp:278-283). */
+nbpg_status nbpg_hnsw_load(nbpg_index *idx, uint64_t max_node_num, uint64_t node_count, uint64_t entry,
+                           const uint32_t *rows, const int64_t *id_in_pre_level, nbpg_hnsw **out);
+
+/* hier_qsearchAll (HNSW/base/hier_beamSearch.h:9-92) with params' k, L, cut, limit and
+ * degree_limit: vector ids of frontier[0:k] per query; visited / distance counts of the
+ * level-0 search (the reference's QueryStatic). */
+nbpg_status nbpg_hnsw_search(nbpg_hnsw *h, const void *queries, uint32_t nq, const nbpg_search_params *params,
+                             uint32_t hier_beam, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
+                             uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps);
+
+nbpg_status nbpg_hnsw_destroy(nbpg_hnsw *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,12 @@ class ServeConfig(C.Structure):
                 ("queue_capacity", C.c_uint32), ("memory_budget_bytes", C.c_uint64)]
 
 
+class HnswParams(C.Structure):
+    _fields_ = [("L", C.c_uint32), ("VL", C.c_uint32), ("top_degree", C.c_uint32), ("hier_beam", C.c_uint32),
+                ("PR", C.c_uint32), ("alpha", C.c_double), ("cos_angle", C.c_double), ("m_l", C.c_double),
+                ("max_node_num", C.c_uint64), ("repair_isolate", C.c_int32)]
+
+
 class BuildStats(C.Structure):
     _fields_ = [("isolated", C.c_uint64), ("seconds", C.c_double), ("batches", C.c_uint64)]
 
@@ -123,6 +129,15 @@ def lib() -> C.CDLL:
     L.nbpg_f32_to_u8.argtypes = [_f32p, C.c_uint64, C.c_uint32, _vp, C.c_int32]
     L.nbpg_build.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
     L.nbpg_build_fgim.argtypes = [_vp, C.POINTER(BuildParams), C.POINTER(BuildStats), _u32p, _u32p]
+    _u64p = C.POINTER(C.c_uint64)
+    L.nbpg_hnsw_sizes.argtypes = [C.c_uint64, C.c_uint32, C.c_double, C.c_uint64, C.POINTER(C.c_double), _u64p]
+    L.nbpg_hnsw_build.argtypes = [_vp, C.POINTER(HnswParams), C.POINTER(_vp), C.POINTER(BuildStats), _u32p, _u32p]
+    L.nbpg_hnsw_info.argtypes = [_vp, _u64p, _u64p, _u64p, _u32p]
+    L.nbpg_hnsw_get.argtypes = [_vp, _u32p, C.POINTER(C.c_int64)]
+    L.nbpg_hnsw_load.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint64, _u32p, C.POINTER(C.c_int64), C.POINTER(_vp)]
+    L.nbpg_hnsw_search.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), C.c_uint32, C.c_uint32, _u32p,
+                                   _f32p, _u32p, _u32p, _u32p]
+    L.nbpg_hnsw_destroy.argtypes = [_vp]
     _lib = L
     return L
 

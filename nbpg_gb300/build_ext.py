@@ -64,17 +64,18 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
 CLI = {"nbpg_vamana": ("vamana.cpp", []), "nbpg_fgim": ("vamana.cpp", ["-DNBPG_FGIM"]),
        "nbpg_compgt": ("compgt.cpp", []), "nbpg_pcacompress": ("pcacompress.cpp", []),
-       "nbpg_fmtconv": ("fmtconv.cpp", [])}
+       "nbpg_fmtconv": ("fmtconv.cpp", []), "nbpg_hnsw": ("hnsw.cpp", [])}
 
 
 def _build_cli() -> None:
-    """The Vamana/CompGT drop-in executables (host C++ over the C ABI)."""
+    """The drop-in executables for the reference's drivers (host C++ over the C ABI)."""
     cxx = os.environ.get("CXX", "g++")
     src_dir = os.path.join(HERE, "cli")
     for exe, (src, defs) in CLI.items():
         out = os.path.join(OUT, exe)
         srcp = os.path.join(src_dir, src)
-        deps = [srcp, os.path.join(src_dir, "flags.h"), os.path.join(INCLUDE, "nbpg.h"), LIB]
+        deps = [srcp, os.path.join(src_dir, "flags.h"), os.path.join(src_dir, "common.h"), os.path.join(INCLUDE, "nbpg.h"),
+                LIB]
         if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
             continue
         cmd = [cxx, "-O2", "-std=c++17", *defs, srcp, f"-I{INCLUDE}", f"-L{OUT}", "-lnbpg_gb300",

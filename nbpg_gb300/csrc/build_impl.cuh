@@ -203,111 +203,178 @@ __device__ void fgim_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t
                                  ns ? st.vs : 0u, lane);
 }
 
-// sort_candidates (prune.h:50-74) on pool[0, np), RobustPrune (limitedSimilarityPrune,
-// prune.h:159-209) with the node's alpha / cos, and the outputs of one insert: the pruned
-// list, the BuildStats counters (search_cmps + the prune's distances, nvis) and, in a
-// popularity pass, one visit per entry of the visited list vis[0, vs).
-template <int DT, int MET, int VPL>
-__device__ void prune_and_emit(const BuildArgs &B, uint32_t t, uint32_t index, uint64_t *pool, uint32_t np,
-                               uint8_t *alive, uint32_t search_cmps, uint32_t nvis, const uint64_t *vis, uint32_t vs,
-                               int lane)
+// sort_candidates (prune.h:50-74) on pool[0, np): p forced last, sort, drop repeats, drop p.
+// Returns the new count.
+__device__ __forceinline__ uint32_t sort_candidates_dev(uint64_t *pool, uint32_t np, uint32_t index, int lane)
 {
-    const SearchArgs &a = B.s;
-    const uint32_t R = B.R;
-    uint32_t rp = 0;
-    // sort_candidates (prune.h:50-74): p forced last, sort, drop repeats, drop p
     const uint64_t pkey = (uint64_t(f2ord(3.402823466e38f)) << 32) | index;
     for (uint32_t i = lane; i < np; i += 32)
         if (key_id(pool[i]) == index) pool[i] = pkey;
     __syncwarp();
     sort_keys(pool, np, lane);
-    {
-        uint32_t outc = 0;
-        uint64_t carry = kKeyMax;
-        for (uint32_t base = 0; base < np; base += 32) {
-            const uint32_t i = base + lane;
-            const uint64_t v = i < np ? pool[i] : kKeyMax;
-            uint64_t prev = __shfl_up_sync(kFull, v, 1);
-            if (lane == 0) prev = carry;
-            carry = __shfl_sync(kFull, v, 31);
-            const bool keep = i < np && v != prev;
-            const unsigned m = __ballot_sync(kFull, keep);
-            __syncwarp();
-            if (keep) pool[outc + __popc(m & lanemask_lt())] = v;
-            outc += __popc(m);
-            __syncwarp();
-        }
-        np = outc;
-        if (np > 0 && key_id(pool[np - 1]) == index) --np;
-    }
-
-    // RobustPrune (limitedSimilarityPrune, prune.h:159-209)
-    const double alpha = double(B.alpha_node ? B.alpha_node[index] : B.alpha_all);
-    const double cosa = double(B.cos_node ? B.cos_node[index] : B.cos_all);
-    uint32_t sel = 0;
-    if (alpha <= kPruneEps && cosa <= kPruneEps) {
-        sel = np < R ? np : R;
-    } else {
-        for (uint32_t i = lane; i < np; i += 32) alive[i] = 1;
+    uint32_t outc = 0;
+    uint64_t carry = kKeyMax;
+    for (uint32_t base = 0; base < np; base += 32) {
+        const uint32_t i = base + lane;
+        const uint64_t v = i < np ? pool[i] : kKeyMax;
+        uint64_t prev = __shfl_up_sync(kFull, v, 1);
+        if (lane == 0) prev = carry;
+        carry = __shfl_sync(kFull, v, 31);
+        const bool keep = i < np && v != prev;
+        const unsigned m = __ballot_sync(kFull, keep);
         __syncwarp();
-        const uint32_t lpr = a.lpr, rows_per = 32u / lpr;
-        const uint32_t grp = uint32_t(lane) / lpr, lq = uint32_t(lane) % lpr;
-        uint32_t scan = 0;
-        while (sel < R && scan < np) {
-            const uint64_t sk = pool[scan];
-            ++scan;
-            if (!alive[scan - 1]) continue;  // pruned (index -1 in the reference)
-            const uint32_t ps = key_id(sk);
-            const float dps = key_dist(sk);
-            __syncwarp();
-            if (lane == 0) pool[sel] = sk;
-            ++sel;
-            __syncwarp();
-            uint4 pv[VPL];
-            load_row_regs<VPL>(a, ps, pv, lane);
-            uint32_t cm = 0;
-            for (uint32_t r0 = scan; r0 < np; r0 += rows_per * 4) {
-                uint4 bv[4][VPL];
-                uint32_t pos[4];
-                bool live[4];
+        if (keep) pool[outc + __popc(m & lanemask_lt())] = v;
+        outc += __popc(m);
+        __syncwarp();
+    }
+    if (outc > 0 && key_id(pool[outc - 1]) == index) --outc;
+    return outc;
+}
+
+// Distances between the row held in pv (node ps) and the candidates pool[i], i in [from, np),
+// whose `alive` flag is set (all of them when alive is null): the pair distance goes to fn(i, d)
+// on the group leader.  Returns how many were computed (on every lane).
+template <int DT, int MET, int VPL, class Fn>
+__device__ __forceinline__ uint32_t pair_dists(const SearchArgs &a, const uint4 (&pv)[VPL], const uint64_t *pool,
+                                               uint32_t from, uint32_t np, const uint8_t *alive, int lane, Fn fn)
+{
+    const uint32_t lpr = a.lpr, rows_per = 32u / lpr;
+    const uint32_t grp = uint32_t(lane) / lpr, lq = uint32_t(lane) % lpr;
+    uint32_t cm = 0;
+    for (uint32_t r0 = from; r0 < np; r0 += rows_per * 4) {
+        uint4 bv[4][VPL];
+        uint32_t pos[4];
+        bool live[4];
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    pos[p] = r0 + p * rows_per + grp;
-                    live[p] = pos[p] < np && alive[pos[p]];
-                    const uint32_t id = live[p] ? key_id(pool[pos[p]]) : 0u;
+        for (int p = 0; p < 4; ++p) {
+            pos[p] = r0 + p * rows_per + grp;
+            live[p] = pos[p] < np && (!alive || alive[pos[p]]);
+            const uint32_t id = live[p] ? key_id(pool[pos[p]]) : 0u;
 #pragma unroll
-                    for (int v = 0; v < VPL; ++v) {
-                        const uint32_t c = lq + v * lpr;
-                        bv[p][v] = (live[p] && c < a.vecs)
-                                       ? __ldg(reinterpret_cast<const uint4 *>(a.base + size_t(id) * a.row_stride) + c)
-                                       : make_uint4(0, 0, 0, 0);
-                    }
-                }
-#pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    uint32_t acc = 0;
-#pragma unroll
-                    for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], pv[v], acc);
-                    for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-                    if (lq == 0 && live[p]) {
-                        ++cm;
-                        const float dsp = finish_dist<DT, MET>(acc);
-                        const float dpp = key_dist(pool[pos[p]]);
-                        bool pruned = false;
-                        if (alpha > kPruneEps && alpha * double(dsp) <= double(dpp)) pruned = true;
-                        else if (cosa > kPruneEps && double(cos_at_p(dps, dpp, dsp)) > cosa) pruned = true;
-                        if (pruned) alive[pos[p]] = 0;
-                    }
-                }
-                __syncwarp();
+            for (int v = 0; v < VPL; ++v) {
+                const uint32_t c = lq + v * lpr;
+                bv[p][v] = (live[p] && c < a.vecs)
+                               ? __ldg(reinterpret_cast<const uint4 *>(a.base + size_t(id) * a.row_stride) + c)
+                               : make_uint4(0, 0, 0, 0);
             }
-            for (uint32_t o = 16; o > 0; o >>= 1) cm += __shfl_xor_sync(kFull, cm, o);
-            rp += cm;
         }
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            uint32_t acc = 0;
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], pv[v], acc);
+            for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+            if (lq == 0 && live[p]) {
+                ++cm;
+                fn(pos[p], finish_dist<DT, MET>(acc));
+            }
+        }
+        __syncwarp();
+    }
+    for (uint32_t o = 16; o > 0; o >>= 1) cm += __shfl_xor_sync(kFull, cm, o);
+    return cm;
+}
+
+// RobustPrune (limitedSimilarityPrune, prune.h:159-209) on pool[0, np) in place: the selected
+// entries end in pool[0, sel).  A candidate equal to p is passed over as a pivot (the
+// reference's p_star == p check).  Adds the pair distances computed to rp.
+template <int DT, int MET, int VPL>
+__device__ uint32_t limited_prune_dev(const SearchArgs &a, uint64_t *pool, uint32_t np, uint8_t *alive, uint32_t p,
+                                      uint32_t R, double alpha, double cosa, uint32_t &rp, int lane)
+{
+    if (alpha <= kPruneEps && cosa <= kPruneEps) return np < R ? np : R;
+    for (uint32_t i = lane; i < np; i += 32) alive[i] = 1;
+    __syncwarp();
+    uint32_t sel = 0, scan = 0;
+    while (sel < R && scan < np) {
+        const uint64_t sk = pool[scan];
+        ++scan;
+        const uint32_t ps = key_id(sk);
+        if (!alive[scan - 1] || ps == p) continue;  // pruned (index -1 in the reference), or p itself
+        const float dps = key_dist(sk);
+        __syncwarp();
+        if (lane == 0) pool[sel] = sk;
+        ++sel;
+        __syncwarp();
+        uint4 pv[VPL];
+        load_row_regs<VPL>(a, ps, pv, lane);
+        rp += pair_dists<DT, MET, VPL>(a, pv, pool, scan, np, alive, lane, [&](uint32_t i, float dsp) {
+            const float dpp = key_dist(pool[i]);
+            bool pruned = false;
+            if (alpha > kPruneEps && alpha * double(dsp) <= double(dpp)) pruned = true;
+            else if (cosa > kPruneEps && double(cos_at_p(dps, dpp, dsp)) > cosa) pruned = true;
+            if (pruned) alive[i] = 0;
+        });
     }
     __syncwarp();
+    return sel;
+}
 
-    // results
+// Prune::maxAnglePrune (prune.h:92-154) on pool[0, np) in place, step for step: each round's
+// pivot is the entry in slot `sel` (read through the slot, so a swap into it changes the
+// distance the cosine uses), every later entry's score is its largest cosine to a pivot,
+// survivors of survives_prune_enhanced (prune.h:240-249) are compacted after the pivot slot
+// and one whose score is below the slot's is swapped into it.  Pair distances of a round are
+// computed by the warp first (an entry is read where it stood at the round's start, which is
+// where the sequential walk, run by lane 0, reaches it).  score and dsp hold np floats each.
+// Returns the selected count, or ~0u where the reference aborts (a pivot equal to p).
+template <int DT, int MET, int VPL>
+__device__ uint32_t max_angle_prune_dev(const SearchArgs &a, uint64_t *pool, uint32_t np, float *score, float *dsp,
+                                        uint32_t p, uint32_t R, double alpha, double cosa, uint32_t &rp, int lane)
+{
+    if (alpha <= kPruneEps && cosa <= kPruneEps) return ~0u;
+    for (uint32_t i = lane; i < np; i += 32) score[i] = -2.f;
+    __syncwarp();
+    uint32_t sel = 0, n = np;
+    while (sel < R && sel < n) {
+        const uint32_t ps = key_id(pool[sel]);
+        if (ps == p) return ~0u;
+        ++sel;
+        uint4 pv[VPL];
+        load_row_regs<VPL>(a, ps, pv, lane);
+        rp += pair_dists<DT, MET, VPL>(a, pv, pool, sel, n, nullptr, lane, [&](uint32_t i, float d) { dsp[i] = d; });
+        __syncwarp();
+        uint32_t se = sel;
+        if (lane == 0) {
+            for (uint32_t i = sel; i < n; ++i) {
+                const float dpp = key_dist(pool[i]);
+                const float cv = cos_at_p(key_dist(pool[sel - 1]), dpp, dsp[i]);
+                if (score[i] < cv) score[i] = cv;
+                const bool keep = (alpha > kPruneEps && alpha * double(dsp[i]) > double(dpp)) ||
+                                  (cosa > kPruneEps && double(cv) < cosa);
+                if (!keep) continue;
+                if (i > se) {
+                    const uint64_t tk = pool[se]; pool[se] = pool[i]; pool[i] = tk;
+                    const float ts = score[se]; score[se] = score[i]; score[i] = ts;
+                }
+                if (score[se] < score[sel - 1]) {
+                    const uint64_t tk = pool[se]; pool[se] = pool[sel - 1]; pool[sel - 1] = tk;
+                    const float ts = score[se]; score[se] = score[sel - 1]; score[sel - 1] = ts;
+                }
+                ++se;
+            }
+        }
+        n = __shfl_sync(kFull, se, 0);
+        __syncwarp();
+    }
+    return sel;
+}
+
+// sort_candidates and RobustPrune with the node's alpha / cos on pool[0, np), then the outputs
+// of one insert: the pruned list, the BuildStats counters (search_cmps + the prune's
+// distances, nvis) and, in a popularity pass, one visit per entry of the visited list vis[0, vs).
+template <int DT, int MET, int VPL>
+__device__ void prune_and_emit(const BuildArgs &B, uint32_t t, uint32_t index, uint64_t *pool, uint32_t np,
+                               uint8_t *alive, uint32_t search_cmps, uint32_t nvis, const uint64_t *vis, uint32_t vs,
+                               int lane)
+{
+    const uint32_t R = B.R;
+    uint32_t rp = 0;
+    np = sort_candidates_dev(pool, np, index, lane);
+    const double alpha = double(B.alpha_node ? B.alpha_node[index] : B.alpha_all);
+    const double cosa = double(B.cos_node ? B.cos_node[index] : B.cos_all);
+    const uint32_t sel = limited_prune_dev<DT, MET, VPL>(B.s, pool, np, alive, index, R, alpha, cosa, rp, lane);
+
     for (uint32_t j = lane; j < sel; j += 32) {
         B.res_ids[size_t(t) * R + j] = key_id(pool[j]);
         B.res_d[size_t(t) * R + j] = key_dist(pool[j]);
@@ -340,7 +407,7 @@ __global__ void __launch_bounds__(512) build_search_prune_kernel(BuildArgs B)
 }
 
 // G[index] = pruned list; slots past the degree zeroed.
-__global__ void forward_write_kernel(BuildArgs B)
+static __global__ void forward_write_kernel(BuildArgs B)
 {
     const uint32_t t = blockIdx.x;
     if (t >= B.bs) return;
@@ -351,7 +418,7 @@ __global__ void forward_write_kernel(BuildArgs B)
         row[j] = j == 0 ? cnt : (j - 1 < cnt ? B.res_ids[size_t(t) * B.R + j - 1] : 0u);
 }
 
-__global__ void rev_count_kernel(BuildArgs B)
+static __global__ void rev_count_kernel(BuildArgs B)
 {
     const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (e >= size_t(B.bs) * B.R) return;
@@ -360,7 +427,7 @@ __global__ void rev_count_kernel(BuildArgs B)
     B.rank[e] = atomicAdd(&B.cnt_node[B.res_ids[e]], 1u);
 }
 
-__global__ void rev_alloc_kernel(BuildArgs B)
+static __global__ void rev_alloc_kernel(BuildArgs B)
 {
     const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (e >= size_t(B.bs) * B.R) return;
@@ -371,7 +438,7 @@ __global__ void rev_alloc_kernel(BuildArgs B)
     B.grp_target[atomicAdd(&B.bump[1], 1u)] = target;
 }
 
-__global__ void rev_scatter_kernel(BuildArgs B)
+static __global__ void rev_scatter_kernel(BuildArgs B)
 {
     const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (e >= size_t(B.bs) * B.R) return;

@@ -138,12 +138,9 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     NBPG_CHECK_ARG(sp && nsp >= 1 && nsp <= P->L && nsp <= 256, "need 1..min(L,256) start points");
     NBPG_CHECK_ARG(R <= 128, "max_degree above 128 is not supported");
     NBPG_CHECK_ARG(P->kernel == NBPG_KERNEL_BATCHED || P->kernel == NBPG_KERNEL_PLAIN, "unknown kernel");
-    {
-        std::vector<uint32_t> s(sp, sp + nsp);
-        for (uint32_t v : s) NBPG_CHECK_ARG(v < n, "start point out of range");
-        std::sort(s.begin(), s.end());
-        NBPG_CHECK_ARG(std::adjacent_find(s.begin(), s.end()) == s.end(), "start points must be distinct");
-    }
+    // repeated start points are accepted as the reference accepts them (the frontier then holds
+    // copies of a key; query_params.h:204-221, beamSearch.h:154-160)
+    for (uint32_t i = 0; i < nsp; ++i) NBPG_CHECK_ARG(sp[i] < n, "start point out of range");
     uint32_t vecs, lpr, vpl;
     row_geometry(idx->row_stride, P->lane_width, vecs, lpr, vpl);
     NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");

@@ -76,6 +76,11 @@ struct SearchArgs {
     uint32_t emit_factor;   // emit frontier[0 : min(k * emit_factor, fs)] instead of [0 : k)
     uint32_t emit_visited;  // LIST mode: emit the final visited list, count its insertions
     uint32_t *out_fs;       // frontier size at the end of each query (may be null)
+    uint32_t filter_L;      // beam that sizes the visited filter when it differs from the search's
+                            // own (HNSW's upper levels search with beam hier_beamSize in a cell
+                            // made for L); 0 = the search's beam
+    uint32_t keep_filter;   // 1: the visited filter is not cleared, it carries over from an earlier
+                            // search in the same cell (HNSW's levels of one insert, hnsw.h:179-190)
     SlotLayout lay;
 };
 
@@ -217,6 +222,20 @@ __device__ __forceinline__ bool contains(const uint64_t *s, uint32_t n, uint64_t
     return p < n && s[p] == key;
 }
 
+// std::set_difference of sorted multisets (beamSearch.h:154-160) for frontier entry i: the
+// r-th copy (from 0) of a key among the frontier's equal keys stays unvisited when the visited
+// list holds at most r copies.  Copies arise only from repeated start points (an HNSW level's
+// entry points can repeat a node reached through an edge between levels).
+__device__ __forceinline__ bool unvisited_multi(const uint64_t *fr, uint32_t i, const uint64_t *vis, uint32_t vs)
+{
+    const uint64_t key = fr[i];
+    const uint32_t r = i - lower_count(fr, i, key);
+    const uint32_t lo = lower_count(vis, vs, key);
+    uint32_t c = 0;
+    while (lo + c < vs && vis[lo + c] == key) ++c;
+    return r >= c;
+}
+
 // Sort the candidates, drop repeats (std::unique after the sort, beamSearch.h:128-130)
 // and drop those already in the frontier (set_union keeps the frontier's copy,
 // beamSearch.h:132-135).  Returns the count of what is left, sorted in cand[].
@@ -275,7 +294,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
                                    uint32_t gslot, int lane, uint32_t self)
 {
     const SlotLayout &lay = a.lay;
-    const uint32_t S = filter_slots_for(L);
+    const uint32_t S = filter_slots_for(a.filter_L ? a.filter_L : L);
     const uint32_t smask = S - 1;
     SearchState st{};
     st.smask = smask;
@@ -308,8 +327,10 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     }
 
     // clear the visited filter (query_params.h:173-180)
-    for (uint32_t i = lane; i < S; i += 32) H[i] = kNoId;
-    __syncwarp();
+    if (!a.keep_filter) {
+        for (uint32_t i = lane; i < S; i += 32) H[i] = kNoId;
+        __syncwarp();
+    }
 
     // init_starting_points (query_params.h:204-221)
     warp_row_keys<DT, MET, VPL>(a, qv, sp, nsp, fr0, lane);
@@ -325,6 +346,17 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         unv[i] = uint16_t(i);
     }
     __syncwarp();
+    // repeated start points: the frontier and visited list then hold copies of a key, and
+    // frontier \ visited takes multiset semantics (the flags of FLAG mode track copies per
+    // position already)
+    bool dup = false;
+    (void)dup;
+    if constexpr (LIST) {
+        for (uint32_t base = 0; base < nsp; base += 32) {
+            const uint32_t i = base + lane;
+            dup |= __any_sync(kFull, i > 0 && i < nsp && fr0[i] == fr0[i - 1]);
+        }
+    }
 
     int b = 0;
     uint32_t fs = nsp;
@@ -441,7 +473,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
                 const uint32_t i = base + lane;
                 bool un = false;
                 if (i < fs) {
-                    if constexpr (LIST) un = !contains(vis, vs, frb[i]);
+                    if constexpr (LIST) un = dup ? unvisited_multi(frb, i, vis, vs) : !contains(vis, vs, frb[i]);
                     else un = flb[i] == 0;
                 }
                 const unsigned m = __ballot_sync(kFull, un);
@@ -506,7 +538,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             const uint32_t i = base + lane;
             bool un = false;
             if (i < fs) {
-                if constexpr (LIST) un = !contains(vis, vs, frn[i]);
+                if constexpr (LIST) un = dup ? unvisited_multi(frn, i, vis, vs) : !contains(vis, vs, frn[i]);
                 else un = fln[i] == 0;
             }
             const unsigned m = __ballot_sync(kFull, un);

@@ -99,12 +99,9 @@ extern "C" nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint
     NBPG_CHECK_ARG(P->L >= 1 && P->L <= 1024 && P->k >= 1 && P->k <= P->L && k_stride >= P->k,
                    "k must be in [1, L], L in [1, 1024], k_stride >= k");
     NBPG_CHECK_ARG(P->kernel == NBPG_KERNEL_BATCHED || P->kernel == NBPG_KERNEL_PLAIN, "unknown kernel");
-    {
-        std::vector<uint32_t> s(start_points, start_points + n_start);
-        for (uint32_t v : s) NBPG_CHECK_ARG(v < n, "start point out of range");
-        std::sort(s.begin(), s.end());
-        NBPG_CHECK_ARG(std::adjacent_find(s.begin(), s.end()) == s.end(), "start points must be distinct");
-    }
+    // repeated start points are accepted as the reference accepts them (the frontier then holds
+    // copies of a key; query_params.h:204-221, beamSearch.h:154-160)
+    for (uint32_t i = 0; i < n_start; ++i) NBPG_CHECK_ARG(start_points[i] < n, "start point out of range");
     if (nq == 0) return NBPG_OK;
 
     int device = 0;

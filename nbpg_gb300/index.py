@@ -14,7 +14,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import BuildParams, BuildStats, IndexDesc, SearchParams, check
+from ._lib import BuildParams, BuildStats, HnswParams, IndexDesc, SearchParams, check
 
 _u32p = C.POINTER(C.c_uint32)
 _f32p = C.POINTER(C.c_float)
@@ -238,6 +238,84 @@ class Index:
         sd = np.zeros(self.n, np.uint32) if with_stats else None
         check(_lib.lib().nbpg_build_fgim(self._h, C.byref(prm), C.byref(st), _p(sv), _p(sd)))
         return st, sv, sd
+
+
+    # -- HNSW -----------------------------------------------------------------
+    def hnsw_sizes(self, m_l: float = 0.0, max_node: int = 0) -> tuple[float, int]:
+        """m_l and the node capacity the HNSW driver derives when they are unset (HNSW.cpp:62-72)."""
+        ml, mn = C.c_double(), C.c_uint64()
+        check(_lib.lib().nbpg_hnsw_sizes(self.n, self.R, m_l, max_node, C.byref(ml), C.byref(mn)))
+        return ml.value, mn.value
+
+    def build_hnsw(self, L: int = 70, VL: int = 140, top_degree: int = 0, hier_beam: int = 1, PR: int = 0,
+                   alpha: float = 1.1, cos_angle: float = 0.0, m_l: float = 0.0, max_node: int = 0,
+                   repair_isolate: bool = True, with_stats: bool = False):
+        """HNSWIndex::batch_insert over all vectors (HNSW.cpp:166-208): an Hnsw over this index's rows."""
+        prm = HnswParams(L, VL, top_degree, hier_beam, PR, alpha, cos_angle, m_l, max_node, int(repair_isolate))
+        _, mn = self.hnsw_sizes(m_l, max_node)
+        st = BuildStats()
+        sv = np.zeros(mn, np.uint32) if with_stats else None
+        sd = np.zeros(mn, np.uint32) if with_stats else None
+        h = C.c_void_p()
+        check(_lib.lib().nbpg_hnsw_build(self._h, C.byref(prm), C.byref(h), C.byref(st), _p(sv), _p(sd)))
+        hn = Hnsw(self, h)
+        if with_stats:
+            return hn, st, sv[:hn.node_count], sd[:hn.node_count]
+        return hn, st
+
+    def load_hnsw(self, graph: np.ndarray, id_in_pre_level: np.ndarray, entry: int, max_node: int) -> "Hnsw":
+        """A hierarchy from .graph / .hid contents."""
+        g = np.ascontiguousarray(graph, dtype=np.uint32)
+        pre = np.ascontiguousarray(id_in_pre_level, dtype=np.int64)
+        if g.shape != (pre.size, self.R + 1):
+            raise ValueError("graph must be (node_count, R + 1)")
+        h = C.c_void_p()
+        check(_lib.lib().nbpg_hnsw_load(self._h, max_node, pre.size, entry, _p(g), pre.ctypes.data_as(
+            C.POINTER(C.c_int64)), C.byref(h)))
+        return Hnsw(self, h)
+
+
+class Hnsw:
+    """A hierarchical graph over an Index's vectors (HIdMapping + Graph of HNSW.cpp)."""
+
+    def __init__(self, index: Index, h):
+        self.index = index  # keeps the rows alive
+        self._h = h
+        mx, cnt, ep, lv = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint32()
+        check(_lib.lib().nbpg_hnsw_info(self._h, C.byref(mx), C.byref(cnt), C.byref(ep), C.byref(lv)))
+        self.max_node, self.node_count, self.entry, self.max_level = mx.value, cnt.value, ep.value, lv.value
+
+    def get(self) -> tuple[np.ndarray, np.ndarray]:
+        """(graph rows [node_count, R + 1], id_in_pre_level [node_count])."""
+        g = np.empty((self.node_count, self.index.R + 1), np.uint32)
+        pre = np.empty(self.node_count, np.int64)
+        check(_lib.lib().nbpg_hnsw_get(self._h, _p(g), pre.ctypes.data_as(C.POINTER(C.c_int64))))
+        return g, pre
+
+    def search(self, queries: np.ndarray, qp: QueryParams, hier_beam: int = 1) -> SearchResult:
+        """hier_qsearchAll: vector ids of the k best per query, level-0 counters."""
+        q = np.ascontiguousarray(queries)
+        if q.ndim != 2 or q.shape[1] != self.index.dims:
+            raise ValueError("queries must be (nq, dims)")
+        nq, k = q.shape[0], int(qp.k)
+        prm = LaunchConfig().params(qp)
+        ids = np.empty((nq, k), np.uint32)
+        ds = np.empty((nq, k), np.float32)
+        cnt, vis, cmps = (np.empty(nq, np.uint32) for _ in range(3))
+        check(_lib.lib().nbpg_hnsw_search(self._h, q.ctypes.data, nq, C.byref(prm), hier_beam, k, _p(ids),
+                                          _p(ds, _f32p), _p(cnt), _p(vis), _p(cmps)))
+        return SearchResult(ids, ds, cnt, vis, cmps)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().nbpg_hnsw_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class SearchGraph:

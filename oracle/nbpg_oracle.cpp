@@ -864,7 +864,7 @@ struct HnswBuild {
                     }
             }
             std::vector<std::vector<Layer>> layers(bs);
-            const uint64_t limit = cur;
+            const uint64_t limit = n;  // Points.size(): the vectors, not the nodes (hnsw.h:56)
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 8)
             for (long long i = 0; i < (long long)bs; ++i) {
                 std::vector<uint32_t> sp(hbs, 0xFFFFFFFFu);
@@ -1339,11 +1339,12 @@ int nbpg_oracle_build_hnsw(int dtype, int metric, uint32_t dims, const void *bas
 // a search of beam hbs (the query's k and cut, visited cap 8L, a fresh filter sized by L) whose
 // visited list gives the next level's entry points; level 0 is the plain search of beam L
 // (visited and distance counts of that search only); the frontier's first k become vector ids.
+// out_entry (nq x hbs, may be null): the entry points of each query's level-0 search.
 int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n,
                             const uint32_t *graph, uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp,
                             const void *queries, uint32_t nq, uint32_t L, uint32_t k, double cut, uint32_t hbs,
                             uint32_t k_stride, uint32_t *out_ids, uint32_t *out_count, uint32_t *out_visited,
-                            uint32_t *out_cmps, int threads)
+                            uint32_t *out_cmps, uint32_t *out_entry, int threads)
 {
     if (k == 0 || k > L || hbs == 0 || hbs > L || sp >= cur) return 1;
     if (threads <= 0) threads = omp_get_max_threads();
@@ -1351,13 +1352,20 @@ int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *ba
     const uint8_t *B = static_cast<const uint8_t *>(base);
     const uint8_t *Q = static_cast<const uint8_t *>(queries);
     std::vector<uint32_t> rootv(cur), lvl(cur);
+    uint32_t top = 0;
     for (uint64_t v = 0; v < cur; ++v) {
         int64_t q = int64_t(v);
         uint32_t l = 0;
         while (pre[q] >= 0) { q = pre[q]; ++l; }
         rootv[v] = uint32_t(-pre[q] - 1);
         lvl[v] = l;
+        top = std::max(top, l);
     }
+    // the reference's walk down the levels has no bound; edges between levels (made when the
+    // entry node lies above the level searched, as on the first insert with a large m_l) can
+    // hold it above level 0, so a walk longer than 4 * (top + 2) steps is refused
+    const uint32_t max_steps = 4 * (top + 2);
+    int failed = 0;
     GraphView gv{graph, R};
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 4)
     for (long long i = 0; i < (long long)nq; ++i) {
@@ -1366,10 +1374,15 @@ int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *ba
         auto dist_to = [&](uint32_t a) { return dist_rows(dtype, metric, B + size_t(rootv[a]) * row, qr, dims); };
         std::vector<uint32_t> spv(hbs, 0xFFFFFFFFu);
         spv[0] = uint32_t(sp);
-        while (true) {
+        for (uint32_t step = 0;; ++step) {
             const uint32_t lv = lvl[spv[0]];
             uint32_t nsp = 1;
             while (nsp < hbs && spv[nsp] != 0xFFFFFFFFu) ++nsp;
+            if (lv > 0 && step >= max_steps) {
+#pragma omp atomic write
+                failed = 1;
+                break;
+            }
             if (lv > 0) {
                 c.reset(L, 8 * L, R);
                 c.restart(hbs, 8 * L);
@@ -1383,6 +1396,7 @@ int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *ba
                 }
                 continue;
             }
+            if (out_entry) std::copy(spv.begin(), spv.end(), out_entry + size_t(i) * hbs);
             c.reset(L, 8 * L, R);
             seed_frontier(c, spv.data(), nsp, dist_to);
             size_t cmps = beam_search(c, gv, dist_to, -1, k, cut, cur, R);
@@ -1395,7 +1409,7 @@ int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *ba
             break;
         }
     }
-    return 0;
+    return failed ? 2 : 0;
 }
 
 // Prune::maxAnglePrune (prune.h:92-154) on one candidate list as given; 3 where the

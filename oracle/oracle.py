@@ -85,7 +85,7 @@ class CpuLib:
             f("search_hnsw").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, _u32p, C.c_uint32, _i64p,
                                          C.c_uint64, C.c_uint64, _u8p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double,
                                          C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p, _u32p] + \
-                ([C.c_int] if prefix == "nbpg_oracle_" else [])
+                ([_u32p, C.c_int] if prefix == "nbpg_oracle_" else [])
             f("max_angle_prune").restype = C.c_int
             f("max_angle_prune").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, _u32p,
                                              _f32p, _u32p, C.c_uint32, C.c_uint32, C.c_double, C.c_double, _u32p]
@@ -252,8 +252,10 @@ class CpuLib:
         c = int(cur[0])
         return g[:c], pre[:c], int(sp[0]), sv[:c], sd[:c], int(iso[0])
 
-    def search_hnsw(self, dtype, metric, base, graph, pre, sp, queries, L, k, cut=1.35, hier_beam=1, threads=0):
-        """hier_qsearchAll (hier_beamSearch.h:9-92); returns (ids, count, visited, cmps)."""
+    def search_hnsw(self, dtype, metric, base, graph, pre, sp, queries, L, k, cut=1.35, hier_beam=1, threads=0,
+                    entry=None):
+        """hier_qsearchAll (hier_beamSearch.h:9-92); returns (ids, count, visited, cmps).  With the
+        oracle, `entry` (an (nq, hier_beam) u32 array) receives each query's level-0 entry points."""
         base = np.ascontiguousarray(base)
         queries = np.ascontiguousarray(queries)
         graph = np.ascontiguousarray(graph, dtype=np.uint32)
@@ -262,7 +264,7 @@ class CpuLib:
         nq = queries.shape[0]
         ids = np.zeros((nq, k), np.uint32)
         cnt, vis, cm = (np.zeros(nq, np.uint32) for _ in range(3))
-        extra = [threads] if self.prefix == "nbpg_oracle_" else []
+        extra = [_p(entry, _u32p), threads] if self.prefix == "nbpg_oracle_" else []
         rc = self._f("search_hnsw")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, _p(graph, _u32p),
                                     graph.shape[1] - 1, _p(pre, _i64p), graph.shape[0], sp, queries.ctypes.data, nq,
                                     L, k, cut, hier_beam, k, _p(ids, _u32p), _p(cnt, _u32p), _p(vis, _u32p),
