@@ -270,6 +270,45 @@ def time_fgim(base, q, gi, L_op, k, local, n_prefix=100_000):
     return out
 
 
+def time_hnsw(base, q, gi, k, local, n_prefix=100_000):
+    """The HNSW builder (HNSW.cpp:166-208; L 70, VL 140, alpha 1.1, hier_beamSize 1 — the
+    driver's defaults — at the workload's R) on the GPU over all rows, its level-by-level search
+    at a few beams through the host API (recall against the same ground truth), and on a prefix
+    of n_prefix rows the GPU build beside the oracle port's on all host cores, graphs compared."""
+    from nbpg_gb300.index import Index, QueryParams
+    kw = dict(L=70, VL=140, alpha=1.1, hier_beam=1)
+    idx = Index(base, "u8", "l2", max_degree=CFG["R"], device=local)
+    h, st = idx.build_hnsw(**kw)
+    out = {"n": len(base), "nodes": h.node_count, "levels": h.max_level + 1, "gpu_s": st.seconds,
+           "isolated_repaired": int(st.isolated), "search": {}}
+    for L in (19, 32, 64):
+        qp = QueryParams(k=k, beamSize=L, cut=CFG["cut"])
+        h.search(q, qp)
+        t = time.perf_counter()
+        res = h.search(q, qp)
+        sec = time.perf_counter() - t
+        out["search"][f"L{L}"] = {"qps_host_api": len(q) / sec, "recall@10": recall_of(res.ids, gi, k),
+                                  "avg_visited": float(res.visited.mean())}
+    h.close()
+    del idx
+    sub = np.ascontiguousarray(base[:n_prefix])
+    pi = Index(sub, "u8", "l2", max_degree=CFG["R"], device=local)
+    ph, pst = pi.build_hnsw(**kw)
+    g_gpu, pre_gpu = ph.get()
+    ph.close()
+    del pi
+    from oracle.oracle import oracle
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    g_cpu, pre_cpu, *_ = oracle().build_hnsw("u8", "l2", sub, R=CFG["R"], threads=threads, **kw)
+    cpu_s = time.perf_counter() - t
+    same = bool(np.array_equal(g_gpu, g_cpu) and np.array_equal(pre_gpu, pre_cpu))
+    out["prefix"] = {"n": n_prefix, "gpu_s": pst.seconds, "graph_equal_to_port": same,
+                     "cpu_baseline": {"seconds": cpu_s, "cores": threads, "kind": "port"},
+                     "gpu_over_cpu": cpu_s / pst.seconds}
+    return out
+
+
 def recall_of(ids, gi, k):
     return float(np.mean([len(set(a[:k].tolist()) & set(b[:k].tolist())) / k for a, b in zip(ids, gi)]))
 
@@ -608,6 +647,12 @@ def main():
         log(f"[bench] FGIM build {fg['gpu_s']:.2f} s on the GPU, recall {fg['recall@10_at_L']:.4f} at L={L_op}; "
             f"{fg['prefix']['n']} rows: GPU {fg['prefix']['gpu_s']:.2f} s vs port "
             f"{fg['prefix']['cpu_baseline']['seconds']:.1f} s, graphs equal: {fg['prefix']['graph_equal_to_port']}")
+        next_rows["hnsw"] = time_hnsw(base, q, gi, k, local)
+        hn = next_rows["hnsw"]
+        log(f"[bench] HNSW build {hn['gpu_s']:.2f} s ({hn['nodes']} nodes, {hn['levels']} levels); search "
+            + ", ".join(f"{n}: {v['qps_host_api']:.3g} QPS recall {v['recall@10']:.4f}" for n, v in hn["search"].items())
+            + f"; {hn['prefix']['n']} rows: GPU {hn['prefix']['gpu_s']:.2f} s vs port "
+            f"{hn['prefix']['cpu_baseline']['seconds']:.1f} s, graphs equal: {hn['prefix']['graph_equal_to_port']}")
         log(f"[bench] PCA encode {next_rows['pca_encode']['ms']:.2f} ms per 1M rows; re-rank "
             f"{next_rows['rerank']['rerank_factor_100']['qps_host_api']:.3g} QPS; device recall "
             f"{next_rows['eval_recall']['recall@10']:.4f}")
