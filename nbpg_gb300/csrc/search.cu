@@ -2,6 +2,9 @@
 // scratch, and the FLAG pass followed by the LIST re-run of tainted queries.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "internal.h"
@@ -72,9 +75,53 @@ struct PassCfg {
     uint32_t S = 0, Vcap = 0;
 };
 
+// Launch plans and kernel shared-memory attributes, process-wide.  A plan depends only on the
+// key's inputs, so it is computed once (the occupancy queries and attribute calls cost more host
+// time than a 10k-query search spends on the device).  The dynamic shared-memory attribute of a
+// kernel is only ever raised, so every cached plan stays launchable.
+static std::mutex g_plan_mu;
+using PlanKey = std::tuple<int, const SearchOps *, int, bool, bool, uint32_t, uint32_t, uint32_t, uint32_t, size_t, int>;
+static std::map<PlanKey, PassCfg> g_plans;
+static std::map<std::tuple<int, const SearchOps *, int, bool, bool>, size_t> g_attr;
+
+static cudaError_t raise_attr(int device, const SearchOps *ops, int metric, bool list, bool plain, size_t smem)
+{
+    size_t &cur = g_attr[std::make_tuple(device, ops, metric, list, plain)];
+    if (smem <= cur) return cudaSuccess;
+    const cudaError_t e = ops->set_attr(metric, list, plain, smem);
+    if (e == cudaSuccess) cur = smem;
+    return e;
+}
+
+cudaError_t raise_search_attr(int device, const SearchOps *ops, int metric, bool list, bool plain, size_t smem)
+{
+    std::lock_guard<std::mutex> g(g_plan_mu);
+    return raise_attr(device, ops, metric, list, plain, smem);
+}
+
+static nbpg_status plan_pass_uncached(nbpg_index *idx, const SearchOps *ops, int metric, bool list, bool plain,
+                                      uint32_t Lmax, uint32_t vf, uint32_t want_warps, PassCfg &pc);
+
 static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, bool list, bool plain, uint32_t Lmax,
                              uint32_t vf, uint32_t want_warps, PassCfg &pc)
 {
+    const PlanKey key{idx->desc.device, ops, metric, list, plain, Lmax, vf, want_warps, idx->desc.max_degree,
+                      idx->smem_optin, idx->sm_count};
+    std::lock_guard<std::mutex> g(g_plan_mu);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) {
+        pc = it->second;
+        return NBPG_OK;
+    }
+    const nbpg_status s = plan_pass_uncached(idx, ops, metric, list, plain, Lmax, vf, want_warps, pc);
+    if (s == NBPG_OK) g_plans.emplace(key, pc);
+    return s;
+}
+
+static nbpg_status plan_pass_uncached(nbpg_index *idx, const SearchOps *ops, int metric, bool list, bool plain,
+                                      uint32_t Lmax, uint32_t vf, uint32_t want_warps, PassCfg &pc)
+{
+    const int dev = idx->desc.device;
     const uint32_t R = idx->desc.max_degree;
     pc.S = filter_slots_for(Lmax);
     pc.Vcap = round_up(vf * Lmax, 32);
@@ -88,7 +135,7 @@ static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, 
     if (plain) {
         pc.warps = 1;
         pc.smem = pc.lay.bytes;
-        NBPG_CUDA_TRY(ops->set_attr(metric, list, true, pc.smem));
+        NBPG_CUDA_TRY(raise_attr(dev, ops, metric, list, true, pc.smem));
         return NBPG_OK;
     }
     uint32_t fit = uint32_t(idx->smem_optin / pc.lay.bytes);
@@ -101,7 +148,7 @@ static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, 
             if (c > fit) continue;
             const size_t sm = size_t(c) * pc.lay.bytes;
             int b = 0;
-            NBPG_CUDA_TRY(ops->set_attr(metric, list, false, sm));
+            NBPG_CUDA_TRY(raise_attr(dev, ops, metric, list, false, sm));
             NBPG_CUDA_TRY(ops->occ(metric, list, false, int(c) * 32, sm, &b));
             if (int(c) * b > best) { best = int(c) * b; w = c; }
         }
@@ -110,7 +157,7 @@ static nbpg_status plan_pass(nbpg_index *idx, const SearchOps *ops, int metric, 
     w = std::max<uint32_t>(1, std::min<uint32_t>(w, std::min<uint32_t>(16, fit)));
     pc.warps = w;
     pc.smem = size_t(w) * pc.lay.bytes;
-    NBPG_CUDA_TRY(ops->set_attr(metric, list, false, pc.smem));
+    NBPG_CUDA_TRY(raise_attr(dev, ops, metric, list, false, pc.smem));
     int blocks = 0;
     NBPG_CUDA_TRY(ops->occ(metric, list, false, w * 32, pc.smem, &blocks));
     if (blocks < 1) {
@@ -215,7 +262,7 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     a.out_visited = d_visited;
     a.out_cmps = d_cmps;
     a.err = q + 2;
-    a.prefetch = plain ? 0 : (P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u));
+    a.prefetch = P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u);
     if (emit) {
         a.emit_factor = emit->factor;
         a.emit_visited = emit->visited ? 1u : 0u;
@@ -299,7 +346,7 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     if ((s = idx->qbuf.ensure(qbytes)) != NBPG_OK) return s;
     if ((s = idx->obuf.ensure(size_t(nq) * per_q + 64)) != NBPG_OK) return s;
     uint8_t *dq = idx->qbuf.as<uint8_t>();
-    NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, qbytes, st));
+    if (idx->row_bytes != idx->row_stride) NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, qbytes, st));  // zero padding
     NBPG_CUDA_TRY(cudaMemcpy2DAsync(dq, idx->row_stride, queries, idx->row_bytes, idx->row_bytes, nq,
                                     cudaMemcpyHostToDevice, st));
     uint8_t *o = idx->obuf.as<uint8_t>();

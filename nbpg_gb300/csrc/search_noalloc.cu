@@ -164,14 +164,14 @@ extern "C" nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint
     a.out_visited = d_out_visited;
     a.out_cmps = d_out_cmps;
     a.err = scratch + 2;
-    a.prefetch = plain ? 0 : (P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u));
+    a.prefetch = P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u);
 
     auto grid_of = [&](bool list, const SlotLayout &lay, uint32_t want, uint32_t &warps, size_t &smem,
                        uint32_t &grid) -> nbpg_status {
         const uint32_t fit = uint32_t(prop.sharedMemPerBlockOptin / lay.bytes);
         warps = std::max<uint32_t>(1, std::min<uint32_t>(want ? want : 16, std::min<uint32_t>(16, fit)));
         smem = size_t(warps) * lay.bytes;
-        NBPG_CUDA_TRY(ops->set_attr(met, list, false, smem));
+        NBPG_CUDA_TRY(raise_search_attr(device, ops, met, list, false, smem));
         int blocks = 0;
         NBPG_CUDA_TRY(ops->occ(met, list, false, warps * 32, smem, &blocks));
         NBPG_CHECK_ARG(blocks >= 1, "search kernel does not fit on an SM");
@@ -184,7 +184,7 @@ extern "C" nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint
     m.taint = flag_first ? scratch + 4 : nullptr;
     m.lay = lay_main;
     if (plain) {
-        NBPG_CUDA_TRY(ops->set_attr(met, !flag_first, true, lay_main.bytes));
+        NBPG_CUDA_TRY(raise_search_attr(device, ops, met, !flag_first, true, lay_main.bytes));
         ops->launch(met, !flag_first, true, nq, 1, lay_main.bytes, m, st);
     } else {
         uint32_t warps, grid;

@@ -12,6 +12,10 @@ struct SearchOps {
                    cudaStream_t st);
 };
 
+// Raises a search kernel's dynamic shared-memory attribute to at least smem on `device`, never
+// lowering it (launch plans are cached process-wide and stay valid).
+cudaError_t raise_search_attr(int device, const SearchOps *ops, int metric, bool list, bool plain, size_t smem);
+
 // one table per (element type, uint4 per lane per row)
 #define NBPG_DECL_OPS(t) extern const SearchOps search_ops_##t##_v1, search_ops_##t##_v2, search_ops_##t##_v4;
 NBPG_DECL_OPS(u8)
