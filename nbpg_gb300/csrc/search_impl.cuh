@@ -511,7 +511,10 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         uint32_t nfs = n0;
         // cut rule (beamSearch.h:140-149): threshold = float(cut * d_k), upper_bound of (0, thr)
         if (k > 0 && n0 > k) {
-            const float thr = __double2float_rn(a.cut * double(key_dist(frn[k])));
+            // the one double product of the loop, on one lane (FP64 issue is scarce on this part)
+            float thr = 0.f;
+            if (lane == 0) thr = __double2float_rn(a.cut * double(key_dist(frn[k])));
+            thr = __shfl_sync(kFull, thr, 0);
             uint32_t ub = 0;
             for (uint32_t base = 0; base < n0; base += 32) {
                 const uint32_t i = base + lane;
