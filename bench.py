@@ -9,11 +9,14 @@ min_alpha=1.05 (max_alpha 1.1, the Vamana default), built on the GPU; ground tru
 k=100 by the GPU brute-force kNN in CompGT-compatible mode.  The beam width L is
 the smallest of the reference's sweep values in [10, 200] reaching recall@10 >= 0.95.
 
-A step = one strict batched search of all 10k queries at that L (k=10, cut=1.35,
-start point 0): the persistent kernel pulling queries from a device queue.
+A step = one strict search of all 10k queries at that L (k=10, cut=1.35, start
+point 0) with the launch nbpg_search_autotune picks (the plain one-query-per-block
+kernel or the persistent kernel pulling queries from a device queue, their lane
+widths and CTA sizes; every candidate returns identical results).
 `value` is device-resident QPS over the timed steps (CUDA events on the launching
 stream); `e2e` is the same search through the C ABI (nbpg_search) from pinned host
-queries to host results.  The index (128 MB vectors + 272 MB graph) is larger than
+queries to host results.  With N ranks (torchrun), each rank searches its own replica
+of the index, the job's time is the slowest rank's, and rank 0 prints the line.  The index (128 MB vectors + 272 MB graph) is larger than
 L2, so no flush is needed between steps.
 
 --impl reference times the reference algorithm on the host cores instead: the CPU
@@ -49,6 +52,23 @@ def log(*a):
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def max_over_ranks(x: float, dist=None) -> float:
+    """The largest x over all ranks (the timing rule: each rank times its own replica, the job
+    takes as long as the slowest); every rank calls it and gets the same value."""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
 
 
 class Clocks:
@@ -556,14 +576,8 @@ def main():
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_s = sum(step_ms) / 1e3
-    if dist:
-        tt = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_s = float(tt.item())
-        if rank == 0:
-            dist.barrier()
-    value = world * nq * args.steps / total_s
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dist)
+    value = job_rate(nq * args.steps, world, total_s)
     ms_step = 1e3 * total_s / args.steps
 
     # the two kernel forms at the same L: plain (one query per block, default launch) and
@@ -631,11 +645,13 @@ def main():
 
     for _ in range(args.warmup):
         host_search()
+    if dist:
+        dist.barrier()
     t = time.perf_counter()
     for _ in range(args.steps):
         host_search()
-    e2e_s = time.perf_counter() - t
-    e2e_qps = world * nq * args.steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t, dist)
+    e2e_qps = job_rate(nq * args.steps, world, e2e_s)
     assert np.array_equal(oh_ids.numpy().view(np.uint32), res_op.ids), "e2e results differ"
     h2d = nq * CFG["dim"]
     d2h = nq * k * 8 + nq * 12 + 4
