@@ -29,6 +29,7 @@ struct nbpg_hnsw {
     std::vector<int64_t> pre;  // id_in_pre_level of the nodes so far
     std::vector<uint32_t> lvl;
     nbpg::DevBuf qbuf, obuf, spbuf, queue, ghash, gvis;
+    nbpg::SearchScratch scratch;  // the level-0 search's
     std::mutex mu;
     ~nbpg_hnsw()
     {
@@ -36,6 +37,7 @@ struct nbpg_hnsw {
                         static_cast<void *>(d_lvl), static_cast<void *>(d_root)})
             if (p) cudaFree(p);
         for (nbpg::DevBuf *b : {&qbuf, &obuf, &spbuf, &queue, &ghash, &gvis}) b->release();
+        scratch.release();
     }
 };
 
@@ -54,7 +56,7 @@ struct HnswKernels {
             e = cudaFuncSetAttribute(rev_merge_kernel<DT, MET, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(smem_merge));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(hnsw_query_kernel<DT, MET, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(hnsw_descend_kernel<DT, MET, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(smem_query));
         return e;
     }
@@ -64,7 +66,7 @@ struct HnswKernels {
     }
     static cudaError_t occ_query(uint32_t threads, size_t smem, int *blocks)
     {
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, hnsw_query_kernel<DT, MET, VPL>, int(threads), smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, hnsw_descend_kernel<DT, MET, VPL>, int(threads), smem);
     }
     static void level(uint32_t grid, uint32_t threads, size_t smem, const HnswArgs &H, cudaStream_t st)
     {
@@ -76,7 +78,7 @@ struct HnswKernels {
     }
     static void query(uint32_t grid, uint32_t threads, size_t smem, const HnswQueryArgs &Q, cudaStream_t st)
     {
-        hnsw_query_kernel<DT, MET, VPL><<<grid, threads, smem, st>>>(Q);
+        hnsw_descend_kernel<DT, MET, VPL><<<grid, threads, smem, st>>>(Q);
     }
 };
 
@@ -491,94 +493,118 @@ static nbpg_status hnsw_search_impl(nbpg_hnsw *h, const void *queries, uint32_t 
     cudaStream_t st = idx->stream;
     nbpg_status s;
 
-    SearchArgs a{};
-    a.base = h->d_rows;
-    a.row_stride = idx->row_stride;
-    a.vecs = vecs;
-    a.lpr = lpr;
-    a.vpl = vpl;
-    a.graph = h->d_graph;
-    a.gstride = idx->gstride;
-    a.R = R;
-    a.n = h->cur;
-    a.cut = P.cut;
-    a.limit = P.limit ? P.limit : h->cur;  // QP.limit = G.size() (check_nn_recall.h:201)
-    a.degree_limit = P.degree_limit ? P.degree_limit : R;
-    a.prefetch = 2;
-    a.filter_L = L;
-    a.nq = nq;
-    a.k_stride = k_stride;
-    const uint32_t S = filter_slots_for(L);
-    const bool ghash = S * 4 > 32768;
-    const uint64_t V = 8ull * L;
-    const bool gvis = V * 8 > 16384;
-    a.lay = make_slot_layout(std::max(L, R), R, !gvis, uint32_t(V), !ghash, S);
-    NBPG_CHECK_ARG(a.lay.bytes <= idx->smem_optin, "per-query working set exceeds shared memory");
-    const uint32_t W = std::max<uint32_t>(1, std::min<uint32_t>(8, uint32_t(idx->smem_optin / a.lay.bytes)));
-    const size_t smem = size_t(W) * a.lay.bytes;
-    NBPG_CUDA_TRY(kt.setup(48 * 1024, size_t(8) * kMergeWarpBytes, smem));
-    int blocks = 0;
-    NBPG_CUDA_TRY(kt.occ_query(W * 32, smem, &blocks));
-    NBPG_CHECK_ARG(blocks >= 1, "HNSW query kernel does not fit on an SM");
-    const uint32_t grid = std::min<uint32_t>(uint32_t(blocks) * uint32_t(idx->sm_count), (nq + W - 1) / W);
-    const size_t nslots = size_t(grid) * W;
-    if (ghash) {
-        if ((s = h->ghash.ensure(nslots * S * 4)) != NBPG_OK) return s;
-        a.g_hash = h->ghash.as<uint32_t>();
-        a.g_hash_slots = S;
-    }
-    if (gvis) {
-        if ((s = h->gvis.ensure(nslots * V * 8)) != NBPG_OK) return s;
-        a.g_vis = h->gvis.as<uint64_t>();
-        a.g_vis_cap = uint32_t(V);
-    }
     const size_t qbytes = size_t(nq) * idx->row_stride;
     if ((s = h->qbuf.ensure(qbytes)) != NBPG_OK) return s;
     if ((s = h->obuf.ensure(size_t(nq) * (size_t(k_stride) * 8 + 12) + 64)) != NBPG_OK) return s;
     if ((s = h->spbuf.ensure(size_t(nq) * hbs * 4)) != NBPG_OK) return s;
     if ((s = h->queue.ensure(16)) != NBPG_OK) return s;
     uint8_t *dq = h->qbuf.as<uint8_t>();
-    NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, qbytes, st));
+    if (idx->row_bytes != idx->row_stride) NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, qbytes, st));
     NBPG_CUDA_TRY(cudaMemcpy2DAsync(dq, idx->row_stride, queries, idx->row_bytes, idx->row_bytes, nq,
                                     cudaMemcpyHostToDevice, st));
     uint8_t *o = h->obuf.as<uint8_t>();
     uint32_t *d_ids = reinterpret_cast<uint32_t *>(o);
     float *d_d = reinterpret_cast<float *>(o + size_t(nq) * k_stride * 4);
     uint32_t *d_c = reinterpret_cast<uint32_t *>(o + size_t(nq) * k_stride * 8);
-    uint32_t *d_v = d_c + nq, *d_m = d_v + nq, *d_err = d_m + nq;
-    NBPG_CUDA_TRY(cudaMemsetAsync(d_err, 0, 4, st));
+    uint32_t *d_v = d_c + nq, *d_m = d_v + nq;
+    uint32_t *d_err = h->queue.as<uint32_t>() + 1;
     NBPG_CUDA_TRY(cudaMemsetAsync(h->queue.ptr, 0, 16, st));
-    a.queries = dq;
-    a.out_ids = d_ids;
-    a.out_dists = d_d;
-    a.out_count = d_c;
-    a.out_visited = d_v;
-    a.out_cmps = d_m;
-    a.err = d_err;
-    a.queue = h->queue.as<uint32_t>();
-    HnswQueryArgs Q{};
-    Q.s = a;
-    Q.L = L;
-    Q.k = k;
-    Q.hbs = hbs;
-    Q.ep = uint32_t(h->ep);
-    Q.lower = h->d_lower;
-    Q.lvl = h->d_lvl;
-    Q.root = h->d_root;
-    Q.sp = h->spbuf.as<uint32_t>();
-    Q.max_steps = 4 * (h->max_level + 2);
-    kt.query(grid, W * 32, smem, Q, st);
+
+    // 1. the walk down to level 0 (only when the hierarchy has levels above it)
+    uint32_t *d_sp = h->spbuf.as<uint32_t>();
+    if (h->max_level > 0) {
+        SearchArgs a{};
+        a.base = h->d_rows;
+        a.row_stride = idx->row_stride;
+        a.vecs = vecs;
+        a.lpr = lpr;
+        a.vpl = vpl;
+        a.graph = h->d_graph;
+        a.gstride = idx->gstride;
+        a.R = R;
+        a.n = h->cur;
+        a.cut = P.cut;
+        a.limit = P.limit ? P.limit : h->cur;  // QP.limit = G.size() (check_nn_recall.h:201)
+        a.degree_limit = P.degree_limit ? P.degree_limit : R;
+        a.filter_L = L;
+        a.queries = dq;
+        a.nq = nq;
+        a.err = d_err;
+        a.queue = h->queue.as<uint32_t>();
+        const uint32_t S = filter_slots_for(L);
+        const bool ghash = S * 4 > 32768;
+        const uint64_t V = 8ull * L;
+        const bool gvis = V * 8 > 16384;
+        a.lay = make_slot_layout(std::max(hbs, R), R, !gvis, uint32_t(V), !ghash, S);
+        NBPG_CHECK_ARG(a.lay.bytes <= idx->smem_optin, "per-query working set exceeds shared memory");
+        const uint32_t W = std::max<uint32_t>(1, std::min<uint32_t>(8, uint32_t(idx->smem_optin / a.lay.bytes)));
+        const size_t smem = size_t(W) * a.lay.bytes;
+        NBPG_CUDA_TRY(kt.setup(48 * 1024, size_t(8) * kMergeWarpBytes, smem));
+        int blocks = 0;
+        NBPG_CUDA_TRY(kt.occ_query(W * 32, smem, &blocks));
+        NBPG_CHECK_ARG(blocks >= 1, "HNSW walk kernel does not fit on an SM");
+        const uint32_t grid = std::min<uint32_t>(uint32_t(blocks) * uint32_t(idx->sm_count), (nq + W - 1) / W);
+        const size_t nslots = size_t(grid) * W;
+        if (ghash) {
+            if ((s = h->ghash.ensure(nslots * S * 4)) != NBPG_OK) return s;
+            a.g_hash = h->ghash.as<uint32_t>();
+            a.g_hash_slots = S;
+        }
+        if (gvis) {
+            if ((s = h->gvis.ensure(nslots * V * 8)) != NBPG_OK) return s;
+            a.g_vis = h->gvis.as<uint64_t>();
+            a.g_vis_cap = uint32_t(V);
+        }
+        HnswQueryArgs Q{};
+        Q.s = a;
+        Q.L = L;
+        Q.k = k;
+        Q.hbs = hbs;
+        Q.ep = uint32_t(h->ep);
+        Q.lower = h->d_lower;
+        Q.lvl = h->d_lvl;
+        Q.sp = d_sp;
+        Q.max_steps = 4 * (h->max_level + 2);
+        kt.query(grid, W * 32, smem, Q, st);
+        NBPG_CUDA_TRY(cudaGetLastError());
+    } else {
+        std::vector<uint32_t> e(size_t(nq) * hbs, kNoId);
+        for (uint32_t i = 0; i < nq; ++i) e[size_t(i) * hbs] = uint32_t(h->ep);
+        NBPG_CUDA_TRY(cudaMemcpyAsync(d_sp, e.data(), e.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+
+    // 2. the level-0 search: the flat search over the nodes' rows and graph from each query's
+    //    entry points (its QueryStatic counters are the reference's), 3. node ids -> vector ids
+    SearchTarget tgt;
+    tgt.base = h->d_rows;
+    tgt.graph = h->d_graph;
+    tgt.n = h->cur;
+    tgt.d_sp = d_sp;
+    tgt.sp_stride = hbs;
+    nbpg_search_params p = P;
+    if (!p.limit) p.limit = h->cur;
+    s = search_device_impl(idx, h->scratch, dq, nq, &p, nullptr, nullptr, nullptr, 0, k_stride, d_ids, d_d, d_c, d_v,
+                           d_m, st, nullptr, &tgt);
+    if (s != NBPG_OK) return s;
+    const size_t cnt = size_t(nq) * k_stride;
+    hnsw_root_ids_kernel<<<uint32_t((cnt + 255) / 256), 256, 0, st>>>(d_ids, cnt, h->d_root);
     NBPG_CUDA_TRY(cudaGetLastError());
-    uint32_t err = 0;
-    NBPG_CUDA_TRY(cudaMemcpyAsync(out_ids, d_ids, size_t(nq) * k_stride * 4, cudaMemcpyDeviceToHost, st));
-    if (out_dists) NBPG_CUDA_TRY(cudaMemcpyAsync(out_dists, d_d, size_t(nq) * k_stride * 4, cudaMemcpyDeviceToHost, st));
+
+    uint32_t err[2] = {0, 0};
+    NBPG_CUDA_TRY(cudaMemcpyAsync(out_ids, d_ids, cnt * 4, cudaMemcpyDeviceToHost, st));
+    if (out_dists) NBPG_CUDA_TRY(cudaMemcpyAsync(out_dists, d_d, cnt * 4, cudaMemcpyDeviceToHost, st));
     if (out_count) NBPG_CUDA_TRY(cudaMemcpyAsync(out_count, d_c, nq * 4, cudaMemcpyDeviceToHost, st));
     if (out_visited) NBPG_CUDA_TRY(cudaMemcpyAsync(out_visited, d_v, nq * 4, cudaMemcpyDeviceToHost, st));
     if (out_cmps) NBPG_CUDA_TRY(cudaMemcpyAsync(out_cmps, d_m, nq * 4, cudaMemcpyDeviceToHost, st));
-    NBPG_CUDA_TRY(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, st));
+    NBPG_CUDA_TRY(cudaMemcpyAsync(&err[0], d_err, 4, cudaMemcpyDeviceToHost, st));
+    NBPG_CUDA_TRY(cudaMemcpyAsync(&err[1], h->scratch.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
     NBPG_CUDA_TRY(cudaStreamSynchronize(st));
-    if (err) {
+    if (err[0]) {
         set_error("a query's walk down the levels did not reach level 0");
+        return NBPG_ERR_INVALID_ARG;
+    }
+    if (err[1]) {
+        set_error("a query was rejected on the device (k > L)");
         return NBPG_ERR_INVALID_ARG;
     }
     return NBPG_OK;

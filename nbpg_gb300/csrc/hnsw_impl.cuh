@@ -130,22 +130,23 @@ static __global__ void hnsw_rows_kernel(uint8_t *rows, const uint8_t *base, cons
 }
 
 // ---------------------------------------------------------------------------
-// hier_qsearchAll (hier_beamSearch.h:9-92): one warp per query.  From the entry node, while the
-// first entry point lies above level 0, a search of beam hbs (the query's k and cut, visited
-// cap 8L, filter sized by L) whose visited list, moved one level down, gives the next entry
-// points; then the level-0 search of beam L, whose frontier[0:k] becomes vector ids.
+// hier_qsearchAll (hier_beamSearch.h:9-92), the walk down the levels: one warp per query.
+// From the entry node, while the first entry point lies above level 0, a search of beam hbs
+// (the query's k and cut, visited cap 8L, a fresh filter sized by L) whose visited list, moved
+// one level down, gives the next entry points.  The level-0 entry points are left in sp for
+// the flat search, which runs the level-0 search of beam L over the node rows.
 // ---------------------------------------------------------------------------
 struct HnswQueryArgs {
-    SearchArgs s;        // node rows/graph, queries, outputs, layout; filter_L = L
+    SearchArgs s;        // node rows/graph, queries, layout; filter_L = L; err
     uint32_t L, k, hbs;
     uint32_t ep;
-    const uint32_t *lower, *lvl, *root;
-    uint32_t *sp;        // per query, hbs entries
+    const uint32_t *lower, *lvl;
+    uint32_t *sp;        // per query, hbs entries: the level-0 entry points on return
     uint32_t max_steps;  // bound on the levels walked (the reference's loop has none)
 };
 
 template <int DT, int MET, int VPL>
-__device__ void hnsw_query(const HnswQueryArgs &Q, uint32_t qi, uint8_t *slot, uint32_t gslot, int lane)
+__device__ void hnsw_descend(const HnswQueryArgs &Q, uint32_t qi, uint8_t *slot, uint32_t gslot, int lane)
 {
     const SearchArgs &a = Q.s;
     const uint8_t *qrow = a.queries + size_t(qi) * a.row_stride;
@@ -154,65 +155,32 @@ __device__ void hnsw_query(const HnswQueryArgs &Q, uint32_t qi, uint8_t *slot, u
     __syncwarp();
     for (uint32_t step = 0;; ++step) {
         const uint32_t lv = Q.lvl[sp[0]];
-        uint32_t nsp = 1;
-        while (nsp < Q.hbs && sp[nsp] != kNoId) ++nsp;
-        if (lv > 0 && step < Q.max_steps) {
-            const SearchState st = search_core<DT, MET, true, VPL>(a, qrow, Q.hbs, Q.k, 8ull * Q.L, sp, nsp, slot,
-                                                                   gslot, lane, kNoId);
-            const uint32_t m = st.vs < Q.hbs ? st.vs : Q.hbs;
-            __syncwarp();
-            for (uint32_t j = lane; j < Q.hbs; j += 32) {
-                uint32_t v = kNoId;
-                if (j < m) {
-                    const uint32_t near = key_id(st.vis[j]);
-                    v = Q.lvl[near] >= lv ? Q.lower[near] : near;
-                }
-                sp[j] = v;
-            }
-            __syncwarp();
-            continue;
-        }
-        if (lv > 0) {
-            // the walk did not reach level 0 within max_steps levels: empty row, error flag
-            for (uint32_t j = lane; j < a.k_stride; j += 32) {
-                a.out_ids[size_t(qi) * a.k_stride + j] = kNoId;
-                if (a.out_dists) a.out_dists[size_t(qi) * a.k_stride + j] = __int_as_float(0x7f800000);
-            }
-            if (lane == 0) {
-                if (a.out_count) a.out_count[qi] = 0;
-                if (a.out_visited) a.out_visited[qi] = 0;
-                if (a.out_cmps) a.out_cmps[qi] = 0;
-                if (a.err) atomicExch(a.err, 1u);
-            }
-            __syncwarp();
+        if (lv == 0) return;
+        if (step >= Q.max_steps) {
+            // the walk did not reach level 0: error flag; the entry point stays a valid node
+            if (lane == 0) atomicExch(a.err, 1u);
             return;
         }
-        const SearchState st = search_core<DT, MET, true, VPL>(a, qrow, Q.L, Q.k, 8ull * Q.L, sp, nsp, slot, gslot,
+        uint32_t nsp = 1;
+        while (nsp < Q.hbs && sp[nsp] != kNoId) ++nsp;
+        const SearchState st = search_core<DT, MET, true, VPL>(a, qrow, Q.hbs, Q.k, 8ull * Q.L, sp, nsp, slot, gslot,
                                                                lane, kNoId);
-        const uint64_t *fr = st.frontier();
-        const uint32_t kk = st.fs < Q.k ? st.fs : Q.k;
-        for (uint32_t j = lane; j < a.k_stride; j += 32) {
-            const size_t o = size_t(qi) * a.k_stride + j;
-            if (j < kk) {
-                a.out_ids[o] = Q.root[key_id(fr[j])];
-                if (a.out_dists) a.out_dists[o] = output_dist<MET>(key_dist(fr[j]));
-            } else {
-                a.out_ids[o] = kNoId;
-                if (a.out_dists) a.out_dists[o] = __int_as_float(0x7f800000);
+        const uint32_t m = st.vs < Q.hbs ? st.vs : Q.hbs;
+        __syncwarp();
+        for (uint32_t j = lane; j < Q.hbs; j += 32) {
+            uint32_t v = kNoId;
+            if (j < m) {
+                const uint32_t near = key_id(st.vis[j]);
+                v = Q.lvl[near] >= lv ? Q.lower[near] : near;
             }
-        }
-        if (lane == 0) {
-            if (a.out_count) a.out_count[qi] = kk;
-            if (a.out_visited) a.out_visited[qi] = uint32_t(st.nvis);
-            if (a.out_cmps) a.out_cmps[qi] = st.cmps;
+            sp[j] = v;
         }
         __syncwarp();
-        return;
     }
 }
 
 template <int DT, int MET, int VPL>
-__global__ void __launch_bounds__(512) hnsw_query_kernel(HnswQueryArgs Q)
+__global__ void __launch_bounds__(512) hnsw_descend_kernel(HnswQueryArgs Q)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -223,8 +191,15 @@ __global__ void __launch_bounds__(512) hnsw_query_kernel(HnswQueryArgs Q)
         if (lane == 0) w = atomicAdd(Q.s.queue, 1u);
         w = __shfl_sync(kFull, w, 0);
         if (w >= Q.s.nq) break;
-        hnsw_query<DT, MET, VPL>(Q, w, slot, gslot, lane);
+        hnsw_descend<DT, MET, VPL>(Q, w, slot, gslot, lane);
     }
+}
+
+// The level-0 search's node ids -> vector ids (hier_beamSearch.h:84-86).
+static __global__ void hnsw_root_ids_kernel(uint32_t *ids, size_t count, const uint32_t *root)
+{
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < count && ids[i] != kNoId) ids[i] = root[ids[i]];
 }
 
 }  // namespace nbpg

@@ -87,11 +87,22 @@ struct SearchEmit {
     uint32_t *d_fs = nullptr;
 };
 
+// What a search runs over when it is not the index's own rows and graph (HNSW's level 0, one row
+// per node), and per-query start points on the device: sp_stride entries per query, kNoId padded,
+// the first always used (the reference's get_sp(i)).
+struct SearchTarget {
+    const uint8_t *base = nullptr;
+    const uint32_t *graph = nullptr;
+    uint64_t n = 0;
+    const uint32_t *d_sp = nullptr;
+    uint32_t sp_stride = 0;
+};
+
 nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
                                const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
                                const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
                                uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st,
-                               const SearchEmit *emit = nullptr);
+                               const SearchEmit *emit = nullptr, const SearchTarget *tgt = nullptr);
 
 }  // namespace nbpg
 

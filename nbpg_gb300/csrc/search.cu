@@ -172,22 +172,30 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
                                const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
                                const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
                                uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st,
-                               const SearchEmit *emit)
+                               const SearchEmit *emit, const SearchTarget *tgt)
 {
     NBPG_CHECK_ARG(idx && P && d_ids, "null argument");
-    NBPG_CHECK_ARG(idx->d_points && idx->d_graph, "index has no points/graph");
+    const uint8_t *base = tgt && tgt->base ? tgt->base : idx->d_points;
+    const uint32_t *graph = tgt && tgt->base ? tgt->graph : idx->d_graph;
+    NBPG_CHECK_ARG(base && graph, "index has no points/graph");
     if (nq == 0) return NBPG_OK;
     const uint32_t R = idx->desc.max_degree;
-    const uint64_t n = idx->desc.n;
+    const uint64_t n = tgt && tgt->base ? tgt->n : idx->desc.n;
+    const bool per_query_sp = tgt && tgt->d_sp;
     NBPG_CHECK_ARG(P->L >= 1 && P->L <= 1024, "L must be in [1, 1024]");
     NBPG_CHECK_ARG(P->k >= 1 && P->k <= P->L, "k must be in [1, L] (the reference aborts on k > L)");
     NBPG_CHECK_ARG(k_stride >= P->k, "k_stride < k");
-    NBPG_CHECK_ARG(sp && nsp >= 1 && nsp <= P->L && nsp <= 256, "need 1..min(L,256) start points");
+    if (per_query_sp) {
+        // checked per query on the device (entries come from a device-side walk)
+        NBPG_CHECK_ARG(tgt->sp_stride >= 1 && tgt->sp_stride <= P->L, "per-query start points: 1..L each");
+    } else {
+        NBPG_CHECK_ARG(sp && nsp >= 1 && nsp <= P->L && nsp <= 256, "need 1..min(L,256) start points");
+        // repeated start points are accepted as the reference accepts them (the frontier then
+        // holds copies of a key; query_params.h:204-221, beamSearch.h:154-160)
+        for (uint32_t i = 0; i < nsp; ++i) NBPG_CHECK_ARG(sp[i] < n, "start point out of range");
+    }
     NBPG_CHECK_ARG(R <= 128, "max_degree above 128 is not supported");
     NBPG_CHECK_ARG(P->kernel == NBPG_KERNEL_BATCHED || P->kernel == NBPG_KERNEL_PLAIN, "unknown kernel");
-    // repeated start points are accepted as the reference accepts them (the frontier then holds
-    // copies of a key; query_params.h:204-221, beamSearch.h:154-160)
-    for (uint32_t i = 0; i < nsp; ++i) NBPG_CHECK_ARG(sp[i] < n, "start point out of range");
     uint32_t vecs, lpr, vpl;
     row_geometry(idx->row_stride, P->lane_width, vecs, lpr, vpl);
     NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");
@@ -227,19 +235,19 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     uint32_t *q = sc.queue.as<uint32_t>();
     NBPG_CUDA_TRY(cudaMemsetAsync(q, 0, 4 * sizeof(uint32_t), st));
     NBPG_CUDA_TRY(cudaMemsetAsync(sc.taint.ptr, 0, sizeof(uint32_t), st));
-    if (sc.sp_host.size() != nsp || !std::equal(sp, sp + nsp, sc.sp_host.begin())) {
+    if (!per_query_sp && (sc.sp_host.size() != nsp || !std::equal(sp, sp + nsp, sc.sp_host.begin()))) {
         NBPG_CUDA_TRY(cudaMemcpyAsync(sc.sp.ptr, sp, nsp * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         NBPG_CUDA_TRY(cudaStreamSynchronize(st));
         sc.sp_host.assign(sp, sp + nsp);
     }
 
     SearchArgs a{};
-    a.base = idx->d_points;
+    a.base = base;
     a.row_stride = idx->row_stride;
     a.vecs = vecs;
     a.lpr = lpr;
     a.vpl = vpl;
-    a.graph = idx->d_graph;
+    a.graph = graph;
     a.gstride = idx->gstride;
     a.R = R;
     a.n = n;
@@ -253,8 +261,9 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     a.limit = P->limit ? P->limit : n;
     a.degree_limit = P->degree_limit ? std::min(P->degree_limit, R) : R;
     a.visited_factor = vf;
-    a.sp = sc.sp.as<uint32_t>();
-    a.nsp = nsp;
+    a.sp = per_query_sp ? tgt->d_sp : sc.sp.as<uint32_t>();
+    a.nsp = per_query_sp ? tgt->sp_stride : nsp;
+    a.sp_stride = per_query_sp ? tgt->sp_stride : 0;
     a.k_stride = k_stride;
     a.out_ids = d_ids;
     a.out_dists = d_dists;

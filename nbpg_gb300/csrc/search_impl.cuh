@@ -57,6 +57,8 @@ struct SearchArgs {
     uint32_t visited_factor;
     const uint32_t *sp;  // device start points
     uint32_t nsp;
+    uint32_t sp_stride;  // > 0: per-query start points, sp_stride entries per query from sp (kNoId
+                         // padded, the first always used): the reference's get_sp(i)
     uint32_t k_stride;
     uint32_t *out_ids;
     float *out_dists;
@@ -569,7 +571,14 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     const uint32_t k = a.ks ? a.ks[qi] : a.k_all;
     const uint32_t S = filter_slots_for(L);
     const uint64_t max_visited = uint64_t(a.visited_factor) * L;
-    if (L == 0 || k == 0 || k > L || L > a.lay.Lcap || a.nsp > L || k > a.k_stride ||
+    const uint32_t *sp = a.sp;
+    uint32_t nsp = a.nsp;
+    if (a.sp_stride) {
+        sp = a.sp + size_t(qi) * a.sp_stride;
+        nsp = 1;
+        while (nsp < a.sp_stride && sp[nsp] != kNoId) ++nsp;
+    }
+    if (L == 0 || k == 0 || k > L || L > a.lay.Lcap || nsp > L || k > a.k_stride ||
         (LIST && !a.g_vis && max_visited > a.lay.Vcap) || (!a.g_hash && S > a.lay.Scap) ||
         (a.g_hash && S > a.g_hash_slots) || (LIST && a.g_vis && max_visited > a.g_vis_cap)) {
         // rejected (the reference aborts on k > L, beamSearch.h:268-273): empty row + error flag
@@ -588,7 +597,7 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
     }
 
     const SearchState st = search_core<DT, MET, LIST, VPL>(a, a.queries + size_t(qi) * a.row_stride, L, k, max_visited,
-                                                      a.sp, a.nsp, slot, gslot, lane, kNoId);
+                                                      sp, nsp, slot, gslot, lane, kNoId);
     const uint64_t *frb = st.frontier();
     const uint32_t fs = st.fs;
     const uint64_t nvis = st.nvis;

@@ -292,13 +292,15 @@ class Hnsw:
         check(_lib.lib().nbpg_hnsw_get(self._h, _p(g), pre.ctypes.data_as(C.POINTER(C.c_int64))))
         return g, pre
 
-    def search(self, queries: np.ndarray, qp: QueryParams, hier_beam: int = 1) -> SearchResult:
-        """hier_qsearchAll: vector ids of the k best per query, level-0 counters."""
+    def search(self, queries: np.ndarray, qp: QueryParams, hier_beam: int = 1,
+               launch: "LaunchConfig | None" = None) -> SearchResult:
+        """hier_qsearchAll: vector ids of the k best per query, level-0 counters.  `launch` shapes
+        the level-0 search (default: the plain one-query-per-block kernel)."""
         q = np.ascontiguousarray(queries)
         if q.ndim != 2 or q.shape[1] != self.index.dims:
             raise ValueError("queries must be (nq, dims)")
         nq, k = q.shape[0], int(qp.k)
-        prm = LaunchConfig().params(qp)
+        prm = (launch or LaunchConfig(kernel="plain")).params(qp)
         ids = np.empty((nq, k), np.uint32)
         ds = np.empty((nq, k), np.float32)
         cnt, vis, cmps = (np.empty(nq, np.uint32) for _ in range(3))
