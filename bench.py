@@ -295,17 +295,18 @@ def time_hnsw(base, q, gi, k, local, n_prefix=100_000):
     driver's defaults — at the workload's R) on the GPU over all rows, its level-by-level search
     at a few beams through the host API (recall against the same ground truth), and on a prefix
     of n_prefix rows the GPU build beside the oracle port's on all host cores, graphs compared."""
-    from nbpg_gb300.index import Index, QueryParams
+    from nbpg_gb300.index import Index, LaunchConfig, QueryParams
     kw = dict(L=70, VL=140, alpha=1.1, hier_beam=1)
     idx = Index(base, "u8", "l2", max_degree=CFG["R"], device=local)
     h, st = idx.build_hnsw(**kw)
     out = {"n": len(base), "nodes": h.node_count, "levels": h.max_level + 1, "gpu_s": st.seconds,
            "isolated_repaired": int(st.isolated), "search": {}}
+    plain = LaunchConfig(kernel="plain")
     for L in (19, 32, 64):
         qp = QueryParams(k=k, beamSize=L, cut=CFG["cut"])
-        h.search(q, qp)
+        h.search(q, qp, launch=plain)
         t = time.perf_counter()
-        res = h.search(q, qp)
+        res = h.search(q, qp, launch=plain)
         sec = time.perf_counter() - t
         out["search"][f"L{L}"] = {"qps_host_api": len(q) / sec, "recall@10": recall_of(res.ids, gi, k),
                                   "avg_visited": float(res.visited.mean())}

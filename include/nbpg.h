@@ -124,6 +124,16 @@ nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t 
                                uint32_t n_start, uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
                                uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps, void *stream);
 
+/* Per-query start points (qsearchAll's get_sp(i), beamSearch.h:257-300): d_start_points holds
+ * sp_stride entries per query on the device, padded with 0xFFFFFFFF after the first (which is
+ * always used); otherwise as nbpg_search_device.  Repeated entries are allowed, as in the
+ * reference. */
+nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                  const nbpg_search_params *params, const uint32_t *d_start_points,
+                                  uint32_t sp_stride, uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
+                                  uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps,
+                                  void *stream);
+
 /* Autotuner for the search launch: times CTA size x lane width x prefetch for the
  * batched kernel, and the plain kernel, on the caller's device-resident queries with
  * the caller's (L, k), and writes the fastest configuration into *tuned (a copy of

@@ -171,7 +171,7 @@ int main(int argc, char **argv)
     if (k > gk) die(std::to_string(k) + "@" + std::to_string(k) + " too large for ground truth data of size " + std::to_string(gk));
     SearchFn search = [&](uint32_t qk, uint32_t beam, double cut, uint64_t limit, uint32_t dl, uint32_t *ids,
                           uint32_t *cnt, uint32_t *vis, uint32_t *cmps) {
-        nbpg_search_params spm{qk, beam, cut, limit, dl, 8, NBPG_KERNEL_PLAIN, 0, 0, -1};
+        nbpg_search_params spm{qk, beam, cut, limit, dl, 8, NBPG_KERNEL_BATCHED, 0, 0, -1};
         check(nbpg_hnsw_search(h, Q.data(), nq, &spm, a.hier_beam, qk, ids, nullptr, cnt, vis, cmps));
     };
     Eval e{idx, false, &Q, nq, &gt, gk, gn, R, a.verbose};

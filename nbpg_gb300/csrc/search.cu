@@ -326,6 +326,23 @@ extern "C" nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries
                               d_out_dists, d_out_count, d_out_visited, d_out_cmps, static_cast<cudaStream_t>(stream));
 }
 
+extern "C" nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                             const nbpg_search_params *params, const uint32_t *d_start_points,
+                                             uint32_t sp_stride, uint32_t k_stride, uint32_t *d_out_ids,
+                                             float *d_out_dists, uint32_t *d_out_count, uint32_t *d_out_visited,
+                                             uint32_t *d_out_cmps, void *stream)
+{
+    if (!idx || !d_start_points) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(idx->mu);
+    cudaSetDevice(idx->desc.device);
+    SearchTarget tgt;
+    tgt.d_sp = d_start_points;
+    tgt.sp_stride = sp_stride;
+    return search_device_impl(idx, idx->scratch, d_queries, nq, params, nullptr, nullptr, nullptr, 0, k_stride,
+                              d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps,
+                              static_cast<cudaStream_t>(stream), nullptr, &tgt);
+}
+
 extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *P,
                                    const uint32_t *Ls, const uint32_t *ks, const uint32_t *start_points,
                                    uint32_t n_start, uint32_t k_stride, uint32_t *out_ids, float *out_dists,

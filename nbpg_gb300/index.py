@@ -189,6 +189,16 @@ class Index:
         check(_lib.lib().nbpg_search_device(self._h, d_queries, nq, C.byref(prm), d_Ls, d_ks, _p(sp), len(sp),
                                             k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
 
+    def search_device_sp(self, d_queries: int, nq: int, qp: QueryParams, d_start_points: int, sp_stride: int,
+                         d_out_ids: int, k_stride: int, d_out_dists: int | None = None, d_count: int | None = None,
+                         d_visited: int | None = None, d_cmps: int | None = None, stream: int = 0,
+                         launch: "LaunchConfig | None" = None) -> None:
+        """As search_device with per-query start points (qsearchAll's get_sp(i)): sp_stride u32 per
+        query at d_start_points, padded with 0xFFFFFFFF after the first."""
+        prm = (launch or LaunchConfig()).params(qp)
+        check(_lib.lib().nbpg_search_device_sp(self._h, d_queries, nq, C.byref(prm), d_start_points, sp_stride,
+                                               k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
+
     def autotune(self, d_queries: int, nq: int, qp: QueryParams, start_points=(0,)):
         """nbpg_search_autotune: the fastest LaunchConfig for these device queries, and its ms per launch."""
         sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
@@ -295,12 +305,13 @@ class Hnsw:
     def search(self, queries: np.ndarray, qp: QueryParams, hier_beam: int = 1,
                launch: "LaunchConfig | None" = None) -> SearchResult:
         """hier_qsearchAll: vector ids of the k best per query, level-0 counters.  `launch` shapes
-        the level-0 search (default: the plain one-query-per-block kernel)."""
+        the level-0 search (default: the persistent kernel, which serves every L; the plain
+        one-query-per-block kernel is faster where its shared-memory slot fits)."""
         q = np.ascontiguousarray(queries)
         if q.ndim != 2 or q.shape[1] != self.index.dims:
             raise ValueError("queries must be (nq, dims)")
         nq, k = q.shape[0], int(qp.k)
-        prm = (launch or LaunchConfig(kernel="plain")).params(qp)
+        prm = (launch or LaunchConfig()).params(qp)
         ids = np.empty((nq, k), np.uint32)
         ds = np.empty((nq, k), np.float32)
         cnt, vis, cmps = (np.empty(nq, np.uint32) for _ in range(3))

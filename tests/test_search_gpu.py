@@ -150,3 +150,39 @@ def test_cuda_graph_replay_matches(gpu_lib, oracle_lib):
             for x, y in zip(got, o):
                 assert np.array_equal(x, y)
         gr.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["batched", "plain"])
+def test_search_with_per_query_start_points(gpu_lib, oracle_lib, kernel):
+    """nbpg_search_device_sp: each query starts from its own list (qsearchAll's get_sp(i)),
+    padded with 0xFFFFFFFF; equal to the oracle searching each query from its list."""
+    import torch
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import Index, LaunchConfig, QueryParams
+    b, q = synth.u8_mixture(4000, 120, dim=32, n_centres=16, seed=11)
+    g, *_ = oracle_lib.build_graph("u8", "l2", b, R=24, L=40, VL=64, num_split=0, num_passes=1)
+    idx = Index(b, "u8", "l2", max_degree=24)
+    idx.set_graph(g)
+    r = np.random.default_rng(3)
+    stride = 3
+    sps = np.full((len(q), stride), 0xFFFFFFFF, np.uint32)
+    for i in range(len(q)):
+        m = int(r.integers(1, stride + 1))
+        sps[i, :m] = r.integers(0, len(b), size=m)   # repeats allowed
+    _, rs, _, _ = idx.device_info()
+    dq = torch.zeros((len(q), rs), dtype=torch.uint8, device="cuda")
+    dq[:, :q.shape[1]] = torch.from_numpy(q).cuda()
+    dsp = torch.from_numpy(sps.view(np.int32)).cuda()
+    k, L = 10, 24
+    ids = torch.empty((len(q), k), dtype=torch.int32, device="cuda")
+    vis = torch.empty(len(q), dtype=torch.int32, device="cuda")
+    cm = torch.empty(len(q), dtype=torch.int32, device="cuda")
+    idx.search_device_sp(dq.data_ptr(), len(q), QueryParams(k=k, beamSize=L), dsp.data_ptr(), stride, ids.data_ptr(), k,
+                         d_visited=vis.data_ptr(), d_cmps=cm.data_ptr(), launch=LaunchConfig(kernel=kernel))
+    torch.cuda.synchronize()
+    gi, gv, gc = ids.cpu().numpy().view(np.uint32), vis.cpu().numpy(), cm.cpu().numpy()
+    for i in range(len(q)):
+        sp = tuple(int(x) for x in sps[i] if x != 0xFFFFFFFF)
+        o = oracle_lib.search("u8", "l2", b, g, q[i:i + 1], L=L, k=k, start_points=sp)
+        assert np.array_equal(gi[i], o[0][0]) and gv[i] == o[3][0] and gc[i] == o[4][0], (i, sp)
