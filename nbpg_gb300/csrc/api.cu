@@ -64,6 +64,8 @@ extern "C" nbpg_status nbpg_index_destroy(nbpg_index *idx)
     if (idx->d_graph) cudaFree(idx->d_graph);
     if (idx->d_raw) cudaFree(idx->d_raw);
     idx->scratch.release();
+    host_call_release(idx->host_call);
+    idx->host_call = nullptr;
     for (DevBuf *b : {&idx->qbuf, &idx->obuf, &idx->ghash, &idx->order_buf}) b->release();
     if (idx->stream) cudaStreamDestroy(idx->stream);
     delete idx;

@@ -98,6 +98,10 @@ struct SearchTarget {
     uint32_t sp_stride = 0;
 };
 
+// The cached CUDA graph of a host call (defined in search.cu); freed with the index.
+struct HostCall;
+void host_call_release(HostCall *hc);
+
 nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
                                const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
                                const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
@@ -122,5 +126,6 @@ struct nbpg_index {
     // scratch
     nbpg::SearchScratch scratch;  // used by the index's own search calls
     nbpg::DevBuf qbuf, obuf, ghash, order_buf;  // host-API staging; build-time visited filters
+    nbpg::HostCall *host_call = nullptr;        // the last pinned-buffer host call, as a CUDA graph
     std::mutex mu;
 };

@@ -343,6 +343,146 @@ extern "C" nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_quer
                               static_cast<cudaStream_t>(stream), nullptr, &tgt);
 }
 
+namespace nbpg {
+
+// A host call of nbpg_search replayed as one CUDA graph: the query upload, both search passes,
+// the result downloads and the error word.  Used when every host buffer is pinned (a graph's
+// copies read and write host memory at replay time) and L and k are uniform; the call's
+// pointers, parameters and start points are the key, and its own staging and scratch buffers
+// keep what the graph reads away from other calls.  One call's graph replaces a dozen runtime
+// calls and the gaps between them.
+struct HostCall {
+    const void *queries = nullptr;
+    uint32_t nq = 0, k_stride = 0;
+    nbpg_search_params P{};
+    std::vector<uint32_t> sp;
+    uint32_t *ids = nullptr, *cnt = nullptr, *vis = nullptr, *cmps = nullptr;
+    float *dists = nullptr;
+    SearchScratch sc;
+    DevBuf qbuf, obuf;
+    uint32_t *err_host = nullptr;  // pinned
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    bool same(const void *q, uint32_t n, const nbpg_search_params &p, const uint32_t *s, uint32_t ns, uint32_t kst,
+              uint32_t *i, float *d, uint32_t *c, uint32_t *v, uint32_t *m) const
+    {
+        return q == queries && n == nq && kst == k_stride && i == ids && d == dists && c == cnt && v == vis &&
+               m == cmps && std::memcmp(&p, &P, sizeof(P)) == 0 && sp.size() == ns &&
+               std::equal(s, s + ns, sp.begin());
+    }
+};
+
+void host_call_release(HostCall *hc)
+{
+    if (!hc) return;
+    if (hc->exec) cudaGraphExecDestroy(hc->exec);
+    if (hc->graph) cudaGraphDestroy(hc->graph);
+    if (hc->err_host) cudaFreeHost(hc->err_host);
+    hc->sc.release();
+    hc->qbuf.release();
+    hc->obuf.release();
+    delete hc;
+}
+
+static bool pinned(const void *p)
+{
+    if (!p) return true;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// The call's work on stream st: upload, search, downloads, error word (no synchronisation).
+static nbpg_status enqueue_host_call(nbpg_index *idx, HostCall *hc, cudaStream_t st)
+{
+    const uint32_t nq = hc->nq, kst = hc->k_stride;
+    uint8_t *dq = hc->qbuf.as<uint8_t>();
+    if (idx->row_bytes != idx->row_stride) NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, size_t(nq) * idx->row_stride, st));
+    NBPG_CUDA_TRY(cudaMemcpy2DAsync(dq, idx->row_stride, hc->queries, idx->row_bytes, idx->row_bytes, nq,
+                                    cudaMemcpyHostToDevice, st));
+    uint8_t *o = hc->obuf.as<uint8_t>();
+    uint32_t *d_ids = reinterpret_cast<uint32_t *>(o);
+    float *d_d = reinterpret_cast<float *>(o + size_t(nq) * kst * 4);
+    uint32_t *d_c = reinterpret_cast<uint32_t *>(o + size_t(nq) * kst * 8);
+    uint32_t *d_v = d_c + nq, *d_m = d_v + nq;
+    const nbpg_status s = search_device_impl(idx, hc->sc, dq, nq, &hc->P, nullptr, nullptr, hc->sp.data(),
+                                             uint32_t(hc->sp.size()), kst, d_ids, d_d, d_c, d_v, d_m, st);
+    if (s != NBPG_OK) return s;
+    NBPG_CUDA_TRY(cudaMemcpyAsync(hc->ids, d_ids, size_t(nq) * kst * 4, cudaMemcpyDeviceToHost, st));
+    if (hc->dists) NBPG_CUDA_TRY(cudaMemcpyAsync(hc->dists, d_d, size_t(nq) * kst * 4, cudaMemcpyDeviceToHost, st));
+    if (hc->cnt) NBPG_CUDA_TRY(cudaMemcpyAsync(hc->cnt, d_c, nq * 4, cudaMemcpyDeviceToHost, st));
+    if (hc->vis) NBPG_CUDA_TRY(cudaMemcpyAsync(hc->vis, d_v, nq * 4, cudaMemcpyDeviceToHost, st));
+    if (hc->cmps) NBPG_CUDA_TRY(cudaMemcpyAsync(hc->cmps, d_m, nq * 4, cudaMemcpyDeviceToHost, st));
+    NBPG_CUDA_TRY(cudaMemcpyAsync(hc->err_host, hc->sc.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+    return NBPG_OK;
+}
+
+// Runs a pinned-buffer host call: replays its graph when the call repeats, else runs it once
+// and captures it for the next time.
+static nbpg_status host_call_graphed(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params &P,
+                                     const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *ids,
+                                     float *dists, uint32_t *cnt, uint32_t *vis, uint32_t *cmps)
+{
+    cudaStream_t st = idx->stream;
+    HostCall *hc = idx->host_call;
+    if (!(hc && hc->exec && hc->same(queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps))) {
+        host_call_release(hc);
+        idx->host_call = hc = new HostCall();
+        hc->queries = queries;
+        hc->nq = nq;
+        hc->k_stride = k_stride;
+        hc->P = P;
+        hc->sp.assign(sp, sp + nsp);
+        hc->ids = ids;
+        hc->dists = dists;
+        hc->cnt = cnt;
+        hc->vis = vis;
+        hc->cmps = cmps;
+        nbpg_status s;
+        if ((s = hc->qbuf.ensure(size_t(nq) * idx->row_stride)) != NBPG_OK ||
+            (s = hc->obuf.ensure(size_t(nq) * (size_t(k_stride) * 8 + 12) + 64)) != NBPG_OK)
+            return s;
+        NBPG_CUDA_TRY(cudaHostAlloc(&hc->err_host, 4, cudaHostAllocDefault));
+        *hc->err_host = 0;
+        // this call, uncaptured (sizes the scratch, stages the start points, plans the launches)
+        if ((s = enqueue_host_call(idx, hc, st)) != NBPG_OK) return s;
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+        const uint32_t err = *hc->err_host;
+        // the same work captured for the calls that repeat it
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            s = enqueue_host_call(idx, hc, st);
+            cudaError_t e2 = cudaStreamEndCapture(st, &hc->graph);
+            if (e2 != cudaSuccess) e = e2;
+        }
+        if (s == NBPG_OK && e == cudaSuccess) e = cudaGraphInstantiate(&hc->exec, hc->graph, 0);
+        if (s != NBPG_OK || e != cudaSuccess) {  // no graph: later calls take the plain path
+            cudaGetLastError();
+            host_call_release(hc);
+            idx->host_call = nullptr;
+        }
+        if (err) {
+            set_error("a query was rejected on the device (k > L or L above the planned maximum)");
+            return NBPG_ERR_INVALID_ARG;
+        }
+        return NBPG_OK;
+    }
+    *hc->err_host = 0;
+    NBPG_CUDA_TRY(cudaGraphLaunch(hc->exec, st));
+    NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (*hc->err_host) {
+        set_error("a query was rejected on the device (k > L or L above the planned maximum)");
+        return NBPG_ERR_INVALID_ARG;
+    }
+    return NBPG_OK;
+}
+
+}  // namespace nbpg
+
 extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *P,
                                    const uint32_t *Ls, const uint32_t *ks, const uint32_t *start_points,
                                    uint32_t n_start, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
@@ -352,6 +492,18 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     std::lock_guard<std::mutex> g(idx->mu);
     cudaSetDevice(idx->desc.device);
     if (nq == 0) return NBPG_OK;
+    if (!Ls && !ks && start_points && n_start >= 1 && n_start <= 256) {
+        // a repeat of the cached call (whose buffers were pinned when it was made), or a new
+        // call whose buffers are all pinned
+        const HostCall *hc = idx->host_call;
+        if ((hc && hc->exec &&
+             hc->same(queries, nq, *P, start_points, n_start, k_stride, out_ids, out_dists, out_count, out_visited,
+                      out_cmps)) ||
+            (pinned(queries) && pinned(out_ids) && pinned(out_dists) && pinned(out_count) && pinned(out_visited) &&
+             pinned(out_cmps)))
+            return host_call_graphed(idx, queries, nq, *P, start_points, n_start, k_stride, out_ids, out_dists,
+                                     out_count, out_visited, out_cmps);
+    }
     nbpg_search_params p = *P;
     if (Ls || ks) {
         uint32_t Lmax = 0;

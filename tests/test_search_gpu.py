@@ -186,3 +186,43 @@ def test_search_with_per_query_start_points(gpu_lib, oracle_lib, kernel):
         sp = tuple(int(x) for x in sps[i] if x != 0xFFFFFFFF)
         o = oracle_lib.search("u8", "l2", b, g, q[i:i + 1], L=L, k=k, start_points=sp)
         assert np.array_equal(gi[i], o[0][0]) and gv[i] == o[3][0] and gc[i] == o[4][0], (i, sp)
+
+
+@pytest.mark.gpu
+def test_host_call_graph_replay_follows_the_buffers(gpu_lib):
+    """nbpg_search with pinned host buffers runs once, is captured, and replays as a CUDA graph
+    on repeats: results equal the plain path's, and new query contents in the same buffers give
+    new results (the graph's copies read the buffers at replay time)."""
+    import ctypes as C
+    import torch
+    from nbpg_gb300 import _lib, synth
+    from nbpg_gb300.index import Index, QueryParams
+    from oracle.oracle import oracle
+    b, q = synth.u8_mixture(5000, 300, dim=64, n_centres=20, seed=5)
+    g, *_ = oracle().build_graph("u8", "l2", b, R=24, L=40, VL=64, num_split=0, num_passes=1)
+    idx = Index(b, "u8", "l2", max_degree=24)
+    idx.set_graph(g)
+    qp = QueryParams(k=10, beamSize=30)
+    ref_a = idx.search(q[:150], qp)                        # pageable: the plain path
+    ref_b = idx.search(q[150:], qp)
+    L = _lib.lib()
+    qh = torch.from_numpy(q[:150].copy()).pin_memory()
+    oi = torch.empty((150, 10), dtype=torch.int32).pin_memory()
+    od = torch.empty((150, 10), dtype=torch.float32).pin_memory()
+    ov = torch.empty(150, dtype=torch.int32).pin_memory()
+    prm = _lib.SearchParams(10, 30, 1.35, 0, 0, 8, _lib.KERNELS["batched"], 0, 0, -1)
+    sp = (C.c_uint32 * 1)(0)
+    u32p = C.POINTER(C.c_uint32)
+
+    def call():
+        _lib.check(L.nbpg_search(idx.handle, qh.data_ptr(), 150, C.byref(prm), None, None, sp, 1, 10,
+                                 C.cast(oi.data_ptr(), u32p), C.cast(od.data_ptr(), C.POINTER(C.c_float)), None,
+                                 C.cast(ov.data_ptr(), u32p), None))
+    for rep in range(3):                                  # capture on the first, replays after
+        call()
+        assert np.array_equal(oi.numpy().view(np.uint32), ref_a.ids), rep
+        assert np.array_equal(od.numpy(), ref_a.dists) and np.array_equal(ov.numpy().view(np.uint32), ref_a.visited)
+    qh.copy_(torch.from_numpy(q[150:].copy()))              # same buffers, new queries
+    call()
+    assert np.array_equal(oi.numpy().view(np.uint32), ref_b.ids)
+    assert np.array_equal(ov.numpy().view(np.uint32), ref_b.visited)
