@@ -443,7 +443,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--save-graph", default=None, help="write the built graph (.graph format) here")
     ap.add_argument("--load-graph", default=None, help="use this graph instead of building one")
-    ap.add_argument("--profile", default=None, choices=["search", "gt"],
+    ap.add_argument("--profile", default=None, choices=["search", "gt", "builds"],
                     help="profiling run: warmup + steps of one kernel only (the search at --L, or the brute-force kNN)")
     ap.add_argument("--gt-engine", default="tensor", choices=["tensor", "dp4a"], help="--profile gt engine")
     ap.add_argument("--L", type=int, default=0, help="beam width for --profile (default: the sweep's choice)")
@@ -478,6 +478,27 @@ def main():
             ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local, engine=args.gt_engine)
         print(json.dumps({"profile": "ground truth", "engine": args.gt_engine,
                           "launches": args.warmup + args.steps}), flush=True)
+        return
+
+    if args.profile == "builds":
+        # the three builders once each on the first 200k rows (the launch list of the build rows):
+        # NBPG at the workload's settings, FGIM at the same, HNSW at its driver's defaults
+        sub = np.ascontiguousarray(base[:200_000])
+        t = {}
+        for name in ("nbpg", "fgim", "hnsw"):
+            bi = Index(sub, "u8", "l2", max_degree=CFG["R"], device=local)
+            kw = dict(L=CFG["L_build"], VL=CFG["VL"], num_split=CFG["num_split"], num_passes=CFG["num_passes"],
+                      dynamic_prune=CFG["dynamic_prune"], min_alpha=CFG["min_alpha"], max_alpha=CFG["max_alpha"])
+            if name == "nbpg":
+                st, _, _ = bi.build_vamana(sp_seed=0, **kw)
+            elif name == "fgim":
+                st, _, _ = bi.build_fgim(**kw)
+            else:
+                h, st = bi.build_hnsw(L=70, VL=140, alpha=1.1, hier_beam=1)
+                h.close()
+            t[name] = st.seconds
+            bi.close()
+        print(json.dumps({"profile": "builds", "n": len(sub), "seconds": t}), flush=True)
         return
 
     # index + build on the GPU
