@@ -346,7 +346,8 @@ extern "C" nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_quer
 namespace nbpg {
 
 // A host call of nbpg_search replayed as one CUDA graph: the query upload, both search passes,
-// the result downloads and the error word.  Used when every host buffer is pinned (a graph's
+// the result downloads and the error word (or, where the caller's pinned buffers map into the
+// device's address space with unpadded rows, the passes reading and writing them directly).  Used when every host buffer is pinned (a graph's
 // copies read and write host memory at replay time) and L and k are uniform; the call's
 // pointers, parameters and start points are the key, and its own staging and scratch buffers
 // keep what the graph reads away from other calls.  One call's graph replaces a dozen runtime
@@ -363,6 +364,12 @@ struct HostCall {
     uint32_t *err_host = nullptr;  // pinned
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // zero-copy form: the kernels read the queries from, and write the results into, the
+    // caller's pinned buffers through their device mappings (no staging copies)
+    bool direct = false;
+    const void *dev_queries = nullptr;
+    uint32_t *dev_ids = nullptr, *dev_cnt = nullptr, *dev_vis = nullptr, *dev_cmps = nullptr;
+    float *dev_dists = nullptr;
 
     bool same(const void *q, uint32_t n, const nbpg_search_params &p, const uint32_t *s, uint32_t ns, uint32_t kst,
               uint32_t *i, float *d, uint32_t *c, uint32_t *v, uint32_t *m) const
@@ -396,10 +403,37 @@ static bool pinned(const void *p)
     return a.type == cudaMemoryTypeHost;
 }
 
+// The device address of a pinned host buffer (null stays null); false when it has none.
+template <class T>
+static bool mapped(T *host, T **dev)
+{
+    if (!host) {
+        *dev = nullptr;
+        return true;
+    }
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, const_cast<void *>(static_cast<const void *>(host)), 0) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    *dev = static_cast<T *>(d);
+    return (reinterpret_cast<uintptr_t>(d) & 15u) == 0;
+}
+
 // The call's work on stream st: upload, search, downloads, error word (no synchronisation).
 static nbpg_status enqueue_host_call(nbpg_index *idx, HostCall *hc, cudaStream_t st)
 {
     const uint32_t nq = hc->nq, kst = hc->k_stride;
+    if (hc->direct) {
+        // the search kernels read each query row from the caller's buffer and write each
+        // result row into the caller's buffers over the host link
+        const nbpg_status s = search_device_impl(idx, hc->sc, hc->dev_queries, nq, &hc->P, nullptr, nullptr,
+                                                 hc->sp.data(), uint32_t(hc->sp.size()), kst, hc->dev_ids,
+                                                 hc->dev_dists, hc->dev_cnt, hc->dev_vis, hc->dev_cmps, st);
+        if (s != NBPG_OK) return s;
+        NBPG_CUDA_TRY(cudaMemcpyAsync(hc->err_host, hc->sc.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+        return NBPG_OK;
+    }
     uint8_t *dq = hc->qbuf.as<uint8_t>();
     if (idx->row_bytes != idx->row_stride) NBPG_CUDA_TRY(cudaMemsetAsync(dq, 0, size_t(nq) * idx->row_stride, st));
     NBPG_CUDA_TRY(cudaMemcpy2DAsync(dq, idx->row_stride, hc->queries, idx->row_bytes, idx->row_bytes, nq,
@@ -443,8 +477,12 @@ static nbpg_status host_call_graphed(nbpg_index *idx, const void *queries, uint3
         hc->vis = vis;
         hc->cmps = cmps;
         nbpg_status s;
-        if ((s = hc->qbuf.ensure(size_t(nq) * idx->row_stride)) != NBPG_OK ||
-            (s = hc->obuf.ensure(size_t(nq) * (size_t(k_stride) * 8 + 12) + 64)) != NBPG_OK)
+        hc->direct = idx->row_bytes == idx->row_stride && mapped(queries, &hc->dev_queries) &&
+                     mapped(ids, &hc->dev_ids) && mapped(dists, &hc->dev_dists) && mapped(cnt, &hc->dev_cnt) &&
+                     mapped(vis, &hc->dev_vis) && mapped(cmps, &hc->dev_cmps);
+        if (!hc->direct &&
+            ((s = hc->qbuf.ensure(size_t(nq) * idx->row_stride)) != NBPG_OK ||
+             (s = hc->obuf.ensure(size_t(nq) * (size_t(k_stride) * 8 + 12) + 64)) != NBPG_OK))
             return s;
         NBPG_CUDA_TRY(cudaHostAlloc(&hc->err_host, 4, cudaHostAllocDefault));
         *hc->err_host = 0;
