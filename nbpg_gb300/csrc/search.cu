@@ -463,7 +463,17 @@ static nbpg_status host_call_graphed(nbpg_index *idx, const void *queries, uint3
 {
     cudaStream_t st = idx->stream;
     HostCall *hc = idx->host_call;
-    if (!(hc && hc->exec && hc->same(queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps))) {
+    bool reuse = hc && hc->exec && hc->same(queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps);
+    if (reuse && hc->direct) {
+        // the buffers' device mappings are the ones the graph was captured with
+        const void *dq = nullptr;
+        uint32_t *di = nullptr, *dc = nullptr, *dv = nullptr, *dm = nullptr;
+        float *dd = nullptr;
+        reuse = mapped(queries, &dq) && mapped(ids, &di) && mapped(dists, &dd) && mapped(cnt, &dc) &&
+                mapped(vis, &dv) && mapped(cmps, &dm) && dq == hc->dev_queries && di == hc->dev_ids &&
+                dd == hc->dev_dists && dc == hc->dev_cnt && dv == hc->dev_vis && dm == hc->dev_cmps;
+    }
+    if (!reuse) {
         host_call_release(hc);
         idx->host_call = hc = new HostCall();
         hc->queries = queries;
@@ -530,18 +540,12 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     std::lock_guard<std::mutex> g(idx->mu);
     cudaSetDevice(idx->desc.device);
     if (nq == 0) return NBPG_OK;
-    if (!Ls && !ks && start_points && n_start >= 1 && n_start <= 256) {
-        // a repeat of the cached call (whose buffers were pinned when it was made), or a new
-        // call whose buffers are all pinned
-        const HostCall *hc = idx->host_call;
-        if ((hc && hc->exec &&
-             hc->same(queries, nq, *P, start_points, n_start, k_stride, out_ids, out_dists, out_count, out_visited,
-                      out_cmps)) ||
-            (pinned(queries) && pinned(out_ids) && pinned(out_dists) && pinned(out_count) && pinned(out_visited) &&
-             pinned(out_cmps)))
-            return host_call_graphed(idx, queries, nq, *P, start_points, n_start, k_stride, out_ids, out_dists,
-                                     out_count, out_visited, out_cmps);
-    }
+    // every host buffer pinned, checked on every call (a buffer freed and its address reused by
+    // pageable memory must not be reached through a stale mapping)
+    if (!Ls && !ks && start_points && n_start >= 1 && n_start <= 256 && pinned(queries) && pinned(out_ids) &&
+        pinned(out_dists) && pinned(out_count) && pinned(out_visited) && pinned(out_cmps))
+        return host_call_graphed(idx, queries, nq, *P, start_points, n_start, k_stride, out_ids, out_dists, out_count,
+                                 out_visited, out_cmps);
     nbpg_search_params p = *P;
     if (Ls || ks) {
         uint32_t Lmax = 0;
