@@ -11,7 +11,14 @@
 //                      hier_beamSize visited nodes, moved one level down, are the next level's
 //                      entry points (hnsw.h:52-83, 178-215; hier_utils.h:24-50).
 // then the flat build's reverse-edge kernels over all levels' lists of the batch at once
-// (hnsw.h:218-222, nsw.h:446-485).
+// (hnsw.h:218-222, nsw.h:446-485).  Each insert's visited filter lives in global memory,
+// cleared once per batch and carried across the level launches, as the reference's search cell
+// is across an insert's levels (hnsw.h:158-190): edges between levels (from the entry node of
+// the first insert, or from the repair) can bring a node seen above into a search below.
+//
+// Queries: hnsw_descend_kernel walks the levels above 0 and leaves each query's level-0 entry
+// points; the level-0 search is the flat search (search.cu) over the nodes' rows with those
+// per-query start points, and hnsw_root_ids_kernel turns node ids into vector ids.
 #pragma once
 #include "build_impl.cuh"
 
