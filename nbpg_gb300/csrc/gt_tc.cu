@@ -424,6 +424,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         while (L.P < k - L.lo) L.P <<= 1;
         TkState S{0u, 0u, -3.402823466e38f, -3.402823466e38f};
         uint32_t qlen = 0;  // queued flagged candidates, in id order
+        bool done = true;   // every tile consumed (false after a timed-out wait)
         // t_j = |b|^2 - 2 q.b (L2) or -q.b (IP) per candidate: the distance / scale minus
         // |q|^2 (L2).  A candidate can survive only if t_j < thr = B / scale - |q|^2.
         // Until the list holds k entries everything passes; padding queries never do.
@@ -438,7 +439,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t s = t % TC_ACC, ph = (t / TC_ACC) & 1;
             // warp-uniform wait so that the warp stays converged for tcgen05.ld
             const bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
-            if (!ok) break;
+            if (!ok) {
+                done = false;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             for (uint32_t c = 0; c < TC_N / 32; ++c) {
                 const uint64_t id0 = uint64_t(t) * TC_N + c * 32;
@@ -529,25 +533,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
             thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
         }
-        // output sorted by (dist, id) (CompGT.cpp:107-124)
-        if (live && S.cnt == k) {
-            // sort (dist, id) in place: distances in shared memory, ids in the output row
-            uint32_t *ids = L.id;
+        // output sorted by (dist, id) (CompGT.cpp:107-124).  Every tile has been through the
+        // MMA, so the operand area is free: the ids go there, [k][128] so that a thread's
+        // entries stride 128 words, and the insertion sort runs on shared memory only.
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        uint32_t *sid = reinterpret_cast<uint32_t *>(smem);
+        if (done && live && S.cnt == k) {
+            for (uint32_t l = 0; l < k; ++l) sid[l * TC_M + tid] = L.id[l];
             for (uint32_t i = 1; i < k; ++i) {
                 const float dv = tk_d[i * TC_M + tid];
-                const uint32_t iv = ids[i];
+                const uint32_t iv = sid[i * TC_M + tid];
                 int32_t j = int32_t(i) - 1;
                 while (j >= 0) {
                     const float dj = tk_d[j * TC_M + tid];
-                    if (!(dj > dv || (dj == dv && ids[j] > iv))) break;
+                    const uint32_t ij = sid[j * TC_M + tid];
+                    if (!(dj > dv || (dj == dv && ij > iv))) break;
                     tk_d[(j + 1) * TC_M + tid] = dj;
-                    ids[j + 1] = ids[j];
+                    sid[(j + 1) * TC_M + tid] = ij;
                     --j;
                 }
                 tk_d[(j + 1) * TC_M + tid] = dv;
-                ids[j + 1] = iv;
+                sid[(j + 1) * TC_M + tid] = iv;
             }
-            for (uint32_t l = 0; l < k; ++l) a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
+            for (uint32_t l = 0; l < k; ++l) {
+                L.id[l] = sid[l * TC_M + tid];
+                a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -633,11 +644,14 @@ size_t gt_tc_smem(uint32_t katoms, uint32_t k, uint32_t stages)
     return need > 120 * 1024 ? need : 120 * 1024;
 }
 
-// deepest ring that fits, 0 if even two stages do not
+// deepest ring that fits, 0 if even two stages do not; the final sort reuses the operand
+// area (query tile + ring) for the ids, so it must hold k x 128 of them
 static uint32_t gt_tc_stages(uint32_t katoms, uint32_t k, size_t smem_optin)
 {
     for (uint32_t st = TC_MAX_STAGES; st >= 2; --st)
-        if (gt_tc_smem(katoms, k, st) <= smem_optin) return st;
+        if (gt_tc_smem(katoms, k, st) <= smem_optin &&
+            size_t(katoms) * TC_M * 128 * (1 + st) >= size_t(k) * TC_M * 4)
+            return st;
     return 0;
 }
 
