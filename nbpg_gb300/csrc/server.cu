@@ -109,7 +109,17 @@ void nbpg_server::run()
         bool progress = false;
         // 1. drain completed batches
         for (auto &b : slots) {
-            if (!b.busy || cudaEventQuery(b.ev) != cudaSuccess) continue;
+            if (!b.busy) continue;
+            const cudaError_t q = cudaEventQuery(b.ev);
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess) {
+                // the batch's work failed on the device: report it to submit/poll and stop
+                std::lock_guard<std::mutex> g(mu);
+                error = int(NBPG_ERR_CUDA);
+                error_text = std::string("nbpg_serve: a batch failed on the device: ") + cudaGetErrorString(q);
+                stop = true;
+                break;
+            }
             const int64_t t = now_ns();
             std::lock_guard<std::mutex> g(mu);
             for (size_t i = 0; i < b.reqs.size(); ++i) {
@@ -124,6 +134,7 @@ void nbpg_server::run()
             b.busy = false;
             progress = true;
         }
+        if (stop.load()) break;
         // 2. admit and launch on a free slot
         BatchSlot *free = nullptr;
         for (auto &b : slots)
