@@ -75,7 +75,7 @@ extern "C" nbpg_status nbpg_index_destroy(nbpg_index *idx)
 extern "C" nbpg_status nbpg_index_set_points(nbpg_index *idx, const void *rows, uint64_t first, uint64_t count)
 {
     NBPG_CHECK_ARG(idx && (rows || count == 0), "null argument");
-    NBPG_CHECK_ARG(first + count <= idx->desc.n, "rows out of range");
+    NBPG_CHECK_ARG(first <= idx->desc.n && count <= idx->desc.n - first, "rows out of range");
     if (count == 0) return NBPG_OK;
     std::lock_guard<std::mutex> g(idx->mu);
     NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
@@ -88,7 +88,7 @@ extern "C" nbpg_status nbpg_index_set_points(nbpg_index *idx, const void *rows, 
 extern "C" nbpg_status nbpg_index_set_graph(nbpg_index *idx, const uint32_t *rows, uint64_t first, uint64_t count)
 {
     NBPG_CHECK_ARG(idx && (rows || count == 0), "null argument");
-    NBPG_CHECK_ARG(first + count <= idx->desc.n, "rows out of range");
+    NBPG_CHECK_ARG(first <= idx->desc.n && count <= idx->desc.n - first, "rows out of range");
     if (count == 0) return NBPG_OK;
     const uint32_t R = idx->desc.max_degree;
     const uint64_t n = idx->desc.n;
@@ -116,7 +116,7 @@ extern "C" nbpg_status nbpg_index_get_graph(const nbpg_index *cidx, uint32_t *ro
 {
     auto *idx = const_cast<nbpg_index *>(cidx);
     NBPG_CHECK_ARG(idx && (rows || count == 0), "null argument");
-    NBPG_CHECK_ARG(first + count <= idx->desc.n, "rows out of range");
+    NBPG_CHECK_ARG(first <= idx->desc.n && count <= idx->desc.n - first, "rows out of range");
     if (count == 0) return NBPG_OK;
     std::lock_guard<std::mutex> g(idx->mu);
     NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));

@@ -152,7 +152,7 @@ extern "C" nbpg_status nbpg_index_set_raw_points(nbpg_index *idx, uint32_t raw_d
 {
     NBPG_CHECK_ARG(idx && (rows || count == 0), "null argument");
     NBPG_CHECK_ARG(raw_dtype <= NBPG_F32 && raw_dims >= 1, "bad raw dtype/dims");
-    NBPG_CHECK_ARG(first + count <= idx->desc.n, "rows out of range");
+    NBPG_CHECK_ARG(first <= idx->desc.n && count <= idx->desc.n - first, "rows out of range");
     std::lock_guard<std::mutex> g(idx->mu);
     NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
     const uint32_t rb = raw_row_bytes(raw_dtype, raw_dims);
