@@ -32,7 +32,7 @@ typedef enum nbpg_status {
     NBPG_ERR_CUDA = 3,        /* a CUDA call failed; see nbpg_last_error() */
     NBPG_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
     NBPG_ERR_FORMAT = 5,      /* malformed graph or vector data */
-    NBPG_ERR_UNSUPPORTED = 6  /* valid request outside what this build supports */
+    NBPG_ERR_UNSUPPORTED = 6  /* valid request outside what this library supports */
 } nbpg_status;
 
 /* Element types: Point<uint8_t>, Point<int8_t>, Point<uint4_2>, Point<int4_2>,

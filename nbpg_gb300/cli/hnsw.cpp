@@ -155,7 +155,7 @@ int main(int argc, char **argv)
 
     // ---- query evaluation (HNSW.cpp:244-288, hier_check_nn_Recall.h)
     if (a.quant_query_path.empty() || a.gt_path.empty()) { nbpg_index_destroy(idx); return 0; }
-    if (!a.base_path.empty()) die("nbpg_hnsw: re-ranked HNSW queries (--base_path) are not supported by this build");
+    if (!a.base_path.empty()) die("nbpg_hnsw: re-ranked HNSW queries (--base_path) are not supported by this library");
     uint32_t nq, qd;
     std::vector<uint8_t> Q = read_rows(a.quant_query_path, nq, qd, a.q_num);
     if (qd != dims) die("query and base dimensions differ");

@@ -4,7 +4,7 @@ Loads ``_build/libnbpg_oracle.so`` (the C++ restatement of the reference's
 algorithms) and, where it was built, ``_ref/libnbpg_ref.so`` (a harness compiled
 from the reference's own headers).  Both export the same C ABI with the prefixes
 ``nbpg_oracle_`` and ``nbpg_ref_``.  Only tests, ``__graft_entry__.smoke`` and the
-CPU-baseline leg of ``bench.py`` use this module, always as the checker or the
+CPU-baseline leg of ``bench.py`` use this module, always as the reference results or the
 timed CPU baseline; the product never imports it.
 """
 from __future__ import annotations
