@@ -51,3 +51,17 @@ def test_oracle_matches_reference_harness(oracle_lib, ref_lib):
                                  dynamic_prune=dyn, max_alpha=1.2, min_alpha=1.05, sp_seed=3)
         assert np.array_equal(go[0], gr[0]) and np.array_equal(go[1], gr[1]) and np.array_equal(go[2], gr[2])
         assert go[3] == gr[3]
+
+
+def test_oracle_build_is_independent_of_thread_count(oracle_lib):
+    """The batched build is batch-synchronous, as the reference's OpenMP phases are: every
+    insert of a batch searches the graph as it stood before the batch and the reverse edges
+    are merged in a fixed order, so the graph and the per-node counters do not depend on how
+    many threads run the batch (NBPG passes with split stage and dynamic prune)."""
+    from nbpg_gb300 import synth
+    base, _ = synth.u8_mixture(6000, 1, dim=32, n_centres=16)
+    runs = [oracle_lib.build_graph("u8", "l2", base, R=24, L=40, VL=64, num_split=4, num_passes=2,
+                                   dynamic_prune=True, min_alpha=1.05, max_alpha=1.1, sp_seed=3, threads=t)
+            for t in (1, 4)]
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
