@@ -21,6 +21,8 @@ ORACLE_SO = os.path.join(HERE, "_build", "libnbpg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnbpg_ref.so")
 REF_COMPGT = os.path.join(HERE, "_ref", "CompGT")
 REF_VAMANA = os.path.join(HERE, "_ref", "Vamana")
+# where the reference sources lie, on the machines that have them (the harness recipe reads them there)
+REF_ROOT = os.environ.get("NBPG_REF_ROOT", "/root/reference")
 
 DTYPES = {"u8": 0, "i8": 1, "u4": 2, "i4": 3, "f32": 4}
 METRICS = {"l2": 0, "ip": 1}
@@ -35,7 +37,7 @@ _i64p = C.POINTER(C.c_int64)
 def build(ref_root: str | None = None) -> None:
     """Compile the oracle (and the reference harness when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    ref_root = ref_root or "/root/reference"
+    ref_root = ref_root or REF_ROOT
     if os.path.isdir(ref_root):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
 
