@@ -217,7 +217,9 @@ nbpg_status nbpg_serve_open(nbpg_index *idx, const nbpg_serve_config *cfg, const
 nbpg_status nbpg_serve_submit(nbpg_server *s, const void *queries, uint32_t count, const uint32_t *Ls,
                               const uint32_t *ks, const uint64_t *request_ids, const int64_t *arrival_ns,
                               uint32_t *accepted);
-/* Collect up to max_results finished requests (ids/dists rows of k_stride >= max_k entries). */
+/* Collect up to max_results finished requests (ids/dists rows of k_stride >= max_k entries).
+ * A batch that failed on the device stops the server: submit and poll then return that
+ * error (NBPG_ERR_CUDA) with its message; close the server. */
 nbpg_status nbpg_serve_poll(nbpg_server *s, uint32_t max_results, uint32_t k_stride, uint64_t *request_ids,
                             uint32_t *out_ids, float *out_dists, uint32_t *out_count, double *latency_ms,
                             uint32_t *n_out);
