@@ -83,3 +83,21 @@ def test_oracle_hnsw_refusals(oracle_lib):
     # a visited cap of 2L above VL overruns the reference's per-cell buffers
     with pytest.raises(RuntimeError, match="1"):
         oracle_lib.build_hnsw("u8", "l2", z["base"], R=16, L=30, VL=48)
+
+
+def test_hnsw_sizes_entry_equals_the_driver_defaults(oracle_lib):
+    """nbpg_hnsw_sizes (host code of the library, no device work) against the oracle's
+    restatement of HNSW.cpp:77-80: m_l = 1 / ln(R) when unset, node capacity
+    (exp(-1 / m_l) * 2 + 1) * n truncated, both only when not given."""
+    import ctypes as C
+    from nbpg_gb300 import _lib
+    L = _lib.lib()
+    ml, mn = C.c_double(), C.c_uint64()
+    for n in (1, 1000, 99_999, 1_000_000, 10_000_000):
+        for R in (2, 16, 32, 48, 64, 128):
+            for m_l in (0.0, 0.3, 1.7):
+                for max_node in (0, 12_345):
+                    assert L.nbpg_hnsw_sizes(n, R, m_l, max_node, C.byref(ml), C.byref(mn)) == 0
+                    want = oracle_lib.hnsw_sizes(n, R, m_l, max_node)
+                    assert (ml.value, mn.value) == want, (n, R, m_l, max_node)
+    assert L.nbpg_hnsw_sizes(1000, 1, 0.0, 0, C.byref(ml), C.byref(mn)) == 1  # ln(1) = 0: no default m_l
