@@ -203,6 +203,8 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
 
     DevBuf d_inserts, d_sp, d_alpha, d_cos, d_pop, d_sv, d_sd, d_res_ids, d_res_d, d_res_cnt, d_rank, d_cnt, d_off,
         d_bump, d_grp, d_edges, d_queue;
+    ReleaseOnExit release_bufs{{&d_inserts, &d_sp, &d_alpha, &d_cos, &d_pop, &d_sv, &d_sd, &d_res_ids, &d_res_d,
+                                &d_res_cnt, &d_rank, &d_cnt, &d_off, &d_bump, &d_grp, &d_edges, &d_queue}};
     auto fail_oom = [&](nbpg_status x) { return x; };
     if ((s = d_inserts.ensure(n * 4)) || (s = d_sp.ensure(n * nsp_max * 4)) || (s = d_alpha.ensure(n * 4)) ||
         (s = d_cos.ensure(n * 4)) || (s = d_pop.ensure(n * 4)) || (s = d_sv.ensure(n * 4)) ||
@@ -245,6 +247,7 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
 
     // FGIM: the graph the pair passes write (toG), which becomes the index's graph
     DevBuf d_tog;
+    ReleaseOnExit release_tog{{&d_tog}};
     uint32_t *tog = nullptr;
     if (fgim) {
         if ((s = d_tog.ensure(size_t(n) * idx->gstride * 4)) != NBPG_OK) return s;

@@ -63,6 +63,16 @@ struct DevBuf {
     T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Releases a function's local buffers on every return path, the early error returns
+// included (cudaFree waits for the device's work first).
+struct ReleaseOnExit {
+    std::vector<DevBuf *> bufs;
+    ~ReleaseOnExit()
+    {
+        for (DevBuf *b : bufs) b->release();
+    }
+};
+
 // Per-launch-sequence device scratch of the search: work counters, the tainted-query
 // list, start points, and global visited-filter / visited-list blocks for large L.
 // Launches that may overlap on the device need separate scratch.

@@ -199,6 +199,7 @@ extern "C" nbpg_status nbpg_search_rerank(nbpg_index *idx, const void *queries, 
     cudaStream_t st = idx->stream;
     const uint32_t rb = idx->raw_row_bytes;
     DevBuf work;
+    ReleaseOnExit release_work{{&work}};
     const size_t qbytes = size_t(nq) * idx->row_stride, rqbytes = size_t(nq) * rb;
     const size_t cand_b = size_t(nq) * cs * 4, outb = size_t(nq) * k_stride * 4;
     nbpg_status s = work.ensure(qbytes + rqbytes + 2 * cand_b + outb * 2 + size_t(nq) * 4 * 6 + 1024);
@@ -322,6 +323,7 @@ extern "C" nbpg_status nbpg_eval_recall(nbpg_index *idx, int32_t use_raw, const 
     const uint32_t dims = use_raw ? idx->raw_dims : idx->desc.dims;
     const uint32_t qrow = use_raw ? idx->raw_row_bytes : idx->row_bytes;
     DevBuf w;
+    ReleaseOnExit release_w{{&w}};
     const size_t qb = size_t(nq) * qrow, ib = size_t(nq) * k_stride * 4, gb = size_t(nq) * gk * 4;
     nbpg_status s = w.ensure(qb + ib + gb + size_t(nq) * 4 + 1024);
     if (s != NBPG_OK) return s;
