@@ -53,6 +53,28 @@ def test_oracle_matches_reference_harness(oracle_lib, ref_lib):
         assert go[3] == gr[3]
 
 
+
+@pytest.mark.parametrize("dtype,metric,dims", [("i8", "l2", 24), ("i8", "ip", 24), ("u4", "l2", 16), ("u4", "ip", 16),
+                                               ("i4", "l2", 16), ("i4", "ip", 16), ("u8", "ip", 32)])
+def test_oracle_matches_reference_harness_every_row_type(oracle_lib, ref_lib, dtype, metric, dims):
+    """The same pins for the other row types and metrics the GPU tests are checked on: searches
+    (ids, distances, counts, expansions, distance counts) and builds (graph, per-node counters,
+    isolated count) with and without the split stage, dynamic prune and top_degree interpolation."""
+    base, q, g = dataset(dtype, metric, dims=dims)
+    for L, k in [(10, 10), (64, 50)]:
+        o = oracle_lib.search(dtype, metric, base, g, q, L=L, k=k)
+        r = ref_lib.search(dtype, metric, base, g, q, L=L, k=k)
+        for x, y in zip(o, r):
+            assert np.array_equal(x, y), (L, k)
+    for split, passes, dyn, td in [(0, 1, False, 0), (4, 2, True, 8)]:
+        kw = dict(R=16, L=24, VL=30, num_split=split, num_passes=passes, dynamic_prune=dyn, max_alpha=1.2,
+                  min_alpha=1.05, top_degree=td, sp_seed=3)
+        go = oracle_lib.build_graph(dtype, metric, base[:1200], **kw)
+        gr = ref_lib.build_graph(dtype, metric, base[:1200], **kw)
+        for a, b in zip(go[:3], gr[:3]):
+            assert np.array_equal(a, b), (split, passes, dyn, td)
+        assert go[3] == gr[3]
+
 def test_oracle_build_is_independent_of_thread_count(oracle_lib):
     """The batched build is batch-synchronous, as the reference's OpenMP phases are: every
     insert of a batch searches the graph as it stood before the batch and the reverse edges
