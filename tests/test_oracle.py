@@ -87,3 +87,28 @@ def test_oracle_build_is_independent_of_thread_count(oracle_lib):
             for t in (1, 4)]
     for a, b in zip(runs[0], runs[1]):
         assert np.array_equal(a, b)
+
+
+def test_oracle_matches_reference_harness_on_options(oracle_lib, ref_lib):
+    """The options the defaults leave untouched: cosine-angle prune bounds, random start points,
+    a visit limit during the build; search limits, degree limits, cut values, a visited cap small
+    enough to overflow (visited_factor 2), repeated start points, and the extreme beams."""
+    base, q, g = dataset("u8", "l2")
+    for extra in [dict(max_cos=0.5, min_cos=0.2, dynamic_prune=True, num_split=4, num_passes=2),
+                  dict(max_cos=0.3, min_cos=0.3, num_split=0, num_passes=1),
+                  dict(rand_sp=True, num_split=4, num_passes=2, dynamic_prune=True),
+                  dict(limit=300, num_split=0, num_passes=1),
+                  dict(limit=500, num_split=4, num_passes=2)]:
+        kw = dict(R=16, L=24, VL=30, max_alpha=1.2, min_alpha=1.05, sp_seed=5, **extra)
+        go = oracle_lib.build_graph("u8", "l2", base[:1500], **kw)
+        gr = ref_lib.build_graph("u8", "l2", base[:1500], **kw)
+        for a, b in zip(go[:3], gr[:3]):
+            assert np.array_equal(a, b), extra
+        assert go[3] == gr[3]
+    for kw in [dict(L=40, k=10, limit=200), dict(L=40, k=10, degree_limit=8), dict(L=64, k=20, cut=1.1),
+               dict(L=64, k=20, cut=2.0, visited_factor=2), dict(L=50, k=10, start_points=(0, 17, 900, 17)),
+               dict(L=200, k=100), dict(L=1, k=1)]:
+        o = oracle_lib.search("u8", "l2", base, g, q, **kw)
+        r = ref_lib.search("u8", "l2", base, g, q, **kw)
+        for x, y in zip(o, r):
+            assert np.array_equal(x, y), kw
