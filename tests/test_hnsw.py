@@ -101,3 +101,17 @@ def test_hnsw_sizes_entry_equals_the_driver_defaults(oracle_lib):
                     want = oracle_lib.hnsw_sizes(n, R, m_l, max_node)
                     assert (ml.value, mn.value) == want, (n, R, m_l, max_node)
     assert L.nbpg_hnsw_sizes(1000, 1, 0.0, 0, C.byref(ml), C.byref(mn)) == 1  # ln(1) = 0: no default m_l
+
+
+@pytest.mark.parametrize("dtype,metric,dims", [("i8", "l2", 24), ("u4", "l2", 16), ("u8", "ip", 32), ("i4", "ip", 16)])
+def test_oracle_hnsw_build_matches_harness_every_row_type(oracle_lib, ref_lib, dtype, metric, dims):
+    """The HNSW build through the harness over the reference's headers, on the other row types
+    and on inner product: graph, id mapping, entry node, per-node counters and isolated count,
+    with the default hierarchy and with three entry points and a larger m_l."""
+    from conftest import dataset
+    base, _, _ = dataset(dtype, metric, dims=dims)
+    for kw in (dict(R=16, L=24, VL=60), dict(R=16, L=20, VL=60, hier_beam=3, m_l=0.6)):
+        o = oracle_lib.build_hnsw(dtype, metric, base[:2000], **kw)
+        r = ref_lib.build_hnsw(dtype, metric, base[:2000], **kw)
+        for a, b in zip(o, r):
+            assert (np.array_equal(a, b) if isinstance(a, np.ndarray) else a == b), kw
