@@ -111,3 +111,34 @@ def test_gpu_reproduces_reference_search(gpu_lib, path):
         r = idx.search(d["queries"], QueryParams(k=k, beamSize=L, cut=1.35), kernel=kernel)
         for a, key in zip([r.ids, r.dists, r.count, r.visited, r.cmps], ["ids", "dists", "count", "visited", "cmps"]):
             assert np.array_equal(a, d[key]), (kernel, key)
+
+
+@pytest.mark.parametrize("dtype,metric,dims", [("i8", "l2", 24), ("u4", "l2", 16), ("u8", "ip", 32), ("i4", "ip", 16)])
+def test_oracle_reproduces_vamana_binary_every_row_type(oracle_lib, tmp_path, dtype, metric, dims):
+    """The reference Vamana binary, run here where it was built from its sources, on .i8bin, .u4bin
+    and .i4bin rows and with --use_mips, with the settings whose output does not depend on
+    std::random_device (no split stage; one split with the popularity and dynamic-prune passes):
+    its .graph equals the oracle's build byte for byte."""
+    import subprocess
+    from oracle.oracle import REF_VAMANA
+    from nbpg_gb300 import formats
+    from conftest import dataset
+    if not os.path.exists(REF_VAMANA):
+        pytest.skip("the reference Vamana binary is not built on this machine")
+    base, _, _ = dataset(dtype, metric, dims=dims)
+    base = base[:1500]
+    path = str(tmp_path / f"b.{dtype}bin")
+    formats.write_vectors(path, base)
+    for flags in (["--num_split", "0", "--num_passes", "1", "--max_alpha", "1.2"],
+                  ["--num_split", "1", "--num_passes", "2", "--dynamic_prune", "--min_alpha", "1.05", "--max_alpha",
+                   "1.2"]):
+        ip = str(tmp_path / "idx")
+        cmd = [REF_VAMANA, "--quant_base_path", path, "--index_path", ip, "--R", "16", "--L", "24", "--VL", "32",
+               "--rebuild", *flags] + (["--use_mips"] if metric == "ip" else [])
+        subprocess.run(cmd, check=True, capture_output=True, timeout=300)
+        f = flags
+        kw = dict(R=16, L=24, VL=32, num_split=int(f[f.index("--num_split") + 1]),
+                  num_passes=int(f[f.index("--num_passes") + 1]), dynamic_prune="--dynamic_prune" in f,
+                  max_alpha=1.2, min_alpha=1.05 if "--min_alpha" in f else 1.0)
+        g, _, _, _ = oracle_lib.build_graph(dtype, metric, base, **kw)
+        assert _graph_bytes(g) == open(ip + ".graph", "rb").read(), flags
