@@ -43,3 +43,30 @@ def test_oracle_rerank_matches_harness(oracle_lib):
                 b = ref.search_rerank(dtype, metric, qb, rawb, g, qq, rawq, L, k, rf)
                 for x, y in zip(a, b):
                     assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (dtype, metric, rawb.dtype, L, k, rf)
+
+
+def test_oracle_rerank_matches_harness_raw_i8_and_other_metrics(oracle_lib):
+    """The same pin with raw i8 rows beside float ones, and the quantised types on the other
+    metric (u4 and u8 inner product, i8 L2), in both modes (rerank factors 100 and 2, filtering)."""
+    from oracle.oracle import reference
+    from nbpg_gb300 import synth
+    ref = reference()
+    if ref is None or not hasattr(ref.lib, "nbpg_ref_search_rerank"):
+        pytest.skip("reference sources not present")
+    r = np.random.default_rng(4)
+    raw = r.normal(size=(2000, 24)).astype(np.float32)
+    rq = r.normal(size=(50, 24)).astype(np.float32)
+    cb = np.clip(np.round((raw + 3) * 40), 0, 255).astype(np.uint8)
+    cq = np.clip(np.round((rq + 3) * 40), 0, 255).astype(np.uint8)
+    rb8 = np.clip(np.round(raw * 40), -127, 127).astype(np.int8)
+    rq8 = np.clip(np.round(rq * 40), -127, 127).astype(np.int8)
+    for dtype, metric, qb, qq in [("u4", "ip", synth.pack_u4(cb >> 4), synth.pack_u4(cq >> 4)), ("u8", "ip", cb, cq),
+                                  ("i8", "l2", (cb.astype(np.int16) - 128).astype(np.int8),
+                                   (cq.astype(np.int16) - 128).astype(np.int8))]:
+        g, _, _, _ = oracle_lib.build_graph(dtype, metric, qb, R=20, L=32, VL=48, num_split=0, num_passes=1)
+        for rawb, rawq in [(rb8, rq8), (raw, rq)]:
+            for L, k, rf in [(24, 10, 100), (24, 10, 2), (30, 8, 0)]:
+                a = oracle_lib.search_rerank(dtype, metric, qb, rawb, g, qq, rawq, L, k, rf)
+                b = ref.search_rerank(dtype, metric, qb, rawb, g, qq, rawq, L, k, rf)
+                for x, y in zip(a, b):
+                    assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (dtype, metric, rawb.dtype, L, k, rf)
