@@ -39,3 +39,26 @@ def test_compgt_file_round_trip(tmp_path, oracle_lib):
     assert np.array_equal(ids, oi) and np.array_equal(ds, od)
     formats.write_gt(str(tmp_path / "w.gt"), ids, ds)
     assert open(gp, "rb").read() == open(str(tmp_path / "w.gt"), "rb").read()
+
+
+def test_compgt_binary_other_k_and_edge_sizes(tmp_path, oracle_lib):
+    """CompGT's replacement rule at k = 1, 7, 250, with n = k and n = k + 1, on u8 and i8 rows,
+    L2 and --use_mips: the reference binary's .gt equals the oracle's kNN."""
+    from oracle.oracle import REF_COMPGT
+    if not os.path.exists(REF_COMPGT):
+        pytest.skip("the reference CompGT binary is not built on this machine")
+    from nbpg_gb300 import synth
+    b, q = synth.u8_mixture(2000, 30, dim=24, n_centres=10, seed=5)
+    i8b, i8q = (b.astype(np.int16) - 128).astype(np.int8), (q.astype(np.int16) - 128).astype(np.int8)
+    for base, qq, k in [(b, q, 1), (b, q, 7), (b, q, 250), (b[:50], q, 50), (b[:50], q, 49), (i8b, i8q, 13)]:
+        dt = "i8" if base.dtype == np.int8 else "u8"
+        bp, qp, gp = (str(tmp_path / n) for n in (f"b.{dt}bin", f"q.{dt}bin", "r.gt"))
+        formats.write_vectors(bp, base)
+        formats.write_vectors(qp, qq)
+        for mips in (False, True):
+            subprocess.run([REF_COMPGT, "--base_path", bp, "--query_path", qp, "--gt_path", gp, "--k", str(k)] +
+                           (["--use_mips"] if mips else []), check=True, capture_output=True, timeout=300,
+                           env={**os.environ, "OMP_NUM_THREADS": "4"})
+            ids, ds = formats.read_gt(gp)
+            oi, od = oracle_lib.gt(dt, "ip" if mips else "l2", base, qq, k=k)
+            assert np.array_equal(ids, oi) and np.array_equal(ds.view(np.uint32), od.view(np.uint32)), (dt, k, mips)
