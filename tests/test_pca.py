@@ -76,3 +76,32 @@ def test_fitter_projects_onto_scaled_principal_axes():
     assert np.allclose(y.std(axis=0), 1 / 3.0, rtol=0.05)          # +-3 sigma -> +-1
     assert np.argmax(np.abs(mat[0])) == 0 and np.argmax(np.abs(mat[1])) == 1  # largest variances first
     np.testing.assert_allclose(fit(x, 4)[0], mat)                   # reproducible signs
+
+
+def test_oracle_pca_matches_reference_binary_more_shapes(oracle_lib, tmp_path):
+    """The reference PCACompress binary, run here where it was built from its sources, on other
+    projections (128 -> 64 as in the 4-bit workload, 24 -> 10, 64 -> 32, and 20 -> 7 for the
+    byte and float outputs): every output file equals the oracle's rows behind the same header."""
+    import subprocess
+    import pytest
+    from oracle.oracle import REF_COMPGT
+    from nbpg_gb300 import formats
+    ref_exe = os.path.join(os.path.dirname(REF_COMPGT), "PCACompress")
+    if not os.path.exists(ref_exe):
+        pytest.skip("the reference PCACompress binary is not built on this machine")
+    r = np.random.default_rng(21)
+    for d_in, d_out, scale in [(128, 64, 0.1), (24, 10, 0.4), (20, 7, 0.4), (64, 32, 1.0)]:
+        x = (r.normal(size=(700, d_in)) * 0.6).astype(np.float32)
+        mat = (r.normal(size=(d_out, d_in)) * scale).astype(np.float32)
+        bias = (r.normal(size=d_out) * 0.1).astype(np.float32)
+        formats.write_vectors(str(tmp_path / "x.fbin"), x)
+        formats.write_matrix(str(tmp_path / "m.mat"), mat, bias)
+        for kind, ext in [("u4", ".u4bin"), ("i4", ".i4bin"), ("u8", ".u8bin"), ("i8", ".i8bin"), ("f32", ".fbin")]:
+            if kind in ("u4", "i4") and d_out % 2:
+                continue
+            out = str(tmp_path / f"o{ext}")
+            subprocess.run([ref_exe, "--ifile", str(tmp_path / "x.fbin"), "--ofile", out, "--matFile",
+                            str(tmp_path / "m.mat")], check=True, capture_output=True, timeout=300)
+            got = oracle_lib.pca_encode(x, mat, bias, kind)
+            header = np.array([700, got.shape[1]], np.uint32).tobytes()
+            assert open(out, "rb").read() == header + got.tobytes(), (d_in, d_out, kind)
