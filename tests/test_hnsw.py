@@ -115,3 +115,18 @@ def test_oracle_hnsw_build_matches_harness_every_row_type(oracle_lib, ref_lib, d
         r = ref_lib.build_hnsw(dtype, metric, base[:2000], **kw)
         for a, b in zip(o, r):
             assert (np.array_equal(a, b) if isinstance(a, np.ndarray) else a == b), kw
+
+
+@pytest.mark.parametrize("dtype,metric,dims", [("i8", "l2", 24), ("u4", "l2", 16), ("u8", "ip", 32), ("i4", "ip", 16)])
+def test_oracle_hnsw_search_matches_harness_every_row_type(oracle_lib, ref_lib, dtype, metric, dims):
+    """hier_qsearchAll through the harness on the other row types and on inner product, with one
+    and with three entry points per level: ids, counts, expansions and distance counts."""
+    from conftest import dataset
+    base, q, _ = dataset(dtype, metric, dims=dims)
+    for bkw, L, k in [(dict(R=16, L=24, VL=60), 24, 10), (dict(R=16, L=20, VL=60, hier_beam=3, m_l=0.6), 40, 20)]:
+        g, pre, sp, _, _, _ = oracle_lib.build_hnsw(dtype, metric, base[:2000], **bkw)
+        hb = bkw.get("hier_beam", 1)
+        a = oracle_lib.search_hnsw(dtype, metric, base[:2000], g, pre, sp, q, L=L, k=k, hier_beam=hb)
+        b = ref_lib.search_hnsw(dtype, metric, base[:2000], g, pre, sp, q, L=L, k=k, hier_beam=hb)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), (hb, L, k)
