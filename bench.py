@@ -330,6 +330,16 @@ def time_hnsw(base, q, gi, k, local, n_prefix=100_000):
     return out
 
 
+def parity_hashes(g, gi, gd):
+    """SHA-256 of the 1M-row index's .graph file bytes and of its CompGT-mode .gt file bytes: the GPU
+    arm and the CPU arm build and compute these independently, so equal hashes in the two JSON
+    lines show the two paths agree at full size."""
+    import hashlib
+    from nbpg_gb300 import formats
+    return {"graph_sha256": hashlib.sha256(formats.graph_bytes(g)).hexdigest(),
+            "gt_sha256": hashlib.sha256(formats.gt_bytes(gi, gd)).hexdigest()}
+
+
 def recall_of(ids, gi, k):
     return float(np.mean([len(set(a[:k].tolist()) & set(b[:k].tolist())) / k for a, b in zip(ids, gi)]))
 
@@ -418,6 +428,8 @@ def run_reference(args):
     t = time.time()
     gi, gd = O.gt("u8", "l2", base, q, k=CFG["gt_k"], exact=False, threads=threads)
     log(f"[bench/ref] CPU ground truth for {len(q)} queries {time.time() - t:.1f}s")
+    hashes = parity_hashes(g, gi, gd)
+    log(f"[bench/ref] parity hashes {hashes}")
     L_op = None
     for L in L_SWEEP:
         ids = O.search("u8", "l2", base, g, q, L=L, k=CFG["k"], cut=CFG["cut"], threads=threads)[0]
@@ -443,7 +455,8 @@ def run_reference(args):
                        "index_built_on": "host CPU (restatement of build_vamana)", "n_base": CFG["n"]},
             "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                              "sample": f"{len(sample)} queries per step at L={L_op}, {args.steps} steps"},
-            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "parity": hashes}
     print(json.dumps(line), flush=True)
 
 
@@ -563,6 +576,8 @@ def main():
     gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
     gt_s = time.time() - t
     log(f"[bench] GPU ground truth (CompGT mode) {gt_s:.2f}s")
+    hashes = parity_hashes(g, gi, gd)
+    log(f"[bench] parity hashes {hashes}")
     gei, ged = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=True, device=local)
     try:
         gt_dev = time_gt_device(base, q, CFG["gt_k"], local)
@@ -807,7 +822,7 @@ def main():
                                                      "p50": serving["at_half_peak"]["p50_ms"],
                                                      "p99": serving["at_half_peak"]["p99_ms"],
                                                      "at_offered_qps": serving["at_half_peak"]["offered_qps"]},
-            "serving": serving, "ground_truth": gt_dev, "next_rows": next_rows}
+            "serving": serving, "ground_truth": gt_dev, "next_rows": next_rows, "parity": hashes}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -42,8 +42,17 @@ typedef enum nbpg_dtype { NBPG_U8 = 0, NBPG_I8 = 1, NBPG_U4 = 2, NBPG_I4 = 3, NB
 /* DistanceMetric::EUCLIDEAN (squared L2) / MIPS (negative dot), point.h:20-24. */
 typedef enum nbpg_metric { NBPG_L2 = 0, NBPG_IP = 1 } nbpg_metric;
 
-/* Search kernels.  STRICT reproduces the reference's expansion order, visited
- * filter and merge rules bit for bit. */
+/* Search modes.  STRICT reproduces the reference's expansion order, visited filter and
+ * merge rules bit for bit (filtered_beam_search, beamSearch.h:43-171).  FAST is this
+ * library's own variant of the same greedy search for serving: an exact open-addressing
+ * visited hash of a chosen size in place of the reference's lossy table
+ * (query_params.h:223-247), and `expand` frontier entries expanded per step with a merge
+ * after every step in place of the one-at-a-time expansion and deferred merge
+ * (beamSearch.h:119-125).  FAST results are valid (dist, id)-ordered neighbour lists,
+ * not the reference's. */
+typedef enum nbpg_search_mode { NBPG_MODE_STRICT = 0, NBPG_MODE_FAST = 1 } nbpg_search_mode;
+
+/* Search kernels.  In STRICT mode every kernel returns identical results. */
 typedef enum nbpg_kernel {
     NBPG_KERNEL_BATCHED = 0, /* persistent CTAs pulling queries from a device queue */
     NBPG_KERNEL_PLAIN = 1    /* one query per thread block */
@@ -102,7 +111,12 @@ typedef struct nbpg_search_params {
     uint32_t lane_width;     /* 16-byte words each lane loads per vector row: 1, 2 or 4
                                 (lanes per row = row words / lane_width); 0 = default */
     int32_t prefetch;        /* adjacency rows of upcoming frontier entries prefetched to L2
-                                per expansion (batched kernel); -1 = default */
+                                per expansion (batched kernel, STRICT); -1 = default */
+    uint32_t mode;           /* nbpg_search_mode; 0 = STRICT */
+    uint32_t expand;         /* FAST: frontier entries expanded per step, expand * R <= 256;
+                                0 = 2 (1 when R > 128) */
+    uint32_t hash_slots;     /* FAST: slots of the visited hash, a power of two in [256, 65536];
+                                0 = the smallest power of two >= max(2048, 64 * L), at most 16384 */
 } nbpg_search_params;
 
 /* Per-query outputs, k_stride entries per query row: ids (UINT32_MAX padding),
@@ -110,7 +124,8 @@ typedef struct nbpg_search_params {
  * computations (QueryStatic, query_params.h:47-94).  Any output pointer except
  * out_ids may be NULL.  Ls/ks give per-query beam width and k (NULL = params).
  * start_points: entry nodes (the reference's get_sp; {0} in check_nn_recall.h:282-297),
- * distinct, at most min L.
+ * at most min(L, 256); repeated entries are allowed, as the reference allows them (the
+ * frontier then holds copies of a key, query_params.h:204-221).
  *
  * nbpg_search: host buffers; copies in and out on the index stream and returns when done.
  * nbpg_search_device: device buffers (start_points stays a host array); enqueued on
@@ -134,12 +149,17 @@ nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_queries, uint32
                                   uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps,
                                   void *stream);
 
-/* Autotuner for the search launch: times CTA size x lane width x prefetch for the
- * batched kernel, and the plain kernel, on the caller's device-resident queries with
- * the caller's (L, k), and writes the fastest configuration into *tuned (a copy of
- * *params with kernel, warps_per_cta, lane_width and prefetch filled in).  Results of
- * every configuration are identical; only speed differs.  best_ms (may be NULL)
- * receives the best time per launch.  Project-written; no vendor tuner involved. */
+/* Autotuner for the search launch, on the caller's device-resident queries with the
+ * caller's (L, k); writes the fastest configuration into *tuned (a copy of *params with
+ * the tuned fields filled in) and its time per launch into best_ms (may be NULL).
+ * STRICT: times CTA size x lane width x prefetch for the batched kernel, and the plain
+ * kernel; results of every configuration are identical, only speed differs.
+ * FAST: also times expand (1, 2, 4) x hash_slots (a quarter, half and all of the default)
+ * for each launch shape.  Those change which nodes a query expands, so a configuration
+ * is eligible only when its mean distance over the returned top-k lists is no worse than
+ * that of the most thorough configuration (expand 1, the largest hash) by more than a
+ * relative 1e-3 (for inner product, on the magnitude of the negative mean).  Project-written;
+ * no vendor tuner involved. */
 nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queries, uint32_t nq,
                                  const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
                                  nbpg_search_params *tuned, float *best_ms);

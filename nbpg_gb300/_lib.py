@@ -17,6 +17,7 @@ STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "FORM
 DTYPES = {"u8": 0, "i8": 1, "u4": 2, "i4": 3, "f32": 4}
 METRICS = {"l2": 0, "ip": 1}
 KERNELS = {"batched": 0, "plain": 1}
+MODES = {"strict": 0, "fast": 1}
 
 
 class NbpgError(RuntimeError):
@@ -33,7 +34,8 @@ class IndexDesc(C.Structure):
 class SearchParams(C.Structure):
     _fields_ = [("k", C.c_uint32), ("L", C.c_uint32), ("cut", C.c_double), ("limit", C.c_uint64),
                 ("degree_limit", C.c_uint32), ("visited_factor", C.c_uint32), ("kernel", C.c_uint32),
-                ("warps_per_cta", C.c_uint32), ("lane_width", C.c_uint32), ("prefetch", C.c_int32)]
+                ("warps_per_cta", C.c_uint32), ("lane_width", C.c_uint32), ("prefetch", C.c_int32),
+                ("mode", C.c_uint32), ("expand", C.c_uint32), ("hash_slots", C.c_uint32)]
 
 
 class BuildParams(C.Structure):

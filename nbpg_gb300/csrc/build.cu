@@ -148,10 +148,6 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     NBPG_CHECK_ARG(n >= 1 && n < 0xFFFFFFFFull, "bad n");
     NBPG_CHECK_ARG(!fgim || P.num_split >= 1, "the FGIM build needs num_split >= 1 (with none, the reference's "
                                               "pair pass reads a stale visited list)");
-    if (P.dir_bias_scale > 0) {
-        set_error("dir_bias_scale > 0 is not supported by the GPU build");
-        return NBPG_ERR_UNSUPPORTED;
-    }
     uint32_t vecs, lpr, vpl;
     row_geometry(idx->row_stride, 0, vecs, lpr, vpl);
     NBPG_CHECK_ARG(vecs <= 128, "rows above 2048 bytes are not supported");
@@ -202,9 +198,9 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     const uint32_t nsp_max = std::max<uint32_t>(1, P.num_split);
 
     DevBuf d_inserts, d_sp, d_alpha, d_cos, d_pop, d_sv, d_sd, d_res_ids, d_res_d, d_res_cnt, d_rank, d_cnt, d_off,
-        d_bump, d_grp, d_edges, d_queue;
+        d_bump, d_grp, d_edges, d_queue, d_bias;
     ReleaseOnExit release_bufs{{&d_inserts, &d_sp, &d_alpha, &d_cos, &d_pop, &d_sv, &d_sd, &d_res_ids, &d_res_d,
-                                &d_res_cnt, &d_rank, &d_cnt, &d_off, &d_bump, &d_grp, &d_edges, &d_queue}};
+                                &d_res_cnt, &d_rank, &d_cnt, &d_off, &d_bump, &d_grp, &d_edges, &d_queue, &d_bias}};
     auto fail_oom = [&](nbpg_status x) { return x; };
     if ((s = d_inserts.ensure(n * 4)) || (s = d_sp.ensure(n * nsp_max * 4)) || (s = d_alpha.ensure(n * 4)) ||
         (s = d_cos.ensure(n * 4)) || (s = d_pop.ensure(n * 4)) || (s = d_sv.ensure(n * 4)) ||
@@ -234,6 +230,18 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     B.bump = d_bump.as<uint32_t>();
     B.grp_target = d_grp.as<uint32_t>();
     B.edges = d_edges.as<uint64_t>();
+    B.dir_bias = nullptr;
+    std::vector<double> bias_host;
+    if (P.dir_bias_scale > 0) {
+        // sort_candidates' factor dir_bias_scale * log(degree + 1) + 1 in double, the float scale
+        // widened as the reference's expression widens it (prune.h:59-63); a degree is at most R
+        bias_host.resize(R + 1);
+        for (uint32_t d = 0; d <= R; ++d) bias_host[d] = P.dir_bias_scale * std::log(double(d + 1)) + 1;
+        if ((s = d_bias.ensure(size_t(R + 1) * sizeof(double))) != NBPG_OK) return s;
+        NBPG_CUDA_TRY(cudaMemcpyAsync(d_bias.ptr, bias_host.data(), size_t(R + 1) * sizeof(double),
+                                      cudaMemcpyHostToDevice, st));
+        B.dir_bias = d_bias.as<double>();
+    }
 
     const float min_alpha = float(P.min_alpha), max_alpha = float(P.max_alpha);
     const float min_cos = float(P.min_cos_angle), max_cos = float(P.max_cos_angle);
@@ -429,7 +437,7 @@ static nbpg_status build_impl(nbpg_index *idx, const nbpg_build_params &P, nbpg_
     if (out_sd) NBPG_CUDA_TRY(cudaMemcpyAsync(out_sd, d_sd.ptr, n * 4, cudaMemcpyDeviceToHost, st));
     NBPG_CUDA_TRY(cudaStreamSynchronize(st));
     for (DevBuf *b : {&d_inserts, &d_sp, &d_alpha, &d_cos, &d_pop, &d_sv, &d_sd, &d_res_ids, &d_res_d, &d_res_cnt,
-                      &d_rank, &d_cnt, &d_off, &d_bump, &d_grp, &d_edges, &d_queue})
+                      &d_rank, &d_cnt, &d_off, &d_bump, &d_grp, &d_edges, &d_queue, &d_bias})
         b->release();
     if (stats) {
         stats->isolated = iso;

@@ -44,6 +44,8 @@ struct BuildArgs {
     uint32_t *grp_target;  // groups
     uint64_t *edges;       // grouped (dist, source) keys
     uint32_t pair;         // FGIM pair pass (FGIM_nsw.h:45-109) instead of searchNghAndPrune
+    const double *dir_bias;  // sort_candidates' degree bias: factor per degree d in [0, R],
+                             // dir_bias_scale * log(d + 1) + 1 (prune.h:59-63); null = none
 };
 
 constexpr double kPruneEps = 1e-5;  // kEpsilon, prune.h:212
@@ -73,7 +75,7 @@ __device__ __forceinline__ void load_row_regs(const SearchArgs &a, uint32_t id, 
 template <int DT, int MET, int VPL>
 __device__ void prune_and_emit(const BuildArgs &B, uint32_t t, uint32_t index, uint64_t *pool, uint32_t np,
                                uint8_t *alive, uint32_t search_cmps, uint32_t nvis, const uint64_t *vis, uint32_t vs,
-                               int lane);
+                               uint64_t *scratch, int lane);
 
 template <int DT, int MET, int VPL>
 __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t gslot, int lane)
@@ -143,7 +145,9 @@ __device__ void build_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_
     np = __shfl_sync(kFull, np, 0);
     __syncwarp();
 
-    prune_and_emit<DT, MET, VPL>(B, t, index, pool, np, alive, st.cmps + rp, uint32_t(st.nvis), st.vis, st.vs, lane);
+    // tmp (fr0) is free once merged: it is the scratch of a biased sort_candidates
+    prune_and_emit<DT, MET, VPL>(B, t, index, pool, np, alive, st.cmps + rp, uint32_t(st.nvis), st.vis, st.vs, tmp,
+                                 lane);
 }
 
 // FGIM pair pass for one insert (FIGM_NSWIndex::pair_batch_insert's searchNghAndPrune,
@@ -199,13 +203,19 @@ __device__ void fgim_one(const BuildArgs &B, uint32_t t, uint8_t *slot, uint32_t
     }
     np = __shfl_sync(kFull, np, 0);
     __syncwarp();
+    // the neighbour keys (nk) are merged into the pool: nk is the scratch of a biased sort_candidates
     prune_and_emit<DT, MET, VPL>(B, t, index, pool, np, alive, ns * st.cmps, ns * uint32_t(st.nvis), st.vis,
-                                 ns ? st.vs : 0u, lane);
+                                 ns ? st.vs : 0u, nk, lane);
 }
 
 // sort_candidates (prune.h:50-74) on pool[0, np): p forced last, sort, drop repeats, drop p.
-// Returns the new count.
-__device__ __forceinline__ uint32_t sort_candidates_dev(uint64_t *pool, uint32_t np, uint32_t index, int lane)
+// With a degree bias (dir_bias_scale > 0, prune.h:59-63) the order is by the biased distance
+// float(dist * bias[degree]) of each candidate (degree in the graph being searched, which no
+// launch of the batch has written yet), then id; the stored distances stay unbiased.  scratch
+// holds np keys (used only with a bias).  Returns the new count.
+__device__ __forceinline__ uint32_t sort_candidates_dev(uint64_t *pool, uint32_t np, uint32_t index,
+                                                        const double *bias, const uint32_t *graph, uint32_t gstride,
+                                                        uint64_t *scratch, int lane)
 {
     const uint64_t pkey = (uint64_t(f2ord(3.402823466e38f)) << 32) | index;
     for (uint32_t i = lane; i < np; i += 32)
@@ -225,6 +235,29 @@ __device__ __forceinline__ uint32_t sort_candidates_dev(uint64_t *pool, uint32_t
         __syncwarp();
         if (keep) pool[outc + __popc(m & lanemask_lt())] = v;
         outc += __popc(m);
+        __syncwarp();
+    }
+    if (bias) {
+        // Ids are distinct now.  scratch = (id, unbiased distance image) sorted by id, for the
+        // lookup after the pool is re-sorted by (biased distance, id).  p keeps FLT_MAX, which
+        // the reference assigns after the bias.
+        for (uint32_t i = lane; i < outc; i += 32) {
+            const uint64_t k = pool[i];
+            const uint32_t id = key_id(k);
+            scratch[i] = (uint64_t(id) << 32) | uint32_t(k >> 32);
+            if (id != index) {
+                const double f = bias[__ldg(graph + size_t(id) * gstride)];
+                pool[i] = make_key(__double2float_rn(double(key_dist(k)) * f), id);
+            }
+        }
+        __syncwarp();
+        sort_keys(scratch, outc, lane);
+        sort_keys(pool, outc, lane);
+        for (uint32_t i = lane; i < outc; i += 32) {
+            const uint32_t id = key_id(pool[i]);
+            const uint32_t pos = lower_count(scratch, outc, uint64_t(id) << 32);
+            pool[i] = (uint64_t(uint32_t(scratch[pos])) << 32) | id;
+        }
         __syncwarp();
     }
     if (outc > 0 && key_id(pool[outc - 1]) == index) --outc;
@@ -366,11 +399,11 @@ __device__ uint32_t max_angle_prune_dev(const SearchArgs &a, uint64_t *pool, uin
 template <int DT, int MET, int VPL>
 __device__ void prune_and_emit(const BuildArgs &B, uint32_t t, uint32_t index, uint64_t *pool, uint32_t np,
                                uint8_t *alive, uint32_t search_cmps, uint32_t nvis, const uint64_t *vis, uint32_t vs,
-                               int lane)
+                               uint64_t *scratch, int lane)
 {
     const uint32_t R = B.R;
     uint32_t rp = 0;
-    np = sort_candidates_dev(pool, np, index, lane);
+    np = sort_candidates_dev(pool, np, index, B.dir_bias, B.s.graph, B.s.gstride, scratch, lane);
     const double alpha = double(B.alpha_node ? B.alpha_node[index] : B.alpha_all);
     const double cosa = double(B.cos_node ? B.cos_node[index] : B.cos_all);
     const uint32_t sel = limited_prune_dev<DT, MET, VPL>(B.s, pool, np, alive, index, R, alpha, cosa, rp, lane);

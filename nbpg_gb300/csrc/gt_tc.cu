@@ -6,8 +6,9 @@
 // integer below 2^24 for the dimensions routed here (<= 128 elements), so the fp32
 // accumulator of a bf16 MMA holds the exact integer dot product.  Distances are then
 // formed in int32 as in the reference (point.h:35-135): L2 = |q|^2 + |b|^2 - 2 q.b,
-// IP = -q.b, 4-bit types scaled by 256.  INT8 MMA is not used: on GB300 its rate is a
-// small fraction of the bf16 rate.
+// IP = -q.b, 4-bit types scaled by 256.  Integer MMA is not available: ptxas refuses
+// tcgen05.mma .kind::i8 for sm_103a ("Feature '.kind::i8' not supported on .target 'sm_103a'"),
+// so the bf16 form is the exact tensor path on this part.
 //
 // One CTA owns 128 queries (the MMA's M = the 128 TMEM lanes) and walks the base in
 // id order in tiles of 128 rows (N).  Warp 4 loads tiles with TMA (128-byte swizzle)

@@ -1,6 +1,7 @@
 // Host driver of the strict search: argument checks, shared-memory layout,
 // scratch, and the FLAG pass followed by the LIST re-run of tainted queries.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -168,6 +169,103 @@ static nbpg_status plan_pass_uncached(nbpg_index *idx, const SearchOps *ops, int
     return NBPG_OK;
 }
 
+// FAST mode: the default hash size for beam L and the default expansions per step.
+uint32_t fast_default_slots(uint32_t L)
+{
+    uint32_t s = 2048;
+    while (s < 64u * L && s < 16384u) s <<= 1;
+    return s;
+}
+
+uint32_t fast_default_expand(uint32_t R) { return R > 128 ? 1u : 2u; }
+
+// Per-warp slot of the FAST kernels (search_fast.cuh): two frontier buffers and their flags,
+// candidates and filtered ids (Ccap each), unexpanded positions, the visited hash (S slots).
+SlotLayout make_fast_layout(uint32_t Lmax, uint32_t Ccap, uint32_t S)
+{
+    SlotLayout l{};
+    l.Lcap = round_up(std::max<uint32_t>(Lmax, 1), 32);
+    l.Ccap = round_up(std::max<uint32_t>(Ccap, 1), 32);
+    l.Rcap = l.Ccap;
+    l.Scap = S;
+    uint32_t off = 0;
+    l.off_fr0 = off; off += l.Lcap * 8;
+    l.off_fr1 = off; off += l.Lcap * 8;
+    l.off_cand = off; off += l.Ccap * 8;
+    l.off_vis = off;
+    l.off_hash = off; off += S * 4;
+    l.off_filt = off; off += l.Ccap * 4;
+    l.off_unv = off; off += l.Lcap * 2;
+    l.off_fl0 = off; off += l.Lcap;
+    l.off_fl1 = off; off += l.Lcap;
+    l.bytes = round_up(off, 16);
+    return l;
+}
+
+using FastKey = std::tuple<int, const SearchOps *, int, bool, uint32_t, uint32_t, uint32_t, uint32_t, size_t, int>;
+static std::map<FastKey, PassCfg> g_fast_plans;
+static std::map<std::tuple<int, const SearchOps *, int, bool>, size_t> g_fast_attr;
+
+static nbpg_status plan_fast(nbpg_index *idx, const SearchOps *ops, int metric, bool plain, uint32_t Lmax,
+                             uint32_t Ccap, uint32_t S, uint32_t want_warps, PassCfg &pc)
+{
+    const int dev = idx->desc.device;
+    const FastKey key{dev, ops, metric, plain, Lmax, Ccap, S, want_warps, idx->smem_optin, idx->sm_count};
+    std::lock_guard<std::mutex> g(g_plan_mu);
+    auto it = g_fast_plans.find(key);
+    if (it != g_fast_plans.end()) {
+        pc = it->second;
+        return NBPG_OK;
+    }
+    auto raise = [&](size_t smem) -> cudaError_t {
+        size_t &cur = g_fast_attr[std::make_tuple(dev, ops, metric, plain)];
+        if (smem <= cur) return cudaSuccess;
+        const cudaError_t e = ops->set_attr_fast(metric, plain, smem);
+        if (e == cudaSuccess) cur = smem;
+        return e;
+    };
+    pc = PassCfg{};
+    pc.S = S;
+    pc.lay = make_fast_layout(Lmax, Ccap, S);
+    if (pc.lay.bytes > idx->smem_optin) {
+        set_error("per-query working set of the FAST search exceeds shared memory (lower hash_slots or L)");
+        return NBPG_ERR_UNSUPPORTED;
+    }
+    if (plain) {
+        pc.warps = 1;
+        pc.smem = pc.lay.bytes;
+        NBPG_CUDA_TRY(raise(pc.smem));
+    } else {
+        const uint32_t fit = uint32_t(idx->smem_optin / pc.lay.bytes);
+        uint32_t w = want_warps;
+        if (!w) {
+            int best = -1;
+            for (uint32_t c : {16u, 8u, 4u, 2u}) {
+                if (c > fit) continue;
+                const size_t sm = size_t(c) * pc.lay.bytes;
+                int b = 0;
+                NBPG_CUDA_TRY(raise(sm));
+                NBPG_CUDA_TRY(ops->occ_fast(metric, false, int(c) * 32, sm, &b));
+                if (int(c) * b > best) { best = int(c) * b; w = c; }
+            }
+            if (!w) w = 1;
+        }
+        w = std::max<uint32_t>(1, std::min<uint32_t>(w, std::min<uint32_t>(16, fit)));
+        pc.warps = w;
+        pc.smem = size_t(w) * pc.lay.bytes;
+        NBPG_CUDA_TRY(raise(pc.smem));
+        int blocks = 0;
+        NBPG_CUDA_TRY(ops->occ_fast(metric, false, w * 32, pc.smem, &blocks));
+        if (blocks < 1) {
+            set_error("FAST search kernel does not fit on an SM");
+            return NBPG_ERR_UNSUPPORTED;
+        }
+        pc.grid = uint32_t(blocks) * uint32_t(idx->sm_count);
+    }
+    g_fast_plans.emplace(key, pc);
+    return NBPG_OK;
+}
+
 nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d_queries, uint32_t nq,
                                const nbpg_search_params *P, const uint32_t *d_Ls, const uint32_t *d_ks,
                                const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *d_ids, float *d_dists,
@@ -205,6 +303,69 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
 
     const int metric = int(idx->desc.metric);
     const bool plain = P->kernel == NBPG_KERNEL_PLAIN;
+    NBPG_CHECK_ARG(P->mode == NBPG_MODE_STRICT || P->mode == NBPG_MODE_FAST, "unknown search mode");
+    if (P->mode == NBPG_MODE_FAST) {
+        if (emit) {
+            set_error("re-ranking and filtering run on the strict search only");
+            return NBPG_ERR_UNSUPPORTED;
+        }
+        const uint32_t E = P->expand ? P->expand : fast_default_expand(R);
+        NBPG_CHECK_ARG(E >= 1 && E * R <= 256 && E <= 8, "FAST: expand must be in [1, 8] with expand * R <= 256");
+        const uint32_t S = P->hash_slots ? P->hash_slots : fast_default_slots(P->L);
+        NBPG_CHECK_ARG(S >= 256 && S <= 65536 && (S & (S - 1)) == 0,
+                       "FAST: hash_slots must be a power of two in [256, 65536]");
+        const uint32_t nsp_max = per_query_sp ? tgt->sp_stride : nsp;
+        PassCfg pc{};
+        nbpg_status s = plan_fast(idx, ops, metric, plain, P->L, std::max(E * R, nsp_max), S, P->warps_per_cta, pc);
+        if (s != NBPG_OK) return s;
+        if ((s = sc.queue.ensure(4 * sizeof(uint32_t))) != NBPG_OK) return s;
+        if ((s = sc.sp.ensure(256 * sizeof(uint32_t))) != NBPG_OK) return s;
+        uint32_t *q = sc.queue.as<uint32_t>();
+        NBPG_CUDA_TRY(cudaMemsetAsync(q, 0, 4 * sizeof(uint32_t), st));
+        if (!per_query_sp && (sc.sp_host.size() != nsp || !std::equal(sp, sp + nsp, sc.sp_host.begin()))) {
+            NBPG_CUDA_TRY(cudaMemcpyAsync(sc.sp.ptr, sp, nsp * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+            sc.sp_host.assign(sp, sp + nsp);
+        }
+        SearchArgs a{};
+        a.base = base;
+        a.row_stride = idx->row_stride;
+        a.vecs = vecs;
+        a.lpr = lpr;
+        a.vpl = vpl;
+        a.graph = graph;
+        a.gstride = idx->gstride;
+        a.R = R;
+        a.n = n;
+        a.queries = static_cast<const uint8_t *>(d_queries);
+        a.nq = nq;
+        a.Ls = d_Ls;
+        a.ks = d_ks;
+        a.L_all = P->L;
+        a.k_all = P->k;
+        a.cut = P->cut;
+        a.limit = P->limit ? P->limit : n;
+        a.degree_limit = P->degree_limit ? std::min(P->degree_limit, R) : R;
+        a.visited_factor = 0;
+        a.sp = per_query_sp ? tgt->d_sp : sc.sp.as<uint32_t>();
+        a.nsp = per_query_sp ? tgt->sp_stride : nsp;
+        a.sp_stride = per_query_sp ? tgt->sp_stride : 0;
+        a.k_stride = k_stride;
+        a.out_ids = d_ids;
+        a.out_dists = d_dists;
+        a.out_count = d_count;
+        a.out_visited = d_visited;
+        a.out_cmps = d_cmps;
+        a.err = q + 2;
+        a.queue = q;
+        a.order = sc.order;
+        a.expand = E;
+        a.fast_slots = S;
+        a.lay = pc.lay;
+        ops->launch_fast(metric, plain, plain ? nq : pc.grid, pc.warps, pc.smem, a, st);
+        NBPG_CUDA_TRY(cudaGetLastError());
+        return NBPG_OK;
+    }
     const uint32_t vf = P->visited_factor ? P->visited_factor : 8;
     // inner product: the cut rule routinely keeps <= k entries, so go straight to LIST;
     // filtering mode needs the visited list itself
@@ -611,8 +772,10 @@ extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_
     return NBPG_OK;
 }
 
-// Search-launch autotuner: every candidate configuration gives identical results, so
-// the fastest one on the caller's own queries wins.
+// Search-launch autotuner.  STRICT: every candidate configuration gives identical results, so
+// the fastest one on the caller's own queries wins.  FAST: expansions per step and hash size
+// join the launch shape; a candidate is eligible when the mean distance of its top-k lists is
+// within a relative 1e-3 of the most thorough configuration's (expand 1, the largest hash).
 extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queries, uint32_t nq,
                                             const nbpg_search_params *params, const uint32_t *start_points,
                                             uint32_t n_start, nbpg_search_params *tuned, float *best_ms)
@@ -620,9 +783,14 @@ extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queri
     if (!idx || !params || !tuned || !d_queries || nq == 0) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
     std::lock_guard<std::mutex> g(idx->mu);
     NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
-    const uint32_t k = params->k;
-    uint32_t *d_ids = nullptr;
-    NBPG_CUDA_TRY(cudaMalloc(&d_ids, size_t(nq) * std::max<uint32_t>(k, 1) * 4));
+    const uint32_t k = std::max<uint32_t>(params->k, 1);
+    const bool fast = params->mode == NBPG_MODE_FAST;
+    const uint32_t R = idx->desc.max_degree;
+    DevBuf d_ids, d_dists;
+    ReleaseOnExit release_bufs{{&d_ids, &d_dists}};
+    nbpg_status s = d_ids.ensure(size_t(nq) * k * 4);
+    if (s == NBPG_OK && fast) s = d_dists.ensure(size_t(nq) * k * 4);
+    if (s != NBPG_OK) return s;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -634,32 +802,74 @@ extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queri
         row_geometry(idx->row_stride, w, vecs, lpr, vpl);
         if (std::find(widths.begin(), widths.end(), vpl) == widths.end()) widths.push_back(vpl);
     }
-    std::vector<nbpg_search_params> cands;
+    std::vector<nbpg_search_params> shapes;
     for (uint32_t w : widths) {
         nbpg_search_params p = *params;
         p.kernel = NBPG_KERNEL_PLAIN;
         p.lane_width = w;
         p.warps_per_cta = 0;
         p.prefetch = 0;
-        cands.push_back(p);
+        shapes.push_back(p);
         for (uint32_t warps : {4u, 8u, 16u})
             for (int pf : {0, 2}) {
+                if (fast && pf) continue;  // the FAST kernels do not prefetch
                 p.kernel = NBPG_KERNEL_BATCHED;
                 p.warps_per_cta = warps;
                 p.prefetch = pf;
-                cands.push_back(p);
+                shapes.push_back(p);
             }
     }
+    std::vector<nbpg_search_params> cands;
+    const uint32_t S0 = params->hash_slots ? params->hash_slots : fast_default_slots(params->L);
+    if (!fast) {
+        cands = shapes;
+    } else {
+        for (const auto &sh : shapes)
+            for (uint32_t E : {1u, 2u, 4u}) {
+                if (E * R > 256) continue;
+                for (uint32_t S : {S0 / 4, S0 / 2, S0}) {
+                    if (S < 256) continue;
+                    nbpg_search_params p = sh;
+                    p.expand = E;
+                    p.hash_slots = S;
+                    cands.push_back(p);
+                }
+            }
+    }
+    // mean distance over the returned lists (FAST eligibility)
+    std::vector<float> hd(fast ? size_t(nq) * k : 0);
+    auto mean_dist = [&](double &m) -> nbpg_status {
+        NBPG_CUDA_TRY(cudaMemcpyAsync(hd.data(), d_dists.ptr, hd.size() * 4, cudaMemcpyDeviceToHost, st));
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+        double sum = 0;
+        size_t cnt = 0;
+        for (float x : hd)
+            if (x == x && x != __builtin_inff()) { sum += x; ++cnt; }
+        m = cnt ? sum / double(cnt) : 0.0;
+        return NBPG_OK;
+    };
+    double ref_mean = 0;
+    if (fast) {
+        nbpg_search_params p = *params;
+        p.expand = 1;
+        p.hash_slots = S0;
+        s = search_device_impl(idx, idx->scratch, d_queries, nq, &p, nullptr, nullptr, start_points, n_start, k,
+                               d_ids.as<uint32_t>(), d_dists.as<float>(), nullptr, nullptr, nullptr, st);
+        if (s == NBPG_OK) s = mean_dist(ref_mean);
+    }
     float best = 1e30f;
-    nbpg_status s = NBPG_OK;
     nbpg_search_params win = *params;
+    bool found = false;
     for (const auto &p : cands) {
+        if (s != NBPG_OK) break;
         float t = 1e30f;
-        for (int rep = 0; rep < 3 && s == NBPG_OK; ++rep) {
+        nbpg_status r = NBPG_OK;
+        for (int rep = 0; rep < 3 && r == NBPG_OK; ++rep) {
             if (rep > 0) cudaEventRecord(e0, st);
-            s = search_device_impl(idx, idx->scratch, d_queries, nq, &p, nullptr, nullptr, start_points, n_start, k,
-                                   d_ids, nullptr, nullptr, nullptr, nullptr, st);
-            if (rep > 0) {
+            r = search_device_impl(idx, idx->scratch, d_queries, nq, &p, nullptr, nullptr, start_points, n_start, k,
+                                   d_ids.as<uint32_t>(), fast ? d_dists.as<float>() : nullptr, nullptr, nullptr,
+                                   nullptr, st);
+            if (rep > 0 && r == NBPG_OK) {
                 cudaEventRecord(e1, st);
                 cudaEventSynchronize(e1);
                 float ms = 0;
@@ -667,14 +877,23 @@ extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queri
                 t = std::min(t, ms);
             }
         }
-        if (s != NBPG_OK) break;
-        if (t < best) { best = t; win = p; }
+        if (r == NBPG_ERR_UNSUPPORTED && fast) continue;  // a hash that does not fit this launch shape
+        if (r != NBPG_OK) { s = r; break; }
+        if (fast) {
+            double m = 0;
+            if ((s = mean_dist(m)) != NBPG_OK) break;
+            if (m > ref_mean + 1e-3 * std::fabs(ref_mean)) continue;
+        }
+        if (t < best) { best = t; win = p; found = true; }
     }
     cudaStreamSynchronize(st);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(d_ids);
     if (s != NBPG_OK) return s;
+    if (!found) {
+        set_error("no launch configuration ran");
+        return NBPG_ERR_UNSUPPORTED;
+    }
     *tuned = win;
     if (best_ms) *best_ms = best;
     return NBPG_OK;

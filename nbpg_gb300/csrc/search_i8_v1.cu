@@ -4,5 +4,7 @@
 
 namespace nbpg {
 const SearchOps search_ops_i8_v1 = {SearchDispatch<DT_I8, 1>::set_attr, SearchDispatch<DT_I8, 1>::occ,
-                                      SearchDispatch<DT_I8, 1>::launch};
+                                      SearchDispatch<DT_I8, 1>::launch,
+                                      SearchDispatch<DT_I8, 1>::set_attr_fast, SearchDispatch<DT_I8, 1>::occ_fast,
+                                      SearchDispatch<DT_I8, 1>::launch_fast};
 }  // namespace nbpg

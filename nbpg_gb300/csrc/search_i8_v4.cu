@@ -4,5 +4,7 @@
 
 namespace nbpg {
 const SearchOps search_ops_i8_v4 = {SearchDispatch<DT_I8, 4>::set_attr, SearchDispatch<DT_I8, 4>::occ,
-                                      SearchDispatch<DT_I8, 4>::launch};
+                                      SearchDispatch<DT_I8, 4>::launch,
+                                      SearchDispatch<DT_I8, 4>::set_attr_fast, SearchDispatch<DT_I8, 4>::occ_fast,
+                                      SearchDispatch<DT_I8, 4>::launch_fast};
 }  // namespace nbpg

@@ -83,6 +83,8 @@ struct SearchArgs {
                             // made for L); 0 = the search's beam
     uint32_t keep_filter;   // 1: the visited filter is not cleared, it carries over from an earlier
                             // search in the same cell (HNSW's levels of one insert, hnsw.h:179-190)
+    uint32_t expand;        // FAST mode: frontier entries expanded per step
+    uint32_t fast_slots;    // FAST mode: slots of the exact visited hash (a power of two)
     SlotLayout lay;
 };
 

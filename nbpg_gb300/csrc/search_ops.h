@@ -1,7 +1,7 @@
 // Per-element-type search kernels, reached through a small table so that each
 // element type compiles in its own translation unit.
 #pragma once
-#include "search_impl.cuh"
+#include "search_fast.cuh"
 
 namespace nbpg {
 
@@ -10,6 +10,11 @@ struct SearchOps {
     cudaError_t (*occ)(int metric, bool list, bool plain, uint32_t threads, size_t smem, int *blocks);
     void (*launch)(int metric, bool list, bool plain, uint32_t grid, uint32_t warps, size_t smem, const SearchArgs &a,
                    cudaStream_t st);
+    // FAST mode kernels (search_fast.cuh)
+    cudaError_t (*set_attr_fast)(int metric, bool plain, size_t smem);
+    cudaError_t (*occ_fast)(int metric, bool plain, uint32_t threads, size_t smem, int *blocks);
+    void (*launch_fast)(int metric, bool plain, uint32_t grid, uint32_t warps, size_t smem, const SearchArgs &a,
+                        cudaStream_t st);
 };
 
 // Raises a search kernel's dynamic shared-memory attribute to at least smem on `device`, never

@@ -4,5 +4,7 @@
 
 namespace nbpg {
 const SearchOps search_ops_u8_v1 = {SearchDispatch<DT_U8, 1>::set_attr, SearchDispatch<DT_U8, 1>::occ,
-                                      SearchDispatch<DT_U8, 1>::launch};
+                                      SearchDispatch<DT_U8, 1>::launch,
+                                      SearchDispatch<DT_U8, 1>::set_attr_fast, SearchDispatch<DT_U8, 1>::occ_fast,
+                                      SearchDispatch<DT_U8, 1>::launch_fast};
 }  // namespace nbpg

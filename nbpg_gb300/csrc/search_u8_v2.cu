@@ -4,5 +4,7 @@
 
 namespace nbpg {
 const SearchOps search_ops_u8_v2 = {SearchDispatch<DT_U8, 2>::set_attr, SearchDispatch<DT_U8, 2>::occ,
-                                      SearchDispatch<DT_U8, 2>::launch};
+                                      SearchDispatch<DT_U8, 2>::launch,
+                                      SearchDispatch<DT_U8, 2>::set_attr_fast, SearchDispatch<DT_U8, 2>::occ_fast,
+                                      SearchDispatch<DT_U8, 2>::launch_fast};
 }  // namespace nbpg

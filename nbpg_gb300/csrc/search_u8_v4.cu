@@ -4,5 +4,7 @@
 
 namespace nbpg {
 const SearchOps search_ops_u8_v4 = {SearchDispatch<DT_U8, 4>::set_attr, SearchDispatch<DT_U8, 4>::occ,
-                                      SearchDispatch<DT_U8, 4>::launch};
+                                      SearchDispatch<DT_U8, 4>::launch,
+                                      SearchDispatch<DT_U8, 4>::set_attr_fast, SearchDispatch<DT_U8, 4>::occ_fast,
+                                      SearchDispatch<DT_U8, 4>::launch_fast};
 }  // namespace nbpg

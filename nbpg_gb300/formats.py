@@ -70,15 +70,19 @@ def read_graph(path: str) -> np.ndarray:
     return g
 
 
-def write_graph(path: str, g: np.ndarray) -> None:
+def graph_bytes(g: np.ndarray) -> bytes:
+    """The bytes of a .graph file (graph.h:339-379): [n][R], the n degrees, then each node's
+    neighbours in order."""
     g = np.ascontiguousarray(g, dtype=np.uint32)
     n, R1 = g.shape
     deg = g[:, 0]
     mask = np.arange(R1 - 1)[None, :] < deg[:, None]
+    return np.array([n, R1 - 1], dtype=np.uint32).tobytes() + deg.tobytes() + g[:, 1:][mask].tobytes()
+
+
+def write_graph(path: str, g: np.ndarray) -> None:
     with open(path, "wb") as f:
-        np.array([n, R1 - 1], dtype=np.uint32).tofile(f)
-        deg.tofile(f)
-        g[:, 1:][mask].tofile(f)
+        f.write(graph_bytes(g))
 
 
 def read_hid(path: str) -> tuple[int, int, int, np.ndarray]:
@@ -107,12 +111,16 @@ def read_gt(path: str) -> tuple[np.ndarray, np.ndarray]:
     return ids, ds
 
 
-def write_gt(path: str, ids: np.ndarray, dists: np.ndarray) -> None:
+def gt_bytes(ids: np.ndarray, dists: np.ndarray) -> bytes:
+    """The bytes of a .gt file (CompGT.cpp:126-133): [nq][k], the ids, then the distances."""
     ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    return (np.array(ids.shape, dtype=np.uint32).tobytes() + ids.tobytes() +
+            np.ascontiguousarray(dists, dtype=np.float32).tobytes())
+
+
+def write_gt(path: str, ids: np.ndarray, dists: np.ndarray) -> None:
     with open(path, "wb") as f:
-        np.array(ids.shape, dtype=np.uint32).tofile(f)
-        ids.tofile(f)
-        np.ascontiguousarray(dists, dtype=np.float32).tofile(f)
+        f.write(gt_bytes(ids, dists))
 
 
 def read_matrix(path: str) -> tuple[np.ndarray, np.ndarray]:

@@ -238,10 +238,12 @@ class Index:
 
     def build_fgim(self, L: int = 70, VL: int = 140, top_degree: int = 0, num_split: int = 4, num_passes: int = 2,
                    limit: int = 0, min_alpha: float = 1.0, max_alpha: float = 1.1, dynamic_prune: bool = False,
-                   rand_sp: bool = False, repair_isolate: bool = True, with_stats: bool = False):
+                   rand_sp: bool = False, repair_isolate: bool = True, with_stats: bool = False,
+                   dir_bias_scale: float = 0.0):
         """The FGIM build (FGIM.cpp:157-265): pair passes searching the current graph and writing a
         second one, then batch_insert on that graph, which becomes the index's graph."""
-        prm = BuildParams(L, VL, top_degree, num_split, num_passes, limit, 0.0, min_alpha, max_alpha, 0.0, 0.0,
+        prm = BuildParams(L, VL, top_degree, num_split, num_passes, limit, dir_bias_scale, min_alpha, max_alpha, 0.0,
+                          0.0,
                           int(dynamic_prune), int(rand_sp), int(repair_isolate), 0)
         st = BuildStats()
         sv = np.zeros(self.n, np.uint32) if with_stats else None

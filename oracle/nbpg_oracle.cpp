@@ -1224,7 +1224,7 @@ int nbpg_oracle_build(int dtype, int metric, uint32_t dims, const void *base, ui
 // num_split must be >= 1 (with none, the reference's pair pass reads a stale visited list).
 int nbpg_oracle_build_fgim(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t R, uint32_t L,
                            uint32_t VL, uint32_t top_degree, uint32_t num_split, uint32_t num_passes, uint64_t limit,
-                           double min_alpha, double max_alpha, double min_cos, double max_cos, int dynamic_prune,
+                           float dir_bias_scale, double min_alpha, double max_alpha, double min_cos, double max_cos, int dynamic_prune,
                            int rand_sp, int repair_isolate, uint32_t *graph, uint32_t *out_stat_visited,
                            uint32_t *out_stat_dist, uint64_t *out_isolated, int threads)
 {
@@ -1233,7 +1233,8 @@ int nbpg_oracle_build_fgim(int dtype, int metric, uint32_t dims, const void *bas
     std::vector<uint32_t> G(graph, graph + size_t(n) * (R + 1));
     std::vector<uint32_t> toG(size_t(n) * (R + 1), 0u);
     BuildCfg cfg{dtype, metric, dims, static_cast<const uint8_t *>(base), row_bytes(dtype, dims), n, R, L, VL,
-                 top_degree, num_split, num_passes, limit == 0 ? n : limit, 0.0f, float(min_alpha), float(max_alpha),
+                 top_degree, num_split, num_passes, limit == 0 ? n : limit, dir_bias_scale, float(min_alpha),
+                 float(max_alpha),
                  float(min_cos), float(max_cos)};
     Builder b(cfg, G);
     std::vector<uint32_t> inserts(n);

@@ -74,7 +74,7 @@ class CpuLib:
         if hasattr(self.lib, prefix + "build_fgim"):
             f("build_fgim").restype = C.c_int
             f("build_fgim").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, C.c_uint32,
-                                        C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_double,
+                                        C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.c_double,
                                         C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _u32p, _u32p,
                                         _u32p, _u64p, C.c_int]
         if hasattr(self.lib, prefix + "build_hnsw"):
@@ -209,7 +209,7 @@ class CpuLib:
 
 
     def build_fgim(self, dtype, metric, base, R, L, VL=140, top_degree=0, num_split=4, num_passes=2, limit=0,
-                   min_alpha=1.0, max_alpha=1.1, min_cos=0.0, max_cos=0.0, dynamic_prune=False, rand_sp=False,
+                   dir_bias_scale=0.0, min_alpha=1.0, max_alpha=1.1, min_cos=0.0, max_cos=0.0, dynamic_prune=False, rand_sp=False,
                    repair_isolate=True, graph=None, threads=0):
         """The FGIM build (FGIM.cpp:157-265); returns (graph, stat_visited, stat_dist, isolated)."""
         base = np.ascontiguousarray(base)
@@ -218,8 +218,9 @@ class CpuLib:
         sv, sd = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
         iso = np.zeros(1, np.uint64)
         rc = self._f("build_fgim")(DTYPES[dtype], METRICS[metric], dims, base.ctypes.data, n, R, L, VL, top_degree,
-                                   num_split, num_passes, limit, min_alpha, max_alpha, min_cos, max_cos,
-                                   int(dynamic_prune), int(rand_sp), int(repair_isolate), _p(g, _u32p), _p(sv, _u32p),
+                                   num_split, num_passes, limit, dir_bias_scale, min_alpha, max_alpha, min_cos,
+                                   max_cos, int(dynamic_prune), int(rand_sp), int(repair_isolate), _p(g, _u32p),
+                                   _p(sv, _u32p),
                                    _p(sd, _u32p), _p(iso, _u64p), threads)
         if rc != 0:
             raise ValueError("build_fgim rejected its arguments")

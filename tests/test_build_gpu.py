@@ -63,3 +63,63 @@ def test_build_continues_from_prior_graph(gpu_lib, oracle_lib):
     idx = Index(base, "u8", "l2", max_degree=16, graph=g0)
     idx.build_vamana(L=24, VL=32, num_split=0, num_passes=1, max_alpha=1.3)
     assert np.array_equal(_mask(idx.get_graph()), _mask(go))
+
+
+OPTION_CASES = {
+    # cosine-angle prune bounds: per node with the popularity pass, and fixed in a Vamana pass
+    "cos_dynamic": dict(R=24, L=32, VL=48, num_split=4, num_passes=2, dynamic_prune=True, min_alpha=1.05,
+                        max_alpha=1.2, min_cos=0.2, max_cos=0.5),
+    "cos_fixed": dict(R=16, L=24, VL=32, num_split=0, num_passes=1, max_alpha=1.2, min_cos=0.3, max_cos=0.3),
+    # the last pass starts each insert's search at node n - id - 1 (--rand_sp)
+    "rand_sp": dict(R=24, L=32, VL=48, num_split=4, num_passes=2, dynamic_prune=True, min_alpha=1.05,
+                    max_alpha=1.2, rand_sp=True),
+    # the visit limit of the build searches (--limit)
+    "limit_vamana": dict(R=16, L=24, VL=32, num_split=0, num_passes=1, max_alpha=1.2, limit=300),
+    "limit_nbpg": dict(R=24, L=32, VL=48, num_split=4, num_passes=2, max_alpha=1.2, limit=500),
+    # the degree bias of sort_candidates (--dir_bias_scale)
+    "dir_bias_vamana": dict(R=16, L=24, VL=32, num_split=0, num_passes=1, max_alpha=1.2, dir_bias_scale=0.5),
+    "dir_bias_nbpg": dict(R=24, L=32, VL=48, num_split=4, num_passes=2, dynamic_prune=True, min_alpha=1.05,
+                          max_alpha=1.2, dir_bias_scale=2.0),
+    "dir_bias_ip": dict(R=16, L=24, VL=40, num_split=0, num_passes=2, max_alpha=1.1, dir_bias_scale=0.75,
+                        metric="ip"),
+}
+
+
+@pytest.mark.parametrize("name", list(OPTION_CASES))
+def test_build_options_match_oracle(gpu_lib, oracle_lib, name):
+    """The build options the defaults leave off (Vamana.cpp:59-85: --max_cos_angle/--min_cos_angle,
+    --rand_sp, --limit, --dir_bias_scale): the GPU graph and BuildStats counters equal the oracle's,
+    which equals the reference's own build through the harness on the same options."""
+    from nbpg_gb300.index import Index
+    c = dict(OPTION_CASES[name])
+    metric = c.pop("metric", "l2")
+    R = c.pop("R")
+    base = _data("u8", n=3000)
+    go, sv, sd, iso = oracle_lib.build_graph("u8", metric, base, R=R, sp_seed=5, **c)
+    kw = dict(c)
+    if "min_cos" in kw:
+        kw["min_cos_angle"] = kw.pop("min_cos")
+    if "max_cos" in kw:
+        kw["max_cos_angle"] = kw.pop("max_cos")
+    idx = Index(base, "u8", metric, max_degree=R)
+    st, gsv, gsd = idx.build_vamana(sp_seed=5, with_stats=True, **kw)
+    g = idx.get_graph()
+    assert np.array_equal(_mask(g), _mask(go)), f"graph rows differ on {int((_mask(g) != _mask(go)).any(1).sum())} nodes"
+    assert st.isolated == iso
+    assert np.array_equal(gsv, sv) and np.array_equal(gsd, sd)
+
+
+@pytest.mark.parametrize("dtype,metric", [("u8", "l2"), ("i8", "ip")])
+def test_fgim_dir_bias_matches_oracle(gpu_lib, oracle_lib, dtype, metric):
+    """The FGIM build with the degree bias (FGIM_nsw.h:93 passes --dir_bias_scale to
+    sort_candidates, degrees from the graph its pair passes search)."""
+    from nbpg_gb300.index import Index
+    base = _data(dtype, n=2500)
+    kw = dict(L=24, VL=32, num_split=2, num_passes=3, dynamic_prune=True, min_alpha=1.05, max_alpha=1.2,
+              dir_bias_scale=0.75)
+    go, sv, sd, iso = oracle_lib.build_fgim(dtype, metric, base, R=16, **kw)
+    idx = Index(base, dtype, metric, max_degree=16)
+    st, gsv, gsd = idx.build_fgim(with_stats=True, **kw)
+    assert np.array_equal(_mask(idx.get_graph()), _mask(go))
+    assert st.isolated == iso
+    assert np.array_equal(gsv, sv) and np.array_equal(gsd, sd)

@@ -16,6 +16,8 @@ def _kw(flags):
         kw["min_alpha"] = float(f[f.index("--min_alpha") + 1])
     if "--max_alpha" in f:
         kw["max_alpha"] = float(f[f.index("--max_alpha") + 1])
+    if "--dir_bias_scale" in f:
+        kw["dir_bias_scale"] = float(f[f.index("--dir_bias_scale") + 1])
     return kw
 
 
@@ -37,8 +39,8 @@ def test_oracle_fgim_matches_reference_graph(oracle_lib, name):
 @pytest.mark.parametrize("dtype,metric,dims", [("i8", "l2", 24), ("u4", "l2", 16), ("u8", "ip", 32), ("i4", "ip", 16)])
 def test_oracle_fgim_matches_reference_binary_every_row_type(oracle_lib, tmp_path, dtype, metric, dims):
     """The reference FGIM binary, run here where it was built from its sources, on the other row
-    types (.i8bin, .u4bin, .i4bin) and on inner product (--use_mips): its .graph equals the
-    oracle's build byte for byte."""
+    types (.i8bin, .u4bin, .i4bin) and on inner product (--use_mips), with and without the degree
+    bias of sort_candidates (--dir_bias_scale): its .graph equals the oracle's build byte for byte."""
     import subprocess
     from oracle.oracle import REF_COMPGT
     from nbpg_gb300 import formats
@@ -52,7 +54,8 @@ def test_oracle_fgim_matches_reference_binary_every_row_type(oracle_lib, tmp_pat
     formats.write_vectors(path, base)
     for flags in (["--num_split", "2", "--num_passes", "2"],
                   ["--num_split", "3", "--num_passes", "3", "--dynamic_prune", "--min_alpha", "1.05", "--max_alpha",
-                   "1.2"]):
+                   "1.2"],
+                  ["--num_split", "2", "--num_passes", "2", "--dir_bias_scale", "0.75"]):
         ip = str(tmp_path / "idx")
         cmd = [exe, "--quant_base_path", path, "--index_path", ip, "--R", "16", "--L", "24", "--VL", "32", "--rebuild",
                *flags] + (["--use_mips"] if metric == "ip" else [])

@@ -91,14 +91,16 @@ def test_oracle_build_is_independent_of_thread_count(oracle_lib):
 
 def test_oracle_matches_reference_harness_on_options(oracle_lib, ref_lib):
     """The options the defaults leave untouched: cosine-angle prune bounds, random start points,
-    a visit limit during the build; search limits, degree limits, cut values, a visited cap small
+    a visit limit during the build, the degree bias of sort_candidates; search limits, degree limits, cut values, a visited cap small
     enough to overflow (visited_factor 2), repeated start points, and the extreme beams."""
     base, q, g = dataset("u8", "l2")
     for extra in [dict(max_cos=0.5, min_cos=0.2, dynamic_prune=True, num_split=4, num_passes=2),
                   dict(max_cos=0.3, min_cos=0.3, num_split=0, num_passes=1),
                   dict(rand_sp=True, num_split=4, num_passes=2, dynamic_prune=True),
                   dict(limit=300, num_split=0, num_passes=1),
-                  dict(limit=500, num_split=4, num_passes=2)]:
+                  dict(limit=500, num_split=4, num_passes=2),
+                  dict(dir_bias_scale=0.5, num_split=0, num_passes=1),
+                  dict(dir_bias_scale=2.0, num_split=4, num_passes=2, dynamic_prune=True)]:
         kw = dict(R=16, L=24, VL=30, max_alpha=1.2, min_alpha=1.05, sp_seed=5, **extra)
         go = oracle_lib.build_graph("u8", "l2", base[:1500], **kw)
         gr = ref_lib.build_graph("u8", "l2", base[:1500], **kw)
