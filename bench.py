@@ -330,6 +330,226 @@ def time_hnsw(base, q, gi, k, local, n_prefix=100_000):
     return out
 
 
+def time_fast(idx, q, qdev, gi, gd, gei, ged, k, stream, reps=50):
+    """FAST mode at the workload: for each L of the sweep, nbpg_search_autotune in fast mode picks
+    expansions per step, visited-hash size and launch shape; the first L whose results reach
+    recall@10 >= 0.95 (CompGT ground truth) is timed with CUDA events over device-resident queries.
+    Also each expansion count alone at that L, for the record."""
+    import torch
+    from nbpg_gb300.index import LaunchConfig, QueryParams
+    from nbpg_gb300.recall import recall_at_k
+    nq = len(q)
+    o_ids = torch.empty((nq, k), dtype=torch.int32, device=qdev.device)
+    o_m = torch.empty(nq, dtype=torch.int32, device=qdev.device)
+    o_v = torch.empty(nq, dtype=torch.int32, device=qdev.device)
+
+    def timed(qp, launch):
+        def run():
+            idx.search_device(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, None, None, o_v.data_ptr(),
+                              o_m.data_ptr(), launch=launch, stream=stream.cuda_stream)
+        for _ in range(3):
+            run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return nq * reps / (e0.elapsed_time(e1) / 1e3)
+
+    sweep, L_op, tuned, rec, r = [], None, None, 0.0, None
+    for L in L_SWEEP:
+        qp = QueryParams(k=k, beamSize=L, cut=CFG["cut"])
+        tuned, _ = idx.autotune(qdev.data_ptr(), nq, qp, mode="fast")
+        r = idx.search(q, qp, launch=tuned)
+        rec = recall_at_k(r.ids, gi, gd, k)
+        sweep.append((L, round(rec, 4), tuned.expand))
+        if rec >= CFG["recall_target"]:
+            L_op = L
+            break
+    if L_op is None:
+        L_op = L_SWEEP[-1]
+    qp = QueryParams(k=k, beamSize=L_op, cut=CFG["cut"])
+    out = {"L": L_op, "recall@10": round(rec, 4), "recall@10_exact_gt": round(recall_at_k(r.ids, gei, ged, k), 4),
+           "qps": timed(qp, tuned), "avg_expansions": float(r.visited.mean()), "avg_dist_cmps": float(r.cmps.mean()),
+           "launch": {"kernel": tuned.kernel, "warps_per_cta": tuned.warps_per_cta, "lane_width": tuned.lane_width,
+                      "expand": tuned.expand, "hash_slots": tuned.hash_slots, "chosen_by": "nbpg_search_autotune"},
+           "L_sweep": sweep, "per_expand": {}}
+    for E in (1, 2, 4):
+        lc = LaunchConfig(kernel=tuned.kernel, warps_per_cta=tuned.warps_per_cta, lane_width=tuned.lane_width,
+                          mode="fast", expand=E, hash_slots=tuned.hash_slots)
+        rr = idx.search(q, qp, launch=lc)
+        out["per_expand"][str(E)] = {"qps": timed(qp, lc), "recall@10": round(recall_at_k(rr.ids, gi, gd, k), 4),
+                                     "avg_expansions": float(rr.visited.mean())}
+    return out
+
+
+def _qps_device(idx, q, qp, launch, local, reps=20, d_Ls=None, d_ks=None, kst=None):
+    """Queries/s of a device-resident search (CUDA events on the launching stream, after warm-up)."""
+    import torch
+    nq = len(q)
+    kst = kst or qp.k
+    _, row_stride, _, _ = idx.device_info()
+    dev = torch.device("cuda", local)
+    qdev = torch.zeros((nq, row_stride), dtype=torch.uint8, device=dev)
+    qdev[:, :q.shape[1]] = torch.from_numpy(np.ascontiguousarray(q).view(np.uint8)).to(dev)
+    o_ids = torch.empty((nq, kst), dtype=torch.int32, device=dev)
+    st = torch.cuda.Stream(device=dev)
+
+    def run():
+        idx.search_device(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), kst, launch=launch, stream=st.cuda_stream,
+                          d_Ls=d_Ls, d_ks=d_ks)
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        run()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    return nq * reps / (e0.elapsed_time(e1) / 1e3), qdev
+
+
+def bench_c1(local):
+    """The reference's CPU-runnable configuration: 100k base + 1k queries x 128 u8 (256-centre
+    mixture), exact k=10 L2 kNN by brute force, Vamana build R=64 L=100 alpha=1.2 one pass, search
+    at L in {20, 50, 100}: recall@10 and QPS, the GPU beside the oracle port on all host cores
+    (the two builds compared)."""
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import Index, QueryParams, ground_truth
+    from nbpg_gb300.recall import recall_at_k
+    from oracle.oracle import oracle
+    threads = os.cpu_count() or 1
+    base, q = synth.u8_mixture(100_000, 1_000, dim=128, n_centres=256)
+    kw = dict(L=100, VL=140, num_split=0, num_passes=1, max_alpha=1.2)
+    idx = Index(base, "u8", "l2", max_degree=64, device=local)
+    st, _, _ = idx.build_vamana(**kw)
+    g = idx.get_graph()
+    O = oracle()
+    t = time.perf_counter()
+    g_cpu, _, _, _ = O.build_graph("u8", "l2", base, R=64, threads=threads, **kw)
+    cpu_build_s = time.perf_counter() - t
+    mask = np.arange(64)[None, :] < g[:, :1]
+    same = bool(np.array_equal(g[:, :1], g_cpu[:, :1]) and np.array_equal(g[:, 1:][mask], g_cpu[:, 1:][mask]))
+    gi, gd = ground_truth(base, q, "u8", "l2", k=10, exact=True, device=local)
+    out = {"n_base": len(base), "n_query": len(q), "gpu_build_s": st.seconds, "cpu_build_s": cpu_build_s,
+           "cpu_threads": threads, "graph_equal_to_port": same, "search": {}}
+    for L in (20, 50, 100):
+        qp = QueryParams(k=10, beamSize=L, cut=CFG["cut"])
+        r = idx.search(q, qp)
+        qps_plain, qdev = _qps_device(idx, q, qp, None, local)
+        tuned, _ = idx.autotune(qdev.data_ptr(), len(q), qp)
+        qps_tuned, _ = _qps_device(idx, q, qp, tuned, local)
+        O.search("u8", "l2", base, g_cpu, q, L=L, k=10, cut=CFG["cut"], threads=threads)
+        reps, t = 0, time.perf_counter()
+        while True:
+            oi = O.search("u8", "l2", base, g_cpu, q, L=L, k=10, cut=CFG["cut"], threads=threads)[0]
+            reps += 1
+            if time.perf_counter() - t >= 2.0:
+                break
+        cpu_qps = reps * len(q) / (time.perf_counter() - t)
+        out["search"][f"L{L}"] = {"recall@10": round(recall_at_k(r.ids, gi, gd, 10), 4),
+                                  "gpu_qps": max(qps_plain, qps_tuned), "gpu_qps_default_batched": qps_plain,
+                                  "cpu_port_qps": cpu_qps, "gpu_over_cpu": max(qps_plain, qps_tuned) / cpu_qps,
+                                  "ids_equal_to_port": bool(np.array_equal(r.ids, oi)),
+                                  "avg_expansions": float(r.visited.mean()), "avg_dist_cmps": float(r.cmps.mean())}
+    idx.close()
+    return out
+
+
+def exact_float_knn(xb, xq, k, local):
+    """Exact float32 L2 kNN in FP64 on the device (a measurement tool for recall, not the product
+    path): squared distances |q|^2 + |b|^2 - 2 q.b in float64, smallest k by (distance, id)."""
+    import torch
+    dev = torch.device("cuda", local)
+    b = torch.from_numpy(xb).to(dev, torch.float64)
+    bn = (b * b).sum(1)
+    out = np.empty((len(xq), k), np.int64)
+    for s in range(0, len(xq), 1000):
+        qq = torch.from_numpy(xq[s:s + 1000]).to(dev, torch.float64)
+        d = (qq * qq).sum(1, keepdim=True) + bn[None, :] - 2.0 * qq @ b.T
+        out[s:s + len(qq)] = torch.topk(d, k, dim=1, largest=False, sorted=True).indices.cpu().numpy()
+        del d
+    del b
+    return out
+
+
+def bench_c3(local):
+    """The PCA-compressed configuration: 1M base + 10k query float32 rows x 128 (1000-centre mixture,
+    centres N(0, 4I), unit noise), PCA fitted in FP64 on the host to 64 dims, encoded on the device to
+    4-bit codes two per byte (32-byte rows) unsigned and signed; NBPG build R=48 L=80 (two passes,
+    split 4, dynamic prune, min_alpha 1.05) on the device; strict search with the nibble-unpacking
+    distance; recall@10 against the float32 exact kNN."""
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import Index, QueryParams
+    from nbpg_gb300.pca import encode, fit
+    xb, xq = synth.f32_mixture(1_000_000, 10_000, dim=128, n_centres=1000)
+    t = time.perf_counter()
+    mat, bias = fit(xb, 64)
+    fit_s = time.perf_counter() - t
+    gt = exact_float_knn(xb, xq, 10, local)
+    out = {"n_base": len(xb), "n_query": len(xq), "pca_fit_s_host_fp64": fit_s, "codes": {}}
+    for code in ("u4", "i4"):
+        b = encode(xb, mat, bias, code, device=local)
+        q = encode(xq, mat, bias, code, device=local)
+        idx = Index(b, code, "l2", max_degree=48, device=local)
+        st, _, _ = idx.build_vamana(L=80, VL=140, num_split=4, num_passes=2, dynamic_prune=True, min_alpha=1.05,
+                                    max_alpha=1.2, sp_seed=0)
+        res = {"build_s": st.seconds, "L_sweep": []}
+        for L in (10, 20, 40, 80, 160):
+            qp = QueryParams(k=10, beamSize=L, cut=CFG["cut"])
+            r = idx.search(q, qp)
+            qps, qdev = _qps_device(idx, q, qp, None, local)
+            tuned, _ = idx.autotune(qdev.data_ptr(), len(q), qp)
+            tq, _ = _qps_device(idx, q, qp, tuned, local)
+            res["L_sweep"].append({"L": L, "recall@10_vs_float_exact": round(recall_of(r.ids, gt, 10), 4),
+                                   "qps": max(qps, tq), "avg_dist_cmps": float(r.cmps.mean())})
+        out["codes"][code] = res
+        idx.close()
+    return out
+
+
+def bench_c4(local):
+    """The uneven batch: 10M base x 96 i8 (unit-normalised mixture x 127), inner product, NBPG build
+    R=64 L=128 (two passes, split 4, dynamic prune) on the device; 100k queries in one call with
+    per-query L drawn from {32, 64, 128, 256} and k from {1, 10, 100} (k clipped to L: the reference
+    rejects k > L); the persistent batched kernel (longest beam first) against the plain kernel,
+    host API (query copies included), and the recall@10 of queries with k >= 10 against the
+    brute-force kNN (exact mode)."""
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import Index, LaunchConfig, QueryParams, ground_truth
+    t = time.perf_counter()
+    b, q = synth.i8_unit_mixture(10_000_000, 100_000, dim=96, n_centres=1000)
+    synth_s = time.perf_counter() - t
+    idx = Index(b, "i8", "ip", max_degree=64, device=local)
+    st, _, _ = idx.build_vamana(L=128, VL=140, num_split=4, num_passes=2, dynamic_prune=True, min_alpha=1.05,
+                                max_alpha=1.2, sp_seed=0)
+    rng = np.random.default_rng(7)
+    Ls = rng.choice([32, 64, 128, 256], size=len(q)).astype(np.uint32)
+    ks = np.minimum(rng.choice([1, 10, 100], size=len(q)), Ls).astype(np.uint32)
+    qp = QueryParams(k=100, beamSize=256, cut=CFG["cut"])
+    out = {"n_base": len(b), "n_query": len(q), "synth_s": synth_s, "build_s": st.seconds}
+    res = {}
+    for name, lc in (("plain", LaunchConfig(kernel="plain")), ("batched", LaunchConfig(kernel="batched")),
+                     ("fast_batched", LaunchConfig(kernel="batched", mode="fast", expand=2, hash_slots=4096))):
+        idx.search(q, qp, Ls=Ls, ks=ks, launch=lc)
+        t = time.perf_counter()
+        r = idx.search(q, qp, Ls=Ls, ks=ks, launch=lc)
+        res[name] = r
+        out[name + "_qps"] = len(q) / (time.perf_counter() - t)
+    out["batched_over_plain"] = out["batched_qps"] / out["plain_qps"]
+    out["identical_plain_batched"] = bool(np.array_equal(res["plain"].ids, res["batched"].ids))
+    gi, _ = ground_truth(b, q, "i8", "ip", k=10, exact=True, device=local)
+    sel = ks >= 10
+    out["recall@10_k>=10_strict"] = round(recall_of(res["batched"].ids[sel], gi[sel], 10), 4)
+    out["recall@10_k>=10_fast"] = round(recall_of(res["fast_batched"].ids[sel], gi[sel], 10), 4)
+    out["fast_launch"] = "batched, expand 2, 4096-slot hash"
+    idx.close()
+    return out
+
+
 def parity_hashes(g, gi, gd):
     """SHA-256 of the 1M-row index's .graph file bytes and of its CompGT-mode .gt file bytes: the GPU
     arm and the CPU arm build and compute these independently, so equal hashes in the two JSON
@@ -368,7 +588,7 @@ def cpu_search_qps(base, g, q, L, threads, min_seconds=8.0):
             return reps * len(q) / el, reps
 
 
-def time_serving(idx, q, res_op, L_op, k, tuned, value):
+def time_serving(idx, q, res_op, L_op, k, tuned, value, mixed_peak):
     """Continuous batching with Poisson arrivals (requests admitted as batch slots and the
     working-set budget free up): p50/p99 latency from each request's arrival to completion,
     at half the measured peak, at 500k QPS, and with the serving configuration's L/k mix."""
@@ -389,19 +609,27 @@ def time_serving(idx, q, res_op, L_op, k, tuned, value):
         log(f"[bench] serving {name}: offered {rate:.3g} QPS, achieved {len(qq) / el:.3g}, "
             f"p50 {p50:.3f} ms, p99 {p99:.3f} ms")
     srv.close()
-    # the serving configuration's request mix: L in {32,64,128,256}, k in {1,10,100}, k <= L
+    # the serving configuration's request mix: L in {32,64,128,256}, k in {1,10,100}, k <= L, at
+    # offered loads from a quarter of to the whole batched peak of the same mix (one 10k-query call
+    # of the persistent kernel), and at 500k QPS
     rng = np.random.default_rng(11)
     Ls = rng.choice([32, 64, 128, 256], size=len(qq)).astype(np.uint32)
     ks = np.minimum(rng.choice([1, 10, 100], size=len(qq)), Ls).astype(np.uint32)
     srv = Server(idx, max_L=256, max_k=100, max_batch=4096, max_in_flight=4,
                  qp=QueryParams(k=100, beamSize=256, cut=CFG["cut"]))
     srv.replay(q[:5000], rate_qps=2e5, Ls=Ls[:5000], ks=ks[:5000], seed=9)
-    ids, ds, cnt, lat, el = srv.replay(qq, rate_qps=5e5, Ls=Ls, ks=ks, seed=5)
-    p50, p99 = np.percentile(lat, [50, 99])
-    serving["mixed_L_k_at_500k_qps"] = {"offered_qps": 5e5, "achieved_qps": len(qq) / el, "p50_ms": float(p50),
-                                       "p99_ms": float(p99), "requests": len(qq),
-                                       "L": "U{32,64,128,256}", "k": "U{1,10,100}, k<=L"}
-    log(f"[bench] serving mixed: achieved {len(qq) / el:.3g}, p50 {p50:.3f} ms, p99 {p99:.3f} ms")
+    points = []
+    for frac, rate in [(None, 5e5)] + [(f, f * mixed_peak) for f in (0.25, 0.5, 0.75, 1.0)]:
+        ids, ds, cnt, lat, el = srv.replay(qq, rate_qps=rate, Ls=Ls, ks=ks, seed=5)
+        p50, p99 = np.percentile(lat, [50, 99])
+        points.append({"offered_fraction_of_peak": frac, "offered_qps": rate, "achieved_qps": len(qq) / el,
+                       "p50_ms": float(p50), "p99_ms": float(p99), "requests": len(qq)})
+        log(f"[bench] serving mixed L/k at {rate:.3g} offered: achieved {len(qq) / el:.3g}, p50 {p50:.3f} ms, "
+            f"p99 {p99:.3f} ms")
+    half = [p for p in points if p["offered_fraction_of_peak"] is not None and p["offered_fraction_of_peak"] >= 0.5]
+    serving["config5_mixed_L_k"] = {"L": "U{32,64,128,256}", "k": "U{1,10,100}, k<=L",
+                                    "batched_peak_qps": mixed_peak, "points": points,
+                                    "p99_le_2ms_at_ge_half_peak": bool(any(p["p99_ms"] <= 2.0 for p in half))}
     srv.close()
     return serving
 
@@ -492,9 +720,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--skip-configs", action="store_true", help="leave out the C1/C3/C4 configuration lines")
     ap.add_argument("--save-graph", default=None, help="write the built graph (.graph format) here")
     ap.add_argument("--load-graph", default=None, help="use this graph instead of building one")
-    ap.add_argument("--profile", default=None, choices=["search", "gt", "builds"],
+    ap.add_argument("--profile", default=None, choices=["search", "gt", "builds", "fast"],
                     help="profiling run: warmup + steps of one kernel only (the search at --L, or the brute-force kNN)")
     ap.add_argument("--gt-engine", default="tensor", choices=["tensor", "dp4a"], help="--profile gt engine")
     ap.add_argument("--L", type=int, default=0, help="beam width for --profile (default: the sweep's choice)")
@@ -572,6 +801,16 @@ def main():
     log(f"[bench] average degree {avg_deg:.2f}")
     if args.profile == "search":
         return profile_search(idx, q, args.L or 19, args)
+    if args.profile == "fast":
+        # FAST mode beside the strict search at the workload (no timed steps, no secondary rows)
+        gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
+        gei, ged = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=True, device=local)
+        _, row_stride, _, _ = idx.device_info()
+        qdev = torch.zeros((nq, row_stride), dtype=torch.uint8, device="cuda")
+        qdev[:, :CFG["dim"]] = torch.from_numpy(q).cuda()
+        print(json.dumps({"profile": "fast", "fast": time_fast(idx, q, qdev, gi, gd, gei, ged, k,
+                                                               torch.cuda.Stream())}), flush=True)
+        return
     t = time.time()
     gi, gd = ground_truth(base, q, "u8", "l2", k=CFG["gt_k"], exact=False, device=local)
     gt_s = time.time() - t
@@ -706,6 +945,16 @@ def main():
     uneven["batched_over_plain"] = uneven["batched_qps"] / uneven["plain_qps"]
     log(f"[bench] uneven L/k: {uneven}")
 
+    # FAST mode (exact visited hash, several expansions per step): QPS at the same recall target
+    try:
+        fast = time_fast(idx, q, qdev, gi, gd, gei, ged, k, stream)
+        fast["over_strict_tuned"] = fast["qps"] / value
+        log(f"[bench] FAST mode: L={fast['L']} recall {fast['recall@10']} {fast['qps']:.3g} QPS "
+            f"({fast['over_strict_tuned']:.2f}x strict), launch {fast['launch']}")
+    except Exception as exc:  # a secondary measurement: reported in the line, not fatal
+        fast = {"error": str(exc)}
+        log(f"[bench] FAST mode failed: {exc}")
+
     # e2e through the C ABI: pinned host queries in, host results out, every step
     L = _lib.lib()
     qh = torch.from_numpy(q).pin_memory()
@@ -767,12 +1016,26 @@ def main():
             next_rows["hnsw"] = {"error": str(exc)}
             log(f"[bench] HNSW failed: {exc}")
 
+    # the other configurations at their stated sizes (secondary lines of the same JSON record)
+    configs = None
+    if rank == 0 and not args.skip_configs:
+        configs = {}
+        for name, fn in (("C1_vamana_100k_u8", bench_c1), ("C3_pca64_4bit_1m", bench_c3),
+                         ("C4_uneven_ip_10m_i8", bench_c4)):
+            t = time.perf_counter()
+            try:
+                configs[name] = fn(local)
+            except Exception as exc:  # reported in the line, not fatal
+                configs[name] = {"error": str(exc)}
+            configs[name]["wall_s"] = round(time.perf_counter() - t, 1)
+            log(f"[bench] {name}: {json.dumps(configs[name])[:600]}")
+
     # serving: continuous batching with Poisson arrivals (requests admitted as batch slots
     # and working-set budget free up); latency from each request's arrival to completion
     serving = None
     if rank == 0:
         try:
-            serving = time_serving(idx, q, res_op, L_op, k, tuned, value)
+            serving = time_serving(idx, q, res_op, L_op, k, tuned, value, uneven["batched_qps"])
         except Exception as exc:  # a secondary measurement: reported in the line, not fatal
             serving = {"error": str(exc)}
             log(f"[bench] serving failed: {exc}")
@@ -809,7 +1072,7 @@ def main():
                                   "chosen_by": "nbpg_search_autotune"},
                        "plain_kernel_qps": plain_qps, "batched_default_qps": batched_default_qps,
                        "tuned_over_plain": value / plain_qps, "cuda_graph_qps": graph_qps,
-                       "uneven_L_k_batch": uneven,
+                       "uneven_L_k_batch": uneven, "fast_mode": fast,
                        "build_s": None if build_s is None else round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
                        "L_sweep": sweep, "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -822,7 +1085,8 @@ def main():
                                                      "p50": serving["at_half_peak"]["p50_ms"],
                                                      "p99": serving["at_half_peak"]["p99_ms"],
                                                      "at_offered_qps": serving["at_half_peak"]["offered_qps"]},
-            "serving": serving, "ground_truth": gt_dev, "next_rows": next_rows, "parity": hashes}
+            "serving": serving, "ground_truth": gt_dev, "next_rows": next_rows, "configs": configs,
+            "parity": hashes}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

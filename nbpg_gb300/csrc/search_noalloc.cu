@@ -17,7 +17,11 @@
 // each other's results: serialise them.  Each device that loads the library holds the
 // array until the process exits.  The first call on a device looks up the array's
 // device address with cudaGetSymbolAddress; make that first call before any stream
-// capture begins.
+// capture begins.  The address is kept together with the device's current context and
+// looked up again when the context changes (after cudaDeviceReset the module is loaded
+// anew and the array can move).
+#include <cuda.h>
+
 #include <algorithm>
 #include <array>
 #include <mutex>
@@ -43,8 +47,28 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
 static std::mutex g_noalloc_mu;
 static std::array<uint32_t *, 64> g_noalloc_ptr{};
+static std::array<void *, 64> g_noalloc_ctx{};  // the context each cached address belongs to
 
-// Once per device, with that device current.
+// The current context of the calling thread (the primary context of the current device once
+// the runtime has touched it), through the driver entry point so that no driver library is linked.
+static void *current_context()
+{
+    using GetCtx = CUresult (*)(CUcontext *);
+    static GetCtx fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<GetCtx>(p);
+    }();
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// With the device current: the array's device address, looked up on a device's first call and
+// again whenever the device's context is not the one the cached address was taken in.
 static nbpg_status noalloc_scratch(int device, uint32_t **out)
 {
     if (device < 0 || device >= int(g_noalloc_ptr.size())) {
@@ -52,7 +76,8 @@ static nbpg_status noalloc_scratch(int device, uint32_t **out)
         return NBPG_ERR_INVALID_ARG;
     }
     std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
+    void *ctx = current_context();
+    if (!g_noalloc_ptr[device] || !ctx || ctx != g_noalloc_ctx[device]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -60,6 +85,7 @@ static nbpg_status noalloc_scratch(int device, uint32_t **out)
             return NBPG_ERR_CUDA;
         }
         g_noalloc_ptr[device] = static_cast<uint32_t *>(p);
+        g_noalloc_ctx[device] = ctx ? ctx : current_context();
     }
     *out = g_noalloc_ptr[device];
     return NBPG_OK;
@@ -99,6 +125,10 @@ extern "C" nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint
     NBPG_CHECK_ARG(P->L >= 1 && P->L <= 1024 && P->k >= 1 && P->k <= P->L && k_stride >= P->k,
                    "k must be in [1, L], L in [1, 1024], k_stride >= k");
     NBPG_CHECK_ARG(P->kernel == NBPG_KERNEL_BATCHED || P->kernel == NBPG_KERNEL_PLAIN, "unknown kernel");
+    if (P->mode != NBPG_MODE_STRICT) {
+        set_error("nbpg_search_noalloc runs the strict search only");
+        return NBPG_ERR_UNSUPPORTED;
+    }
     // repeated start points are accepted as the reference accepts them (the frontier then holds
     // copies of a key; query_params.h:204-221, beamSearch.h:154-160)
     for (uint32_t i = 0; i < n_start; ++i) NBPG_CHECK_ARG(start_points[i] < n, "start point out of range");
@@ -163,13 +193,30 @@ extern "C" nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint
     a.out_count = d_out_count;
     a.out_visited = d_out_visited;
     a.out_cmps = d_out_cmps;
+    // The error word is cleared above and never read back: the argument checks of this function
+    // (k <= L, start points <= L, the filter and visited list fitting the slot the layout sizes
+    // for L) cover every case in which search_query rejects a query on the device.
     a.err = scratch + 2;
     a.prefetch = P->prefetch < 0 ? 0u : std::min<uint32_t>(uint32_t(P->prefetch), 8u);
 
     auto grid_of = [&](bool list, const SlotLayout &lay, uint32_t want, uint32_t &warps, size_t &smem,
                        uint32_t &grid) -> nbpg_status {
         const uint32_t fit = uint32_t(prop.sharedMemPerBlockOptin / lay.bytes);
-        warps = std::max<uint32_t>(1, std::min<uint32_t>(want ? want : 16, std::min<uint32_t>(16, fit)));
+        uint32_t w = want;
+        if (!w) {
+            // the CTA size with the most resident warps per SM, as the regular entry point picks it
+            int best = -1;
+            for (uint32_t c : {16u, 8u, 4u, 2u}) {
+                if (c > fit) continue;
+                const size_t sm = size_t(c) * lay.bytes;
+                int b = 0;
+                NBPG_CUDA_TRY(raise_search_attr(device, ops, met, list, false, sm));
+                NBPG_CUDA_TRY(ops->occ(met, list, false, int(c) * 32, sm, &b));
+                if (int(c) * b > best) { best = int(c) * b; w = c; }
+            }
+            if (!w) w = 1;
+        }
+        warps = std::max<uint32_t>(1, std::min<uint32_t>(w, std::min<uint32_t>(16, fit)));
         smem = size_t(warps) * lay.bytes;
         NBPG_CUDA_TRY(raise_search_attr(device, ops, met, list, false, smem));
         int blocks = 0;

@@ -37,16 +37,29 @@ class QueryParams:
 
 @dataclass
 class LaunchConfig:
-    """How a search is launched (never what it returns): kernel form and its knobs."""
+    """How a search is launched: kernel form and its knobs, which never change what a strict
+    search returns; and the mode: "strict" (the reference's results) or "fast" (an exact visited
+    hash of hash_slots slots and `expand` frontier entries expanded per step; valid neighbour
+    lists that are not the reference's)."""
     kernel: str = "batched"   # "batched" (persistent, device queue) or "plain" (one query per block)
     warps_per_cta: int = 0    # 0 = default
     lane_width: int = 0       # 16-byte words per lane per vector row; 0 = default
     prefetch: int = -1        # upcoming adjacency rows prefetched to L2; -1 = default
+    mode: str = "strict"      # "strict" or "fast"
+    expand: int = 0           # fast: frontier entries expanded per step; 0 = default
+    hash_slots: int = 0       # fast: visited-hash slots (power of two); 0 = default for L
 
     def params(self, qp: "QueryParams") -> SearchParams:
         return SearchParams(int(qp.k), int(qp.beamSize), float(qp.cut), int(qp.limit), int(qp.degree_limit),
                             int(qp.visited_factor), _lib.KERNELS[self.kernel], int(self.warps_per_cta),
-                            int(self.lane_width), int(self.prefetch))
+                            int(self.lane_width), int(self.prefetch), _lib.MODES[self.mode], int(self.expand),
+                            int(self.hash_slots))
+
+    @staticmethod
+    def of(p: SearchParams) -> "LaunchConfig":
+        kern = {v: k for k, v in _lib.KERNELS.items()}[p.kernel]
+        mode = {v: k for k, v in _lib.MODES.items()}[p.mode]
+        return LaunchConfig(kern, p.warps_per_cta, p.lane_width, p.prefetch, mode, p.expand, p.hash_slots)
 
 
 @dataclass
@@ -111,7 +124,8 @@ class Index:
     # -- search ----------------------------------------------------------------
     def search(self, queries: np.ndarray, qp: QueryParams, start_points=(0,), kernel: str = "batched",
                Ls=None, ks=None, warps_per_cta: int = 0, launch: "LaunchConfig | None" = None) -> SearchResult:
-        """Strict search of host queries; results identical to the reference's."""
+        """Search of host queries: in strict mode (the default launch) results identical to the
+        reference's; `launch` may select the fast mode."""
         q = np.ascontiguousarray(queries)
         if q.ndim != 2 or q.shape[1] != self.dims:
             raise ValueError("queries must be (nq, dims)")
@@ -199,16 +213,17 @@ class Index:
         check(_lib.lib().nbpg_search_device_sp(self._h, d_queries, nq, C.byref(prm), d_start_points, sp_stride,
                                                k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
 
-    def autotune(self, d_queries: int, nq: int, qp: QueryParams, start_points=(0,)):
-        """nbpg_search_autotune: the fastest LaunchConfig for these device queries, and its ms per launch."""
+    def autotune(self, d_queries: int, nq: int, qp: QueryParams, start_points=(0,), mode: str = "strict",
+                 hash_slots: int = 0):
+        """nbpg_search_autotune: the fastest LaunchConfig for these device queries, and its ms per
+        launch.  In fast mode it also picks expansions per step and the visited-hash size."""
         sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
-        prm = LaunchConfig().params(qp)
+        prm = LaunchConfig(mode=mode, hash_slots=hash_slots).params(qp)
         out = SearchParams()
         ms = C.c_float(0)
         check(_lib.lib().nbpg_search_autotune(self._h, d_queries, nq, C.byref(prm), _p(sp), len(sp), C.byref(out),
                                               C.byref(ms)))
-        kern = {v: k for k, v in _lib.KERNELS.items()}[out.kernel]
-        return LaunchConfig(kern, out.warps_per_cta, out.lane_width, out.prefetch), ms.value
+        return LaunchConfig.of(out), ms.value
 
     def search_graph(self, d_queries: int, nq: int, qp: QueryParams, d_out_ids: int, k_stride: int,
                      d_out_dists=None, d_count=None, d_visited=None, d_cmps=None, start_points=(0,),
