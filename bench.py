@@ -1040,11 +1040,18 @@ def main():
             serving = {"error": str(exc)}
             log(f"[bench] serving failed: {exc}")
 
-    # roofline of the search kernel: algorithmic bytes per launch
-    vis = res_op.visited.astype(np.float64)
+    # roofline of the search kernel: algorithmic bytes per launch, from the kernel's own per-query
+    # counters (adjacency words read, distances computed) of the timed request
+    o_adj = torch.empty(nq, dtype=torch.int32, device="cuda")
+    idx.search_device_adj(qdev.data_ptr(), nq, qp, o_ids.data_ptr(), k, o_adj.data_ptr(), launch=tuned,
+                          stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    adj = o_adj.cpu().numpy().view(np.uint32).astype(np.float64)
+    assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "counted search results differ"
     cmps = res_op.cmps.astype(np.float64)
     row = float(CFG["dim"])
-    alg_bytes = float((vis * 4.0 * (1.0 + avg_deg) + cmps * row + row).sum())
+    alg_bytes = float((adj * 4.0 + cmps * row + row).sum())
+    alg_bytes_avg_deg = float((res_op.visited.astype(np.float64) * 4.0 * (1.0 + avg_deg) + cmps * row + row).sum())
     peak, peak_src = measured_peaks()
     achieved = alg_bytes / (total_s / args.steps) / 1e9
     tpq = traffic_per_query()
@@ -1079,6 +1086,11 @@ def main():
             "gpu_launches": 2 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "algorithmic_bytes_rule": "sum over queries of 4 x adjacency words read (1 + neighbours "
+                                                   "scanned per expansion, the kernel's own counter) + 128 B x "
+                                                   "(distances + 1)",
+                         "algorithmic_bytes_with_graph_avg_degree": alg_bytes_avg_deg,
                          "traffic": None if tpq is None else tpq * nq},
             "cpu_baseline": cpu, "clocks": clocks,
             "latency_ms": None if not serving or "at_half_peak" not in serving else {

@@ -113,7 +113,7 @@ typedef struct nbpg_search_params {
     int32_t prefetch;        /* adjacency rows of upcoming frontier entries prefetched to L2
                                 per expansion (batched kernel, STRICT); -1 = default */
     uint32_t mode;           /* nbpg_search_mode; 0 = STRICT */
-    uint32_t expand;         /* FAST: frontier entries expanded per step, expand * R <= 256;
+    uint32_t expand;         /* FAST: frontier entries expanded per step, expand * ceil(R / 32) <= 8;
                                 0 = 2 (1 when R > 128) */
     uint32_t hash_slots;     /* FAST: slots of the visited hash, a power of two in [256, 65536];
                                 0 = the smallest power of two >= max(2048, 64 * L), at most 16384 */
@@ -138,6 +138,18 @@ nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t 
                                const uint32_t *d_Ls, const uint32_t *d_ks, const uint32_t *start_points,
                                uint32_t n_start, uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
                                uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps, void *stream);
+
+/* As nbpg_search_device (uniform L and k), plus d_out_adj_words (nq entries, may be NULL): per
+ * query, the 32-bit adjacency words the search read, 1 + the neighbours scanned for every node it
+ * expanded.  With the distance count it gives the query's algorithmic bytes,
+ * 4 * adj_words + row_bytes * (cmps + 1) (the query row, then one base row per distance): the
+ * numerator of the search's memory roofline.  No counterpart in the reference, whose QueryStatic
+ * counts expansions and distances only (query_params.h:47-94). */
+nbpg_status nbpg_search_device_adj(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                   const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
+                                   uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists, uint32_t *d_out_count,
+                                   uint32_t *d_out_visited, uint32_t *d_out_cmps, uint32_t *d_out_adj_words,
+                                   void *stream);
 
 /* Per-query start points (qsearchAll's get_sp(i), beamSearch.h:257-300): d_start_points holds
  * sp_stride entries per query on the device, padded with 0xFFFFFFFF after the first (which is

@@ -95,6 +95,8 @@ struct SearchEmit {
     uint32_t factor = 0;
     bool visited = false;
     uint32_t *d_fs = nullptr;
+    uint32_t *d_adj = nullptr;  // per query: adjacency words read (1 + neighbours scanned per expansion)
+    bool rerank() const { return factor || visited || d_fs; }
 };
 
 // What a search runs over when it is not the index's own rows and graph (HNSW's level 0, one row

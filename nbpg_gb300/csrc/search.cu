@@ -305,12 +305,13 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
     const bool plain = P->kernel == NBPG_KERNEL_PLAIN;
     NBPG_CHECK_ARG(P->mode == NBPG_MODE_STRICT || P->mode == NBPG_MODE_FAST, "unknown search mode");
     if (P->mode == NBPG_MODE_FAST) {
-        if (emit) {
+        if (emit && emit->rerank()) {
             set_error("re-ranking and filtering run on the strict search only");
             return NBPG_ERR_UNSUPPORTED;
         }
         const uint32_t E = P->expand ? P->expand : fast_default_expand(R);
-        NBPG_CHECK_ARG(E >= 1 && E * R <= 256 && E <= 8, "FAST: expand must be in [1, 8] with expand * R <= 256");
+        NBPG_CHECK_ARG(E >= 1 && E * ((R + 31) / 32) <= 8,
+                       "FAST: expand must be >= 1 with expand * ceil(R / 32) <= 8 (adjacency chunks in flight)");
         const uint32_t S = P->hash_slots ? P->hash_slots : fast_default_slots(P->L);
         NBPG_CHECK_ARG(S >= 256 && S <= 65536 && (S & (S - 1)) == 0,
                        "FAST: hash_slots must be a power of two in [256, 65536]");
@@ -359,6 +360,7 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
         a.err = q + 2;
         a.queue = q;
         a.order = sc.order;
+        a.out_adj = emit ? emit->d_adj : nullptr;
         a.expand = E;
         a.fast_slots = S;
         a.lay = pc.lay;
@@ -437,6 +439,7 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
         a.emit_factor = emit->factor;
         a.emit_visited = emit->visited ? 1u : 0u;
         a.out_fs = emit->d_fs;
+        a.out_adj = emit->d_adj;
     }
 
     // main pass (queries in the caller's order, or longest beam first when given)
@@ -485,6 +488,22 @@ extern "C" nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries
     return search_device_impl(idx, idx->scratch, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride,
                               d_out_ids,
                               d_out_dists, d_out_count, d_out_visited, d_out_cmps, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" nbpg_status nbpg_search_device_adj(nbpg_index *idx, const void *d_queries, uint32_t nq,
+                                              const nbpg_search_params *params, const uint32_t *start_points,
+                                              uint32_t n_start, uint32_t k_stride, uint32_t *d_out_ids,
+                                              float *d_out_dists, uint32_t *d_out_count, uint32_t *d_out_visited,
+                                              uint32_t *d_out_cmps, uint32_t *d_out_adj_words, void *stream)
+{
+    if (!idx) { set_error("null index"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(idx->mu);
+    cudaSetDevice(idx->desc.device);
+    SearchEmit em;
+    em.d_adj = d_out_adj_words;
+    return search_device_impl(idx, idx->scratch, d_queries, nq, params, nullptr, nullptr, start_points, n_start,
+                              k_stride, d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps,
+                              static_cast<cudaStream_t>(stream), &em);
 }
 
 extern "C" nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_queries, uint32_t nq,
@@ -826,7 +845,7 @@ extern "C" nbpg_status nbpg_search_autotune(nbpg_index *idx, const void *d_queri
     } else {
         for (const auto &sh : shapes)
             for (uint32_t E : {1u, 2u, 4u}) {
-                if (E * R > 256) continue;
+                if (E * ((R + 31) / 32) > 8) continue;
                 for (uint32_t S : {S0 / 4, S0 / 2, S0}) {
                     if (S < 256) continue;
                     nbpg_search_params p = sh;

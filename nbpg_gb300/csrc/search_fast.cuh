@@ -57,7 +57,7 @@ __device__ void search_fast_query(const SearchArgs &a, uint32_t qi, uint8_t *slo
         while (nsp < a.sp_stride && sp[nsp] != kNoId) ++nsp;
     }
     if (L == 0 || k == 0 || k > L || L > lay.Lcap || nsp > L || k > a.k_stride || S > lay.Scap || S < 32 ||
-        E == 0 || E * a.R > lay.Ccap) {
+        E == 0 || E * ((a.R + 31) / 32) > 8 || E * a.R > lay.Ccap) {
         for (uint32_t j = lane; j < a.k_stride; j += 32) {
             a.out_ids[size_t(qi) * a.k_stride + j] = kNoId;
             if (a.out_dists) a.out_dists[size_t(qi) * a.k_stride + j] = __int_as_float(0x7f800000);
@@ -110,7 +110,7 @@ __device__ void search_fast_query(const SearchArgs &a, uint32_t qi, uint8_t *slo
     __syncwarp();
 
     int b = 0;
-    uint32_t fs = ns, remain = ns, cmps = ns;
+    uint32_t fs = ns, remain = ns, cmps = ns, adj = 0;
     uint64_t nvis = 0;
     uint64_t tail = fs == L ? fr0[L - 1] : kKeyMax;
     const uint32_t nch = (a.R + 31) / 32;
@@ -145,6 +145,7 @@ __device__ void search_fast_query(const SearchArgs &a, uint32_t qi, uint8_t *slo
             if (e >= ne) break;
             uint32_t d = __shfl_sync(kFull, mydeg, int(e));
             if (d > a.degree_limit) d = a.degree_limit;
+            if (c == 0) adj += 1 + d;
             const uint32_t i = c * 32 + lane;
             const bool keep = i < d && fast_insert(H, smask, shift, nbv[j]);
             const unsigned km = __ballot_sync(kFull, keep);
@@ -231,6 +232,7 @@ __device__ void search_fast_query(const SearchArgs &a, uint32_t qi, uint8_t *slo
         if (a.out_count) a.out_count[qi] = kk;
         if (a.out_visited) a.out_visited[qi] = uint32_t(nvis);
         if (a.out_cmps) a.out_cmps[qi] = cmps;
+        if (a.out_adj) a.out_adj[qi] = adj;
     }
     __syncwarp();
 }

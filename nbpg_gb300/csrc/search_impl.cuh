@@ -78,6 +78,7 @@ struct SearchArgs {
     uint32_t emit_factor;   // emit frontier[0 : min(k * emit_factor, fs)] instead of [0 : k)
     uint32_t emit_visited;  // LIST mode: emit the final visited list, count its insertions
     uint32_t *out_fs;       // frontier size at the end of each query (may be null)
+    uint32_t *out_adj;      // adjacency words read per query, 1 + neighbours scanned per expansion (may be null)
     uint32_t filter_L;      // beam that sizes the visited filter when it differs from the search's
                             // own (HNSW's upper levels search with beam hier_beamSize in a cell
                             // made for L); 0 = the search's beam
@@ -287,6 +288,7 @@ struct SearchState {
     int b;
     uint32_t fs, vs, cmps, smask;
     uint32_t ins;  // LIST mode: expansions inserted into the capped visited list
+    uint32_t adj;  // adjacency words read: 1 + neighbours scanned, per expansion
     uint64_t nvis;
     bool taint;
     __device__ uint64_t *frontier() const { return b ? fr1 : fr0; }
@@ -365,6 +367,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     int b = 0;
     uint32_t fs = nsp;
     uint32_t cmps = nsp;
+    uint32_t adj = 0;
     uint64_t nvis = 0;
     uint32_t vs = 0;
     uint32_t remain = nsp, offset = 0, cs = 0, ins = 0;
@@ -402,6 +405,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             }
         }
         const uint32_t ne = deg < a.degree_limit ? deg : a.degree_limit;
+        adj += 1 + ne;
 
         // visited filter, in neighbour order (beamSearch.h:71-83)
         uint32_t nf = 0;
@@ -559,6 +563,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
     st.fs = fs;
     st.vs = vs;
     st.cmps = cmps;
+    st.adj = adj;
     st.ins = ins;
     st.nvis = nvis;
     st.taint = taint;
@@ -636,6 +641,7 @@ __device__ void search_query(const SearchArgs &a, uint32_t qi, uint8_t *slot, ui
         if (a.out_count) a.out_count[qi] = kk;
         if (a.out_visited) a.out_visited[qi] = uint32_t(nvis);
         if (a.out_cmps) a.out_cmps[qi] = cmps_out;
+        if (a.out_adj) a.out_adj[qi] = st.adj;
         if (a.out_fs) a.out_fs[qi] = fs;
         if constexpr (!LIST) {
             if (taint && a.taint) {

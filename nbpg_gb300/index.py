@@ -203,6 +203,16 @@ class Index:
         check(_lib.lib().nbpg_search_device(self._h, d_queries, nq, C.byref(prm), d_Ls, d_ks, _p(sp), len(sp),
                                             k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
 
+    def search_device_adj(self, d_queries: int, nq: int, qp: QueryParams, d_out_ids: int, k_stride: int,
+                          d_out_adj: int, d_visited: int | None = None, d_cmps: int | None = None,
+                          start_points=(0,), stream: int = 0, launch: "LaunchConfig | None" = None) -> None:
+        """nbpg_search_device_adj: a device search that also writes each query's adjacency words read
+        (1 + neighbours scanned per expansion), the numerator of the search's memory roofline."""
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        prm = (launch or LaunchConfig()).params(qp)
+        check(_lib.lib().nbpg_search_device_adj(self._h, d_queries, nq, C.byref(prm), _p(sp), len(sp), k_stride,
+                                                d_out_ids, None, None, d_visited, d_cmps, d_out_adj, stream))
+
     def search_device_sp(self, d_queries: int, nq: int, qp: QueryParams, d_start_points: int, sp_stride: int,
                          d_out_ids: int, k_stride: int, d_out_dists: int | None = None, d_count: int | None = None,
                          d_visited: int | None = None, d_cmps: int | None = None, stream: int = 0,

@@ -226,3 +226,36 @@ def test_host_call_graph_replay_follows_the_buffers(gpu_lib):
     call()
     assert np.array_equal(oi.numpy().view(np.uint32), ref_b.ids)
     assert np.array_equal(ov.numpy().view(np.uint32), ref_b.visited)
+
+
+@pytest.mark.parametrize("mode", ["strict", "fast"])
+def test_adjacency_word_counter(gpu_lib, mode):
+    """nbpg_search_device_adj counts 1 + the neighbours scanned per expanded node: on a graph whose
+    every node has exactly d neighbours that is visited x (1 + min(d, degree_limit))."""
+    import torch
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import Index, LaunchConfig, QueryParams
+    base, q = synth.u8_mixture(3000, 200, dim=32, n_centres=24)
+    rng = np.random.default_rng(5)
+    R, d = 24, 20
+    g = np.zeros((len(base), R + 1), np.uint32)
+    g[:, 0] = d
+    for i in range(len(base)):
+        g[i, 1:d + 1] = rng.choice(np.delete(np.arange(len(base)), i), d, replace=False)
+    idx = Index(base, "u8", "l2", max_degree=R, graph=g)
+    _, rs, _, _ = idx.device_info()
+    qd = torch.zeros((len(q), rs), dtype=torch.uint8, device="cuda")
+    qd[:, :32] = torch.from_numpy(q).cuda()
+    for dl, per in ((0, 1 + d), (8, 9)):
+        qp = QueryParams(k=10, beamSize=40, degree_limit=dl)
+        ids = torch.empty((len(q), 10), dtype=torch.int32, device="cuda")
+        adj, vis, cm = (torch.zeros(len(q), dtype=torch.int32, device="cuda") for _ in range(3))
+        idx.search_device_adj(qd.data_ptr(), len(q), qp, ids.data_ptr(), 10, adj.data_ptr(), vis.data_ptr(),
+                              cm.data_ptr(), launch=LaunchConfig(mode=mode))
+        torch.cuda.synchronize()
+        v = vis.cpu().numpy()
+        assert (v > 0).all()
+        assert np.array_equal(adj.cpu().numpy(), v * per)
+        if mode == "strict":
+            r = idx.search(q, qp)
+            assert np.array_equal(ids.cpu().numpy().view(np.uint32), r.ids) and np.array_equal(v, r.visited)
