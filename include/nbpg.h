@@ -452,6 +452,18 @@ nbpg_status nbpg_hnsw_search(nbpg_hnsw *h, const void *queries, uint32_t nq, con
                              uint32_t hier_beam, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
                              uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps);
 
+/* hier_qsearchAll with raw rows (HNSW.cpp:93-124 with --base_path and --rerank_factor): where the
+ * index holds raw rows of another row size (nbpg_index_set_raw_points), level 0 runs
+ * beam_search_rerank over the nodes (each node's raw row is its vector's, hier_beamSearch.h:41-42):
+ * rerank_factor > 0 re-ranks frontier[0 : min(k * rerank_factor, frontier)] by raw distance,
+ * 0 filters the visited list; ties by node id, then the ids become vector ids.  raw_queries: nq
+ * raw rows.  Without such raw rows this is nbpg_hnsw_search.  out_dists are the raw distances;
+ * k <= 256 and the re-rank set <= 4096 as for nbpg_search_rerank. */
+nbpg_status nbpg_hnsw_search_rerank(nbpg_hnsw *h, const void *queries, const void *raw_queries, uint32_t nq,
+                                    const nbpg_search_params *params, uint32_t hier_beam, uint32_t rerank_factor,
+                                    uint32_t k_stride, uint32_t *out_ids, float *out_dists, uint32_t *out_count,
+                                    uint32_t *out_visited, uint32_t *out_cmps);
+
 nbpg_status nbpg_hnsw_destroy(nbpg_hnsw *h);
 
 #ifdef __cplusplus

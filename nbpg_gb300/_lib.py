@@ -140,6 +140,8 @@ def lib() -> C.CDLL:
     L.nbpg_hnsw_build.argtypes = [_vp, C.POINTER(HnswParams), C.POINTER(_vp), C.POINTER(BuildStats), _u32p, _u32p]
     L.nbpg_hnsw_info.argtypes = [_vp, _u64p, _u64p, _u64p, _u32p]
     L.nbpg_hnsw_get.argtypes = [_vp, _u32p, C.POINTER(C.c_int64)]
+    L.nbpg_hnsw_search_rerank.argtypes = [_vp, _vp, _vp, C.c_uint32, C.POINTER(SearchParams), C.c_uint32,
+                                          C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p, _u32p, _u32p]
     L.nbpg_hnsw_load.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint64, _u32p, C.POINTER(C.c_int64), C.POINTER(_vp)]
     L.nbpg_hnsw_search.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), C.c_uint32, C.c_uint32, _u32p,
                                    _f32p, _u32p, _u32p, _u32p]

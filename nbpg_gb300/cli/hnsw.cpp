@@ -3,8 +3,8 @@
 // is <index_path>.graph (one row per node, graph.h:339-379 layout) and <index_path>.hid
 // (HIdMapping::save, hier_idmapping.h:35-46), loaded instead of rebuilt unless --rebuild
 // (HNSW.cpp:172-177).  Query evaluation is search_and_parse over hier_qsearchAll
-// (hier_check_nn_Recall.h:46-80) on the quantised rows; a --base_path (raw rows for re-ranking)
-// is refused, as that path is not built here.
+// (hier_check_nn_Recall.h:46-80): on the quantised rows, or, with --base_path raw rows and
+// --query_path raw queries, re-ranked at level 0 (nbpg_hnsw_search_rerank, --rerank_factor).
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -155,10 +155,28 @@ int main(int argc, char **argv)
 
     // ---- query evaluation (HNSW.cpp:244-288, hier_check_nn_Recall.h)
     if (a.quant_query_path.empty() || a.gt_path.empty()) { nbpg_index_destroy(idx); return 0; }
-    if (!a.base_path.empty()) die("nbpg_hnsw: re-ranked HNSW queries (--base_path) are not supported by this library");
     uint32_t nq, qd;
     std::vector<uint8_t> Q = read_rows(a.quant_query_path, nq, qd, a.q_num);
     if (qd != dims) die("query and base dimensions differ");
+    // raw rows for re-ranking (HNSW.cpp:255-281): --base_path of any vector type with --query_path of
+    // the same type; level 0 of each query then re-ranks (--rerank_factor > 0) or filters (0)
+    uint32_t raw_dtype = dtype, raw_dims = dims, rn = n, rqn = nq;
+    std::vector<uint8_t> raw_base, raw_q;
+    const bool raw = !a.base_path.empty();
+    if (raw) {
+        if (ends_with(a.base_path, ".u8bin")) raw_dtype = NBPG_U8;
+        else if (ends_with(a.base_path, ".u4bin")) raw_dtype = NBPG_U4;
+        else if (ends_with(a.base_path, ".i8bin")) raw_dtype = NBPG_I8;
+        else if (ends_with(a.base_path, ".i4bin")) raw_dtype = NBPG_I4;
+        else if (ends_with(a.base_path, ".fbin") || ends_with(a.base_path, ".bin")) raw_dtype = NBPG_F32;
+        else { nbpg_index_destroy(idx); return 0; }  // the reference runs no query for other extensions
+        const size_t elem = raw_dtype == NBPG_F32 ? 4 : 1;
+        raw_base = read_rows(a.base_path, rn, raw_dims, 0, elem);
+        uint32_t rqd = 0;
+        raw_q = read_rows(a.query_path, rqn, rqd, a.q_num, elem);
+        if (rn != n || rqn != nq || rqd != raw_dims) die("raw base/query files do not match the quantised ones");
+        check(nbpg_index_set_raw_points(idx, raw_dtype, raw_dims, raw_base.data(), 0, n));
+    }
     G = read_graph(gfile, gn, R);
     uint64_t mx = 0, sp = 0;
     std::vector<int64_t> pre = read_hid(hfile, mx, sp);
@@ -172,9 +190,15 @@ int main(int argc, char **argv)
     SearchFn search = [&](uint32_t qk, uint32_t beam, double cut, uint64_t limit, uint32_t dl, uint32_t *ids,
                           uint32_t *cnt, uint32_t *vis, uint32_t *cmps) {
         nbpg_search_params spm{qk, beam, cut, limit, dl, 8, NBPG_KERNEL_BATCHED, 0, 0, -1};
-        check(nbpg_hnsw_search(h, Q.data(), nq, &spm, a.hier_beam, qk, ids, nullptr, cnt, vis, cmps));
+        if (raw)
+            check(nbpg_hnsw_search_rerank(h, Q.data(), raw_q.data(), nq, &spm, a.hier_beam, a.rerank_factor, qk, ids,
+                                          nullptr, cnt, vis, cmps));
+        else
+            check(nbpg_hnsw_search(h, Q.data(), nq, &spm, a.hier_beam, qk, ids, nullptr, cnt, vis, cmps));
     };
-    Eval e{idx, false, &Q, nq, &gt, gk, gn, R, a.verbose};
+    // tie-extended recall over the raw rows when --base_path gave them, else the quantised rows
+    const std::vector<uint8_t> &tie_q = raw ? raw_q : Q;
+    Eval e{idx, raw, &tie_q, nq, &gt, gk, gn, R, a.verbose};
     search_and_parse(e, search, k, a.Q, a.res_path, "HNSW", params, gn, build_s, avg_deg, maxdeg, isolated);
     nbpg_hnsw_destroy(h);
     nbpg_index_destroy(idx);

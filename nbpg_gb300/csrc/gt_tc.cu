@@ -34,10 +34,7 @@ constexpr int TC_N = 128;        // base rows per tile
 constexpr int TC_KATOM = 64;     // bf16 elements per 128-byte swizzled row
 constexpr uint32_t TC_MAX_STAGES = 4;  // shared-memory ring of base tiles: 2..4 deep as memory allows
 constexpr uint32_t TC_ACC = 4;         // TMEM accumulators of 128 columns: all 512 columns of the SM
-constexpr int TC_EPI_WARPS = 16;  // epilogue: 4 TMEM lane quarters x 4 column chunks
-constexpr int TC_WARP_TMA = TC_EPI_WARPS, TC_WARP_MMA = TC_EPI_WARPS + 1;
-constexpr int TC_THREADS = (TC_EPI_WARPS + 2) * 32;  // warps 0-15 epilogue, 16 TMA, 17 MMA
-constexpr uint32_t TC_BARS = 2 * 4 + 7 * 4 + 2;      // mbarriers (stage ring, accumulators, norms, masks)
+constexpr int TC_THREADS = 192;  // warps 0-3 epilogue, 4 TMA, 5 MMA
 constexpr uint64_t TC_WAIT_NS = 2000000000ull;  // 2 s: far above any wait of a working pipeline
 constexpr uint32_t TC_WAIT_POLLS = 1u << 30;
 constexpr uint32_t TC_QUEUE = 8;  // flagged candidates queued per query before a drain
@@ -114,19 +111,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
             "r"(dst),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
         : "memory");
-}
-
-// plain bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on bar
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void named_barrier_sync(uint32_t id, uint32_t threads)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 
 // K-major operand, 128-byte swizzle: rows of 128 B, 8-row groups 1024 B apart
@@ -315,15 +299,9 @@ __device__ __forceinline__ float tk_offer(const TkList &L, TkState &S, float dis
     return S.cnt < L.k ? kInf : S.topdist;
 }
 
-// Epilogue.  Sixteen warps read the accumulator: warp w serves TMEM lane quarter w % 4 (queries
-// 32 (w % 4) .. +31 of the CTA, a warp may only reach its own quarter's lanes) and column chunk
-// w / 4 (ids 32 (w / 4) .. +31 of each 128-row tile), so each SM scheduler interleaves four
-// epilogue warps instead of one.  Per tile every warp flags, for each of its queries, the
-// candidates of its chunk whose distance is below the query's survivor bound B; the chunk-0 warp
-// of the quarter owns the queries: it collects the other three chunks' flag masks (shared memory,
-// an mbarrier per accumulator and quarter) and replays the flagged candidates in id order,
-// reading their accumulators back from TMEM, through the admission rule; it publishes the new
-// bound for the next tiles' tests (a stale, larger bound only flags more).
+// Epilogue of one query (one thread, one TMEM lane).  Per 32-column chunk a cheap test
+// flags the candidates whose distance is below the survivor bound B; only those are
+// replayed through the admission rule, in id order.
 //   CompGT: B = max(topdist, max of the list).  B never grows: an admission replaces an
 //           entry below topdist and the new topdist is an entry of the list or the value
 //           of topk[0] read before the overwrite, which was at most B.  A candidate at or
@@ -331,8 +309,7 @@ __device__ __forceinline__ float tk_offer(const TkList &L, TkState &S, float dis
 //   exact:  B = the k-th distance; ids only grow, so a tie at B never enters.
 // Distances stay exact integers in fp32 throughout: L2 = (|q|^2 + (|b|^2 - 2 q.b)) * scale,
 // IP = -(q.b) * scale; the tests compare on the accumulator side (q.b, |b|^2 - 2 q.b) against
-// B / scale shifted by |q|^2, all exact below 2^24.  The base norms of the tile in an
-// accumulator come into shared memory with it (a bulk copy the MMA warp issues).
+// B / scale shifted by |q|^2, all exact below 2^24.
 template <int MET>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gt_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a)
@@ -343,28 +320,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t atom_bytes = TC_M * 128;  // one 64-element column of 128 rows (A and B tiles alike)
     const uint32_t tile_bytes = a.katoms * atom_bytes;
     uint8_t *sA = smem;
-    uint8_t *sB = smem + tile_bytes;                                          // a.stages tiles
-    uint8_t *win = sB + a.stages * tile_bytes;                                // [128][128] tree nodes
-    float *qv = reinterpret_cast<float *>(win + TC_M * TC_M);                 // [TC_QUEUE][128] queued accumulators
-    uint32_t *qi = reinterpret_cast<uint32_t *>(qv + TC_QUEUE * TC_M);          // [TC_QUEUE][128] queued ids
-    uint32_t *masks = qi + TC_QUEUE * TC_M;                                   // [TC_ACC][4 chunks][128] flags
-    float *thr_s = reinterpret_cast<float *>(masks + TC_ACC * 4 * TC_M);      // [128] published bounds
-    float *nring = thr_s + TC_M;                                              // [TC_ACC][128] base norms
-    uint64_t *bars = reinterpret_cast<uint64_t *>(nring + TC_ACC * TC_M);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + TC_BARS);
-    float *tk_d = reinterpret_cast<float *>(tmem_slot + 4);                   // [k][128]
+    uint8_t *sB = smem + tile_bytes;                                        // a.stages tiles
+    uint8_t *win = sB + a.stages * tile_bytes;                              // [128][128] tree nodes
+    float *qv = reinterpret_cast<float *>(win + TC_M * TC_M);               // [TC_QUEUE][128] queued accumulators
+    uint32_t *qi = reinterpret_cast<uint32_t *>(qv + TC_QUEUE * TC_M);        // [TC_QUEUE][128] queued ids
+    uint64_t *bars = reinterpret_cast<uint64_t *>(qi + TC_QUEUE * TC_M);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 24);
+    float *tk_d = reinterpret_cast<float *>(tmem_slot + 4);                 // [k][128]
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // full/empty: the base-tile ring; tfull/tempty: the TMEM accumulators; nfull: the norms of the
-    // tile in an accumulator; mfull: the non-owner flag masks of an accumulator's tile, per quarter
+    // full/empty: the base-tile ring; tfull/tempty: the TMEM accumulators
     const uint32_t bar_full = smem_u32(bars + 0), bar_empty = smem_u32(bars + TC_MAX_STAGES),
                    bar_tfull = smem_u32(bars + 2 * TC_MAX_STAGES),
                    bar_tempty = smem_u32(bars + 2 * TC_MAX_STAGES + TC_ACC),
-                   bar_nfull = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC),
-                   bar_mfull = smem_u32(bars + 2 * TC_MAX_STAGES + 3 * TC_ACC),
-                   bar_a = smem_u32(bars + 2 * TC_MAX_STAGES + 7 * TC_ACC),
-                   bar_done = smem_u32(bars + 2 * TC_MAX_STAGES + 7 * TC_ACC + 1);
-    const uint32_t q0 = blockIdx.x * TC_M;
+                   bar_a = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC),
+                   bar_done = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 1);
     if (tid == 0) {
         for (uint32_t s = 0; s < a.stages; ++s) {
             mbar_init(bar_full + 8 * s, 1);
@@ -372,16 +342,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         for (uint32_t s = 0; s < TC_ACC; ++s) {
             mbar_init(bar_tfull + 8 * s, 1);
-            mbar_init(bar_tempty + 8 * s, TC_EPI_WARPS * 32);
-            mbar_init(bar_nfull + 8 * s, 1);
-            for (uint32_t g = 0; g < 4; ++g) mbar_init(bar_mfull + 8 * (s * 4 + g), 3);
+            mbar_init(bar_tempty + 8 * s, TC_M);
         }
         mbar_init(bar_a, 1);
         mbar_init(bar_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp < 4) thr_s[tid] = q0 + tid < a.nq ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
-    if (warp == TC_WARP_TMA) {
+    if (warp == 4) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
@@ -389,9 +356,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    const uint32_t q0 = blockIdx.x * TC_M;
     const uint32_t T = a.ntiles;
 
-    if (warp == TC_WARP_TMA) {
+    if (warp == 4) {
         if (lane == 0) {
             // queries once, then base tiles through the ring
             mbar_expect_tx(bar_a, tile_bytes);
@@ -413,21 +381,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 mbar_wait(bar_full + 8 * (t % a.stages), (t / a.stages) & 1, a.err);
         }
         __syncwarp();
-    } else if (warp == TC_WARP_MMA) {
+    } else if (warp == 5) {
         if (lane == 0) {
             const uint32_t idesc = tc_idesc(TC_M, TC_N);
             bool ok = mbar_wait(bar_a, 0, a.err);
-            uint32_t s = 0, ph = 0, nissued = 0;
+            uint32_t s = 0, ph = 0;
             for (uint32_t t = 0; ok && t < T; ++t) {
                 const uint32_t ts = t % TC_ACC, tph = (t / TC_ACC) & 1;  // TMEM accumulator
                 if (!mbar_wait(bar_full + 8 * s, ph, a.err)) break;
                 if (!mbar_wait(bar_tempty + 8 * ts, tph ^ 1, a.err)) break;
-                if constexpr (MET == M_L2) {
-                    // the tile's base norms beside its accumulator (the epilogue released both)
-                    mbar_expect_tx(bar_nfull + 8 * ts, TC_N * 4);
-                    bulk_load(smem_u32(nring + ts * TC_M), a.bnorm + size_t(t) * TC_N, TC_N * 4, bar_nfull + 8 * ts);
-                    ++nissued;
-                }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t d = tmem + ts * TC_N;
                 const uint32_t aB = smem_u32(sA), bB = smem_u32(sB + s * tile_bytes);
@@ -439,18 +401,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 tc_commit(bar_tfull + 8 * ts);   // accumulator ts ready
                 if (++s == a.stages) { s = 0; ph ^= 1; }
             }
-            // all issued MMAs complete, and the last norm copies landed, before teardown
+            // all issued MMAs complete before teardown
             tc_commit(bar_done);
             mbar_wait(bar_done, 0, a.err);
-            for (uint32_t t = nissued > TC_ACC ? nissued - TC_ACC : 0; t < nissued; ++t)
-                mbar_wait(bar_nfull + 8 * (t % TC_ACC), (t / TC_ACC) & 1, a.err);
         }
         __syncwarp();
     } else {
-        const uint32_t quarter = uint32_t(warp) & 3u, chunk = uint32_t(warp) >> 2;
-        const uint32_t tq = quarter * 32 + lane;  // TMEM lane = query slot of the CTA
-        const bool owner = chunk == 0;            // owner warps are 0..3, so tid == tq there
-        const uint32_t q = q0 + tq;
+        const uint32_t q = q0 + tid;
         const bool live = q < a.nq;
         const float qn = live ? a.qnorm[q] : 0.0f;
         const uint32_t k = a.k;
@@ -460,7 +417,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         L.d = tk_d;
         L.id = live ? a.out_ids + size_t(q) * k : nullptr;
         L.win = win;
-        L.tid = int(tq);
+        L.tid = tid;
         L.k = k;
         L.exact = a.exact;
         L.lo = a.exact ? 0u : 1u;
@@ -473,32 +430,48 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // |q|^2 (L2).  A candidate can survive only if t_j < thr = B / scale - |q|^2.
         // Until the list holds k entries everything passes; padding queries never do.
         float thr = live ? kInf : -kInf;
-        const uint32_t lane_addr = tmem + ((quarter * 32) << 16);
+        float4 bn_next[8];
+        if constexpr (MET == M_L2) {
+            const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) bn_next[j] = __ldg(bp + j);
+        }
         for (uint32_t t = 0; t < T; ++t) {
             const uint32_t s = t % TC_ACC, ph = (t / TC_ACC) & 1;
-            // warp-uniform waits so that the warp stays converged for tcgen05.ld
-            bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
-            if constexpr (MET == M_L2) ok = ok && __all_sync(kFull, mbar_wait(bar_nfull + 8 * s, ph, a.err));
+            // warp-uniform wait so that the warp stays converged for tcgen05.ld
+            const bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
             if (!ok) {
                 done = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const float *bnt = nring + s * TC_M;
-            const uint64_t tile0 = uint64_t(t) * TC_N;
-            // ids at or past n are zero padding rows of the last tile
-            const uint32_t nvalid = a.n - tile0 >= TC_N ? uint32_t(TC_N) : uint32_t(a.n - tile0);
-            uint32_t v[32];
-            auto flag_chunk = [&](uint32_t c, float bound) -> uint32_t {
+            for (uint32_t c = 0; c < TC_N / 32; ++c) {
+                const uint64_t id0 = uint64_t(t) * TC_N + c * 32;
+                float bn[32];
+                if constexpr (MET == M_L2) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        bn[4 * j] = bn_next[j].x;
+                        bn[4 * j + 1] = bn_next[j].y;
+                        bn[4 * j + 2] = bn_next[j].z;
+                        bn[4 * j + 3] = bn_next[j].w;
+                    }
+                    // the next chunk's norms (n_pad entries; the last chunk re-reads its own)
+                    const uint64_t nx = id0 + 32 < uint64_t(T) * TC_N ? id0 + 32 : id0;
+                    const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm + nx);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) bn_next[j] = __ldg(bp + j);
+                }
+                uint32_t v[32];
                 __syncwarp();
-                tc_ld32(lane_addr + s * TC_N + c * 32, v);
+                tc_ld32(tmem + (uint32_t(warp * 32) << 16) + s * TC_N + c * 32, v);
                 // chunk minimum of t_j by a tree (independent operations)
                 float m[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     if constexpr (MET == M_L2)
-                        m[j] = fminf(fmaf(-2.0f, __uint_as_float(v[j]), bnt[c * 32 + j]),
-                                     fmaf(-2.0f, __uint_as_float(v[j + 16]), bnt[c * 32 + j + 16]));
+                        m[j] = fminf(fmaf(-2.0f, __uint_as_float(v[j]), bn[j]),
+                                     fmaf(-2.0f, __uint_as_float(v[j + 16]), bn[j + 16]));
                     else
                         m[j] = fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 16]));
                 }
@@ -507,60 +480,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                     for (int j = 0; j < w; ++j) m[j] = MET == M_L2 ? fminf(m[j], m[j + w]) : fmaxf(m[j], m[j + w]);
                 const float tmin = MET == M_L2 ? m[0] : -m[0];
+                // flagged candidates of this chunk; ids at or past n are zero padding rows of the last tile
                 uint32_t mask = 0;
-                if (tmin < bound && c * 32 < nvalid) {
-                    mask = nvalid - c * 32 >= 32 ? kFull : (1u << (nvalid - c * 32)) - 1u;
+                if (tmin < thr) {
+                    if (id0 < a.n) mask = a.n - id0 >= 32 ? kFull : (1u << uint32_t(a.n - id0)) - 1u;
                     uint32_t pass = 0;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
-                        const float tj = MET == M_L2 ? fmaf(-2.0f, __uint_as_float(v[j]), bnt[c * 32 + j])
-                                                     : -__uint_as_float(v[j]);
-                        pass |= uint32_t(tj < bound) << j;
+                        const float tj =
+                            MET == M_L2 ? fmaf(-2.0f, __uint_as_float(v[j]), bn[j]) : -__uint_as_float(v[j]);
+                        pass |= uint32_t(tj < thr) << j;
                     }
                     mask &= pass;
                 }
-                return mask;
-            };
-            if (!owner) {
-                // flag this chunk against the owner's last published bound, hand the mask over
-                const uint32_t mask = flag_chunk(chunk, thr_s[tq]);
-                masks[(s * 4 + chunk) * TC_M + tq] = mask;
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(bar_mfull + 8 * (s * 4 + quarter));
-                mbar_arrive(bar_tempty + 8 * s);
-                continue;
-            }
-            uint32_t mask0 = flag_chunk(0, thr);
-            if (!__all_sync(kFull, mbar_wait(bar_mfull + 8 * (s * 4 + quarter), ph, a.err))) {
-                done = false;
-                break;
-            }
-            for (uint32_t c = 0; c < 4; ++c) {
-                uint32_t mask = c == 0 ? mask0 : masks[(s * 4 + c) * TC_M + tq];
-                if (!__any_sync(kFull, mask != 0)) continue;
-                if (c != 0) {
-                    __syncwarp();
-                    tc_ld32(lane_addr + s * TC_N + c * 32, v);
-                }
-                const uint64_t id0 = tile0 + c * 32;
-                // Queue the flagged candidates; when some thread's queue would overflow, the warp
-                // drains every queue (older ids first) and replays this chunk directly.  Admissions
-                // then cost the warp about the largest per-thread count, not one round per chunk.
+                // Queue them; when some thread's queue would overflow, the warp drains every
+                // queue (older ids first) and replays this chunk directly.  Admissions then
+                // cost the warp about the largest per-thread count, not one round per chunk.
                 if (__any_sync(kFull, qlen + __popc(mask) > TC_QUEUE)) {
                     for (uint32_t e = 0; e < qlen; ++e) {
-                        const float tj = MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tq], a.bnorm[qi[e * TC_M + tq]])
-                                                     : -qv[e * TC_M + tq];
+                        const float tj = MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tid], a.bnorm[qi[e * TC_M + tid]])
+                                                     : -qv[e * TC_M + tid];
                         if (!(tj < thr)) continue;  // the bound fell since the chunk test
                         const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
-                        thr = tk_offer(L, S, dist, qi[e * TC_M + tq]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
+                        thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
                     }
                     qlen = 0;
                     while (mask) {
                         const uint32_t j = __ffs(mask) - 1;
                         mask &= mask - 1;
                         const float acc = __uint_as_float(pick32(v, j));
-                        const float tj = MET == M_L2 ? fmaf(-2.0f, acc, bnt[c * 32 + j]) : -acc;
+                        const float tj = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
                         if (!(tj < thr)) continue;
                         const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
                         thr = tk_offer(L, S, dist, uint32_t(id0) + j) * inv_scale - (MET == M_L2 ? qn : 0.0f);
@@ -569,59 +518,53 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     while (mask) {
                         const uint32_t j = __ffs(mask) - 1;
                         mask &= mask - 1;
-                        qv[qlen * TC_M + tq] = __uint_as_float(pick32(v, j));
-                        qi[qlen * TC_M + tq] = uint32_t(id0) + j;
+                        qv[qlen * TC_M + tid] = __uint_as_float(pick32(v, j));
+                        qi[qlen * TC_M + tid] = uint32_t(id0) + j;
                         ++qlen;
                     }
                 }
             }
-            thr_s[tq] = thr;
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
             mbar_arrive(bar_tempty + 8 * s);
         }
-        if (owner) {
-            for (uint32_t e = 0; e < qlen; ++e) {
-                const float tj =
-                    MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tq], a.bnorm[qi[e * TC_M + tq]]) : -qv[e * TC_M + tq];
-                if (!(tj < thr)) continue;
-                const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
-                thr = tk_offer(L, S, dist, qi[e * TC_M + tq]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
-            }
+        for (uint32_t e = 0; e < qlen; ++e) {
+            const float tj =
+                MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tid], a.bnorm[qi[e * TC_M + tid]]) : -qv[e * TC_M + tid];
+            if (!(tj < thr)) continue;
+            const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+            thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
         }
-        // every epilogue warp is past the tile loop before the operand area is reused
-        named_barrier_sync(1, TC_EPI_WARPS * 32);
         // output sorted by (dist, id) (CompGT.cpp:107-124).  Every tile has been through the
         // MMA, so the operand area is free: the ids go there, [k][128] so that a thread's
         // entries stride 128 words, and the insertion sort runs on shared memory only.
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         uint32_t *sid = reinterpret_cast<uint32_t *>(smem);
-        if (owner && done && live && S.cnt == k) {
-            for (uint32_t l = 0; l < k; ++l) sid[l * TC_M + tq] = L.id[l];
+        if (done && live && S.cnt == k) {
+            for (uint32_t l = 0; l < k; ++l) sid[l * TC_M + tid] = L.id[l];
             for (uint32_t i = 1; i < k; ++i) {
-                const float dv = tk_d[i * TC_M + tq];
-                const uint32_t iv = sid[i * TC_M + tq];
+                const float dv = tk_d[i * TC_M + tid];
+                const uint32_t iv = sid[i * TC_M + tid];
                 int32_t j = int32_t(i) - 1;
                 while (j >= 0) {
-                    const float dj = tk_d[j * TC_M + tq];
-                    const uint32_t ij = sid[j * TC_M + tq];
+                    const float dj = tk_d[j * TC_M + tid];
+                    const uint32_t ij = sid[j * TC_M + tid];
                     if (!(dj > dv || (dj == dv && ij > iv))) break;
-                    tk_d[(j + 1) * TC_M + tq] = dj;
-                    sid[(j + 1) * TC_M + tq] = ij;
+                    tk_d[(j + 1) * TC_M + tid] = dj;
+                    sid[(j + 1) * TC_M + tid] = ij;
                     --j;
                 }
-                tk_d[(j + 1) * TC_M + tq] = dv;
-                sid[(j + 1) * TC_M + tq] = iv;
+                tk_d[(j + 1) * TC_M + tid] = dv;
+                sid[(j + 1) * TC_M + tid] = iv;
             }
             for (uint32_t l = 0; l < k; ++l) {
-                L.id[l] = sid[l * TC_M + tq];
-                a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tq]);
+                L.id[l] = sid[l * TC_M + tid];
+                a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == TC_WARP_TMA) {
+    if (warp == 4) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
     }
@@ -698,8 +641,7 @@ static bool make_map(CUtensorMap *m, void *base, uint64_t rows, uint32_t K)
 size_t gt_tc_smem(uint32_t katoms, uint32_t k, uint32_t stages)
 {
     const size_t need = 1024 + size_t(katoms) * TC_M * 128 * (1 + stages) + TC_M * TC_M + TC_QUEUE * TC_M * 8 +
-                        TC_ACC * 4 * TC_M * 4 + TC_M * 4 + TC_ACC * TC_M * 4 + TC_BARS * 8 + 16 +
-                        size_t(k) * TC_M * 4;
+                        24 * 8 + 16 + size_t(k) * TC_M * 4;
     return need > 120 * 1024 ? need : 120 * 1024;
 }
 

@@ -476,12 +476,26 @@ static nbpg_status hnsw_build_impl(nbpg_index *idx, const nbpg_hnsw_params &P, n
     return NBPG_OK;
 }
 
+// raw_queries null: hier_qsearchAll on the quantised rows.  Otherwise the index's raw rows differ
+// in size from its quantised ones and level 0 re-ranks (rerank_factor > 0) or filters (0) as
+// beam_search_rerank does over HierPointRange views (hier_beamSearch.h:41-42, 78-80).
 static nbpg_status hnsw_search_impl(nbpg_hnsw *h, const void *queries, uint32_t nq, const nbpg_search_params &P,
                                     uint32_t hbs, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
-                                    uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps)
+                                    uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps,
+                                    const void *raw_queries = nullptr, uint32_t rerank_factor = 0)
 {
     nbpg_index *idx = h->idx;
     const uint32_t L = P.L, k = P.k, R = h->R;
+    const bool rerank = raw_queries != nullptr;
+    const bool filtering = rerank && rerank_factor == 0;
+    uint32_t cs = 0;  // re-rank set per query
+    if (rerank) {
+        NBPG_CHECK_ARG(k <= 256, "re-ranked queries need k <= 256");
+        const uint32_t vf = P.visited_factor ? P.visited_factor : 8;
+        const uint64_t c64 = filtering ? uint64_t(vf) * L : std::min<uint64_t>(uint64_t(k) * rerank_factor, L);
+        NBPG_CHECK_ARG(c64 <= 4096, "the re-rank set (visited_factor * L, or min(k * rerank_factor, L)) exceeds 4096");
+        cs = uint32_t(std::max<uint64_t>(c64, k));
+    }
     NBPG_CHECK_ARG(L >= 1 && L <= 1024 && k >= 1 && k <= L, "k must be in [1, L] (the reference aborts on k > L)");
     NBPG_CHECK_ARG(k <= k_stride, "k above k_stride");
     NBPG_CHECK_ARG(hbs >= 1 && hbs <= L, "hier_beam must be in [1, L]");
@@ -583,9 +597,38 @@ static nbpg_status hnsw_search_impl(nbpg_hnsw *h, const void *queries, uint32_t 
     tgt.sp_stride = hbs;
     nbpg_search_params p = P;
     if (!p.limit) p.limit = h->cur;
-    s = search_device_impl(idx, h->scratch, dq, nq, &p, nullptr, nullptr, nullptr, 0, k_stride, d_ids, d_d, d_c, d_v,
-                           d_m, st, nullptr, &tgt);
-    if (s != NBPG_OK) return s;
+    if (!rerank) {
+        s = search_device_impl(idx, h->scratch, dq, nq, &p, nullptr, nullptr, nullptr, 0, k_stride, d_ids, d_d, d_c,
+                               d_v, d_m, st, nullptr, &tgt);
+        if (s != NBPG_OK) return s;
+    } else {
+        // the search emits each query's re-rank set (node ids), the second kernel sorts it by the raw
+        // rows of the nodes' vectors (d_root), ties by node id, first k
+        DevBuf work;
+        ReleaseOnExit release_work{{&work}};
+        const uint32_t rb = idx->raw_row_bytes;
+        const size_t cand_b = size_t(nq) * cs * 4, rq_b = size_t(nq) * rb;
+        if ((s = work.ensure(2 * cand_b + rq_b + size_t(nq) * 8 + 1024)) != NBPG_OK) return s;
+        uint8_t *w = work.as<uint8_t>();
+        auto take = [&](size_t b) { uint8_t *r0 = w; w += (b + 255) / 256 * 256; return r0; };
+        uint32_t *d_cand = reinterpret_cast<uint32_t *>(take(cand_b));
+        float *d_cd = reinterpret_cast<float *>(take(cand_b));
+        uint8_t *drq = take(rq_b);
+        uint32_t *d_cc = reinterpret_cast<uint32_t *>(take(size_t(nq) * 4));
+        uint32_t *d_fs = reinterpret_cast<uint32_t *>(take(size_t(nq) * 4));
+        NBPG_CUDA_TRY(cudaMemcpyAsync(drq, raw_queries, rq_b, cudaMemcpyHostToDevice, st));
+        SearchEmit emit;
+        emit.factor = filtering ? 0 : rerank_factor;
+        emit.visited = filtering;
+        emit.d_fs = d_fs;
+        s = search_device_impl(idx, h->scratch, dq, nq, &p, nullptr, nullptr, nullptr, 0, cs, d_cand, d_cd, d_cc, d_v,
+                               d_m, st, &emit, &tgt);
+        if (s != NBPG_OK) return s;
+        if ((s = rerank_device(idx, drq, d_cand, cs, d_cc, d_fs, nq, k, filtering, k_stride, d_ids, d_d, d_c,
+                               h->d_root, st)) != NBPG_OK)
+            return s;
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));  // the work buffer is released on return
+    }
     const size_t cnt = size_t(nq) * k_stride;
     hnsw_root_ids_kernel<<<uint32_t((cnt + 255) / 256), 256, 0, st>>>(d_ids, cnt, h->d_root);
     NBPG_CUDA_TRY(cudaGetLastError());
@@ -723,6 +766,25 @@ extern "C" nbpg_status nbpg_hnsw_search(nbpg_hnsw *h, const void *queries, uint3
     cudaSetDevice(h->idx->desc.device);
     return hnsw_search_impl(h, queries, nq, *params, hier_beam, k_stride, out_ids, out_dists, out_count, out_visited,
                             out_cmps);
+}
+
+extern "C" nbpg_status nbpg_hnsw_search_rerank(nbpg_hnsw *h, const void *queries, const void *raw_queries,
+                                               uint32_t nq, const nbpg_search_params *params, uint32_t hier_beam,
+                                               uint32_t rerank_factor, uint32_t k_stride, uint32_t *out_ids,
+                                               float *out_dists, uint32_t *out_count, uint32_t *out_visited,
+                                               uint32_t *out_cmps)
+{
+    if (!h || !params || !queries || !out_ids) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
+    if (nq == 0) return NBPG_OK;
+    nbpg_index *idx = h->idx;
+    // no raw rows, or raw rows of the quantised row size: the plain query (beamSearch.h:23-26)
+    const bool exact = idx->d_raw && idx->raw_row_bytes != idx->row_bytes;
+    if (exact && !raw_queries) { set_error("raw queries are required with raw base rows"); return NBPG_ERR_INVALID_ARG; }
+    std::lock_guard<std::mutex> g(h->mu);
+    std::lock_guard<std::mutex> gi(idx->mu);
+    cudaSetDevice(idx->desc.device);
+    return hnsw_search_impl(h, queries, nq, *params, hier_beam, k_stride, out_ids, out_dists, out_count, out_visited,
+                            out_cmps, exact ? raw_queries : nullptr, rerank_factor);
 }
 
 extern "C" nbpg_status nbpg_hnsw_destroy(nbpg_hnsw *h)

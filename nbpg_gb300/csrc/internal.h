@@ -120,6 +120,11 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
                                uint32_t *d_count, uint32_t *d_visited, uint32_t *d_cmps, cudaStream_t st,
                                const SearchEmit *emit = nullptr, const SearchTarget *tgt = nullptr);
 
+nbpg_status rerank_device(const nbpg_index *idx, const uint8_t *d_raw_queries, const uint32_t *d_cand, uint32_t cs,
+                          const uint32_t *d_cnt, const uint32_t *d_fs, uint32_t nq, uint32_t k, bool filtering,
+                          uint32_t k_stride, uint32_t *d_ids, float *d_dists, uint32_t *d_count,
+                          const uint32_t *row_map, cudaStream_t st);
+
 }  // namespace nbpg
 
 struct nbpg_index {

@@ -26,6 +26,7 @@ namespace nbpg {
 
 struct RerankArgs {
     const uint8_t *raw;        // n raw rows, raw_row bytes apart
+    const uint32_t *row_map;   // raw row of candidate id c: row_map[c] (HNSW nodes -> vectors); null = c
     uint32_t raw_row, dims;    // dims: elements (bytes for 4-bit rows)
     const uint8_t *rq;         // nq raw query rows, raw_row bytes apart
     const uint32_t *cand;      // nq x cs candidate ids from the search
@@ -82,7 +83,8 @@ __device__ void chunk_keys(const RerankArgs &a, uint32_t qi, uint32_t n, uint32_
         const uint32_t j = c0 + r * 32 + lane;
         if (j < n) {
             const uint32_t id = a.cand[size_t(qi) * a.cs + j];
-            v[r] = make_key(raw_distance<RDT, MET>(a.raw + size_t(id) * a.raw_row, q, a.dims), id);
+            const uint32_t row = a.row_map ? a.row_map[id] : id;
+            v[r] = make_key(raw_distance<RDT, MET>(a.raw + size_t(row) * a.raw_row, q, a.dims), id);
         } else {
             v[r] = kKeyMax;
         }
@@ -141,6 +143,28 @@ static void launch_rerank(int metric, const RerankArgs &a, cudaStream_t st)
 static uint32_t raw_row_bytes(uint32_t dtype, uint32_t dims)
 {
     return dtype == NBPG_F32 ? dims * 4 : dims;  // 4-bit rows: dims is bytes, as in the file headers
+}
+
+// The second kernel of a re-ranked search: exact distances of each query's candidates (nq rows of
+// cs ids, d_cnt valid each) from the index's raw rows (candidate c's row: row_map[c], or c), sorted
+// by (distance, id), first k (filtering mode: at most the query's final frontier size d_fs).
+nbpg_status rerank_device(const nbpg_index *idx, const uint8_t *d_raw_queries, const uint32_t *d_cand, uint32_t cs,
+                          const uint32_t *d_cnt, const uint32_t *d_fs, uint32_t nq, uint32_t k, bool filtering,
+                          uint32_t k_stride, uint32_t *d_ids, float *d_dists, uint32_t *d_count,
+                          const uint32_t *row_map, cudaStream_t st)
+{
+    RerankArgs ra{idx->d_raw, row_map, idx->raw_row_bytes, idx->raw_dims, d_raw_queries, d_cand, cs, d_cnt, d_fs, nq,
+                  k, filtering ? 1u : 0u, k_stride, d_ids, d_dists, d_count};
+    const int metric = int(idx->desc.metric);
+    switch (idx->raw_dtype) {
+    case NBPG_U8: launch_rerank<DT_U8>(metric, ra, st); break;
+    case NBPG_I8: launch_rerank<DT_I8>(metric, ra, st); break;
+    case NBPG_U4:
+    case NBPG_I4: launch_rerank<DT_U4>(metric, ra, st); break;
+    default: launch_rerank<DT_F32>(metric, ra, st);
+    }
+    NBPG_CUDA_TRY(cudaGetLastError());
+    return NBPG_OK;
 }
 
 }  // namespace nbpg
@@ -225,17 +249,9 @@ extern "C" nbpg_status nbpg_search_rerank(nbpg_index *idx, const void *queries, 
     s = search_device_impl(idx, idx->scratch, dq, nq, P, nullptr, nullptr, start_points, n_start, cs, d_cand, d_cd,
                            d_cc, d_v, d_m, st, &emit);
     if (s != NBPG_OK) return s;
-    RerankArgs ra{idx->d_raw, rb, idx->raw_dims, drq, d_cand, cs, d_cc, d_fs, nq, P->k, filtering ? 1u : 0u,
-                  k_stride, d_ids, d_d, d_c};
-    const int metric = int(idx->desc.metric);
-    switch (idx->raw_dtype) {
-    case NBPG_U8: launch_rerank<DT_U8>(metric, ra, st); break;
-    case NBPG_I8: launch_rerank<DT_I8>(metric, ra, st); break;
-    case NBPG_U4:
-    case NBPG_I4: launch_rerank<DT_U4>(metric, ra, st); break;
-    default: launch_rerank<DT_F32>(metric, ra, st);
-    }
-    NBPG_CUDA_TRY(cudaGetLastError());
+    if ((s = rerank_device(idx, drq, d_cand, cs, d_cc, d_fs, nq, P->k, filtering, k_stride, d_ids, d_d, d_c, nullptr,
+                           st)) != NBPG_OK)
+        return s;
     uint32_t err = 0;
     NBPG_CUDA_TRY(cudaMemcpyAsync(out_ids, d_ids, outb, cudaMemcpyDeviceToHost, st));
     if (out_dists) NBPG_CUDA_TRY(cudaMemcpyAsync(out_dists, d_d, outb, cudaMemcpyDeviceToHost, st));

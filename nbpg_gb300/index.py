@@ -346,6 +346,22 @@ class Hnsw:
                                           _p(ds, _f32p), _p(cnt), _p(vis), _p(cmps)))
         return SearchResult(ids, ds, cnt, vis, cmps)
 
+    def search_rerank(self, queries: np.ndarray, raw_queries: np.ndarray, qp: QueryParams, rerank_factor: int,
+                      hier_beam: int = 1, launch: "LaunchConfig | None" = None) -> SearchResult:
+        """hier_qsearchAll with the index's raw rows (HNSW.cpp:93-124): level 0 re-ranks the frontier
+        head (rerank_factor > 0) or filters the visited list (0) by raw distance."""
+        q = np.ascontiguousarray(queries)
+        rq = np.ascontiguousarray(raw_queries)
+        nq, k = q.shape[0], int(qp.k)
+        prm = (launch or LaunchConfig()).params(qp)
+        ids = np.empty((nq, k), np.uint32)
+        ds = np.empty((nq, k), np.float32)
+        cnt, vis, cmps = (np.empty(nq, np.uint32) for _ in range(3))
+        check(_lib.lib().nbpg_hnsw_search_rerank(self._h, q.ctypes.data, rq.ctypes.data, nq, C.byref(prm), hier_beam,
+                                                 rerank_factor, k, _p(ids), _p(ds, _f32p), _p(cnt), _p(vis),
+                                                 _p(cmps)))
+        return SearchResult(ids, ds, cnt, vis, cmps)
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.lib().nbpg_hnsw_destroy(self._h)

@@ -1338,20 +1338,29 @@ int nbpg_oracle_build_hnsw(int dtype, int metric, uint32_t dims, const void *bas
 
 // hier_qsearchAll (HNSW/base/hier_beamSearch.h:9-92): from the entry, each level above 0 runs
 // a search of beam hbs (the query's k and cut, visited cap 8L, a fresh filter sized by L) whose
-// visited list gives the next level's entry points; level 0 is the plain search of beam L
-// (visited and distance counts of that search only); the frontier's first k become vector ids.
+// visited list gives the next level's entry points; level 0 is beam_search_rerank of beam L
+// (visited and distance counts of that search only); the results become vector ids.  Without
+// raw rows (raw_base null, or raw rows of the quantised row size) level 0 returns frontier[0:k];
+// with them it re-ranks by the raw rows of the nodes' vectors as nbpg_oracle_search_rerank does
+// (rerank_factor > 0: frontier[0 : min(k * rerank_factor, fs)]; 0: filtering mode), ties broken
+// by node id before the ids become vector ids.
 // out_entry (nq x hbs, may be null): the entry points of each query's level-0 search.
-int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n,
-                            const uint32_t *graph, uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp,
-                            const void *queries, uint32_t nq, uint32_t L, uint32_t k, double cut, uint32_t hbs,
-                            uint32_t k_stride, uint32_t *out_ids, uint32_t *out_count, uint32_t *out_visited,
+static int search_hnsw_impl(int dtype, int raw_dtype, int metric, uint32_t dims, uint32_t raw_dims, const void *base,
+                            const void *raw_base, const uint32_t *graph, uint32_t R, const int64_t *pre, uint64_t cur,
+                            uint64_t sp, const void *queries, const void *raw_queries, uint32_t nq, uint32_t L,
+                            uint32_t k, uint32_t rerank_factor, double cut, uint32_t hbs, uint32_t k_stride,
+                            uint32_t *out_ids, float *out_dists, uint32_t *out_count, uint32_t *out_visited,
                             uint32_t *out_cmps, uint32_t *out_entry, int threads)
 {
     if (k == 0 || k > L || hbs == 0 || hbs > L || sp >= cur) return 1;
     if (threads <= 0) threads = omp_get_max_threads();
     const size_t row = row_bytes(dtype, dims);
+    const size_t rrb = raw_base ? (raw_dtype == 4 ? size_t(raw_dims) * 4 : row_bytes(raw_dtype, raw_dims)) : row;
+    const bool exact = raw_base && rrb != row;
     const uint8_t *B = static_cast<const uint8_t *>(base);
+    const uint8_t *RB = static_cast<const uint8_t *>(raw_base);
     const uint8_t *Q = static_cast<const uint8_t *>(queries);
+    const uint8_t *RQ = static_cast<const uint8_t *>(raw_queries);
     std::vector<uint32_t> rootv(cur), lvl(cur);
     uint32_t top = 0;
     for (uint64_t v = 0; v < cur; ++v) {
@@ -1401,16 +1410,68 @@ int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *ba
             c.reset(L, 8 * L, R);
             seed_frontier(c, spv.data(), nsp, dist_to);
             size_t cmps = beam_search(c, gv, dist_to, -1, k, cut, cur, R);
-            const size_t kk = std::min<size_t>(k, c.fs);
-            for (uint32_t j = 0; j < k_stride; ++j)
-                out_ids[size_t(i) * k_stride + j] = j < kk ? rootv[c.frontier[j].id] : 0xFFFFFFFFu;
-            if (out_count) out_count[i] = uint32_t(kk);
+            // level 0: beam_search_rerank over the nodes (HierPointRange: a node's rows are its vector's)
+            std::vector<Node> pts;
+            if (!exact) {
+                pts.assign(c.frontier.begin(), c.frontier.begin() + std::min<size_t>(k, c.fs));
+            } else {
+                const uint8_t *rq = RQ + size_t(i) * rrb;
+                auto raw_to = [&](uint32_t node) {
+                    return raw_dist(raw_dtype, metric, RB + size_t(rootv[node]) * rrb, rq, raw_dims);
+                };
+                if (rerank_factor > 0) {
+                    const size_t num_check = std::min<size_t>(size_t(k) * rerank_factor, c.fs);
+                    for (size_t j = 0; j < num_check; ++j) pts.push_back(Node{c.frontier[j].id, raw_to(c.frontier[j].id)});
+                    std::sort(pts.begin(), pts.end(), node_less);
+                    pts.resize(std::min<size_t>(k, pts.size()));
+                } else {
+                    for (size_t j = 0; j < c.vs; ++j) pts.push_back(Node{c.visited[j].id, raw_to(c.visited[j].id)});
+                    std::sort(pts.begin(), pts.end(), node_less);
+                    pts.resize(std::min<size_t>(k, std::min(c.fs, c.vs)));
+                    cmps += c.inserted;
+                }
+            }
+            for (uint32_t j = 0; j < k_stride; ++j) {
+                out_ids[size_t(i) * k_stride + j] = j < pts.size() ? rootv[pts[j].id] : 0xFFFFFFFFu;
+                if (out_dists)
+                    out_dists[size_t(i) * k_stride + j] =
+                        j < pts.size() ? pts[j].d : std::numeric_limits<float>::infinity();
+            }
+            if (out_count) out_count[i] = uint32_t(pts.size());
             if (out_visited) out_visited[i] = uint32_t(c.num_visited);
             if (out_cmps) out_cmps[i] = uint32_t(cmps);
             break;
         }
     }
     return failed ? 2 : 0;
+}
+
+int nbpg_oracle_search_hnsw(int dtype, int metric, uint32_t dims, const void *base, uint64_t n,
+                            const uint32_t *graph, uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp,
+                            const void *queries, uint32_t nq, uint32_t L, uint32_t k, double cut, uint32_t hbs,
+                            uint32_t k_stride, uint32_t *out_ids, uint32_t *out_count, uint32_t *out_visited,
+                            uint32_t *out_cmps, uint32_t *out_entry, int threads)
+{
+    (void)n;
+    return search_hnsw_impl(dtype, 0, metric, dims, 0, base, nullptr, graph, R, pre, cur, sp, queries, nullptr, nq, L,
+                            k, 0, cut, hbs, k_stride, out_ids, nullptr, out_count, out_visited, out_cmps, out_entry,
+                            threads);
+}
+
+// hier_qsearchAll with raw rows of raw_dtype (U8/I8/U4/I4 = 0..3, F32 = 4) beside the quantised
+// rows searched: level 0 re-ranks (HNSW.cpp:93-124 with --base_path and --rerank_factor).
+int nbpg_oracle_search_hnsw_rerank(int dtype, int raw_dtype, int metric, uint32_t dims, uint32_t raw_dims,
+                                   const void *base, const void *raw_base, uint64_t n, const uint32_t *graph,
+                                   uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp, const void *queries,
+                                   const void *raw_queries, uint32_t nq, uint32_t L, uint32_t k,
+                                   uint32_t rerank_factor, double cut, uint32_t hbs, uint32_t k_stride,
+                                   uint32_t *out_ids, float *out_dists, uint32_t *out_count, uint32_t *out_visited,
+                                   uint32_t *out_cmps, int threads)
+{
+    (void)n;
+    return search_hnsw_impl(dtype, raw_dtype, metric, dims, raw_dims, base, raw_base, graph, R, pre, cur, sp, queries,
+                            raw_queries, nq, L, k, rerank_factor, cut, hbs, k_stride, out_ids, out_dists, out_count,
+                            out_visited, out_cmps, nullptr, threads);
 }
 
 // Prune::maxAnglePrune (prune.h:92-154) on one candidate list as given; 3 where the

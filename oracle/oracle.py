@@ -91,6 +91,13 @@ class CpuLib:
             f("max_angle_prune").restype = C.c_int
             f("max_angle_prune").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, _u32p,
                                              _f32p, _u32p, C.c_uint32, C.c_uint32, C.c_double, C.c_double, _u32p]
+        if hasattr(self.lib, prefix + "search_hnsw_rerank"):
+            f("search_hnsw_rerank").restype = C.c_int
+            f("search_hnsw_rerank").argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
+                                                C.c_void_p, C.c_uint64, _u32p, C.c_uint32, _i64p, C.c_uint64,
+                                                C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                                C.c_uint32, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32, _u32p,
+                                                _f32p, _u32p, _u32p, _u32p, C.c_int]
         if hasattr(self.lib, prefix + "search_rerank"):
             f("search_rerank").restype = C.c_int
             f("search_rerank").argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -275,6 +282,30 @@ class CpuLib:
         if rc != 0:
             raise ValueError("search_hnsw rejected its arguments")
         return ids, cnt, vis, cm
+
+    def search_hnsw_rerank(self, dtype, metric, base, raw_base, graph, pre, sp, queries, raw_queries, L, k,
+                           rerank_factor, cut=1.35, hier_beam=1, threads=0):
+        """hier_qsearchAll with raw rows (f32, u8 or i8) beside the quantised rows: level 0 re-ranks
+        (rerank_factor > 0) or filters (0); returns (ids, dists, count, visited, cmps) (the harness,
+        like the reference, returns no distances: its dists stay +inf)."""
+        base, raw_base = np.ascontiguousarray(base), np.ascontiguousarray(raw_base)
+        queries, raw_queries = np.ascontiguousarray(queries), np.ascontiguousarray(raw_queries)
+        graph = np.ascontiguousarray(graph, dtype=np.uint32)
+        pre = np.ascontiguousarray(pre, dtype=np.int64)
+        raw_dt = {np.dtype(np.float32): 4, np.dtype(np.uint8): 0, np.dtype(np.int8): 1}[raw_base.dtype]
+        n, nq = base.shape[0], queries.shape[0]
+        ids = np.zeros((nq, k), np.uint32)
+        ds = np.full((nq, k), np.inf, np.float32)
+        cnt, vis, cm = (np.zeros(nq, np.uint32) for _ in range(3))
+        rc = self._f("search_hnsw_rerank")(DTYPES[dtype], raw_dt, METRICS[metric], base.shape[1], raw_base.shape[1],
+                                           base.ctypes.data, raw_base.ctypes.data, n, _p(graph, _u32p),
+                                           graph.shape[1] - 1, _p(pre, _i64p), graph.shape[0], sp,
+                                           queries.ctypes.data, raw_queries.ctypes.data, nq, L, k, rerank_factor,
+                                           cut, hier_beam, k, _p(ids, _u32p), _p(ds, _f32p), _p(cnt, _u32p),
+                                           _p(vis, _u32p), _p(cm, _u32p), threads)
+        if rc != 0:
+            raise ValueError("search_hnsw_rerank rejected its arguments")
+        return ids, ds, cnt, vis, cm
 
     def max_angle_prune(self, dtype, metric, base, p, ids, dists, R, PR, alpha, cos_angle=0.0):
         """Prune::maxAnglePrune (prune.h:92-154) on a candidate list; returns (ids, dists, cmps)

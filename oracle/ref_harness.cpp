@@ -280,6 +280,42 @@ int hnsw_search_t(uint32_t dims, int metric, const void *base, uint64_t n, const
     return 0;
 }
 
+// hier_qsearchAll with raw rows (Base_Points of type TR) beside the quantised ones: level 0 is
+// beam_search_rerank over HierPointRange views of both (hier_beamSearch.h:41-42, 78-80).
+template <typename T, typename TR>
+int hnsw_search_rerank_t(uint32_t dims, uint32_t raw_dims, int metric, const void *base, const void *raw_base,
+                         uint64_t n, const uint32_t *graph, uint32_t R, const int64_t *pre, uint64_t cur, uint64_t sp,
+                         const void *queries, const void *raw_queries, uint32_t nq, uint32_t L, uint32_t k,
+                         uint32_t rerank_factor, double cut, uint32_t hbs, uint32_t k_stride, uint32_t *out_ids,
+                         uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    auto Q = make_points<T>(queries, nq, dims, metric);
+    auto RB = make_points<TR>(raw_base, n, raw_dims, metric);
+    auto RQ = make_points<TR>(raw_queries, nq, raw_dims, metric);
+    auto G = make_graph(graph, cur, R);
+    HIdMapping hid(cur);
+    hid.cur_node_num = cur;
+    for (uint64_t i = 0; i < cur; ++i) hid.id_in_pre_level[i] = pre[i];
+    hid.set_sp(sp);
+    QueryStatic stats(nq);
+    uint32_t spv = uint32_t(sp);
+    std::function<std::pair<uint32_t *, uint32_t>(uint32_t)> get_sp = [&](uint32_t) {
+        return std::make_pair(&spv, uint32_t(1));
+    };
+    QueryParams QP(k, L, cut, cur, R);
+    QP.rerank_factor = rerank_factor;
+    auto res = hier_qsearchAll<uint32_t>(RQ, Q, G, hid, RB, B, stats, get_sp, QP, hbs);
+    for (uint32_t i = 0; i < nq; ++i) {
+        for (uint32_t j = 0; j < k_stride; ++j)
+            out_ids[size_t(i) * k_stride + j] = j < res[i].size() ? res[i][j] : 0xFFFFFFFFu;
+        if (out_count) out_count[i] = uint32_t(res[i].size());
+        if (out_visited) out_visited[i] = stats.visited[i];
+        if (out_cmps) out_cmps[i] = stats.distances[i];
+    }
+    return 0;
+}
+
 // Prune::maxAnglePrune (prune.h:92-154) on one candidate list, as given (no sort_candidates).
 template <typename T>
 int max_angle_prune_t(uint32_t dims, int metric, const void *base, uint64_t n, uint32_t p, uint32_t *ids,
@@ -442,6 +478,38 @@ int nbpg_ref_search_hnsw(int dtype, int metric, uint32_t dims, const void *base,
     default: return 1;
     }
 #undef NBPG_REF_HS
+}
+
+int nbpg_ref_search_hnsw_rerank(int dtype, int raw_dtype, int metric, uint32_t dims, uint32_t raw_dims,
+                                const void *base, const void *raw_base, uint64_t n, const uint32_t *graph, uint32_t R,
+                                const int64_t *pre, uint64_t cur, uint64_t sp, const void *queries,
+                                const void *raw_queries, uint32_t nq, uint32_t L, uint32_t k, uint32_t rerank_factor,
+                                double cut, uint32_t hbs, uint32_t k_stride, uint32_t *out_ids, float *out_dists,
+                                uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps, int threads)
+{
+    (void)out_dists;  // hier_qsearchAll returns ids only
+    (void)threads;
+    if (k > L || hbs == 0 || hbs > L) return 1;
+#define NBPG_REF_HR(T, TR)                                                                                          \
+    return hnsw_search_rerank_t<T, TR>(dims, raw_dims, metric, base, raw_base, n, graph, R, pre, cur, sp, queries,  \
+                                       raw_queries, nq, L, k, rerank_factor, cut, hbs, k_stride, out_ids, out_count, \
+                                       out_visited, out_cmps)
+#define NBPG_REF_HR_RAW(T)                                                                                          \
+    switch (raw_dtype) {                                                                                            \
+    case 0: NBPG_REF_HR(T, uint8_t);                                                                                \
+    case 1: NBPG_REF_HR(T, int8_t);                                                                                 \
+    case 4: NBPG_REF_HR(T, float);                                                                                  \
+    default: return 1;                                                                                              \
+    }
+    switch (dtype) {
+    case 0: NBPG_REF_HR_RAW(uint8_t);
+    case 1: NBPG_REF_HR_RAW(int8_t);
+    case 2: NBPG_REF_HR_RAW(uint4_2);
+    case 3: NBPG_REF_HR_RAW(int4_2);
+    default: return 1;
+    }
+#undef NBPG_REF_HR
+#undef NBPG_REF_HR_RAW
 }
 
 int nbpg_ref_max_angle_prune(int dtype, int metric, uint32_t dims, const void *base, uint64_t n, uint32_t p,

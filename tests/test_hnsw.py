@@ -130,3 +130,34 @@ def test_oracle_hnsw_search_matches_harness_every_row_type(oracle_lib, ref_lib, 
         b = ref_lib.search_hnsw(dtype, metric, base[:2000], g, pre, sp, q, L=L, k=k, hier_beam=hb)
         for x, y in zip(a, b):
             assert np.array_equal(x, y), (hb, L, k)
+
+
+@pytest.mark.parametrize("dtype,raw", [("u8", "f32"), ("u4", "u8"), ("i8", "f32")])
+def test_oracle_hnsw_rerank_matches_harness(oracle_lib, ref_lib, dtype, raw):
+    """hier_qsearchAll with raw rows beside the quantised ones (HNSW.cpp:93-124, --base_path with
+    --rerank_factor): level 0 re-ranks the frontier head (rerank_factor 3 and 100) or, in filtering
+    mode (0), the visited list by raw distances; ids, counts, expansions and distance counts equal
+    the reference's through the harness, with one and with three entry points per level."""
+    from conftest import dataset
+    base, q, _ = dataset(dtype, "l2", dims=16 if dtype == "u4" else 32)
+    base, n = base[:2000], 2000
+    rng = np.random.default_rng(4)
+    if raw == "f32":
+        rb = base.astype(np.float32) + rng.normal(size=base.shape).astype(np.float32) * 0.3
+        rq = q.astype(np.float32) + rng.normal(size=q.shape).astype(np.float32) * 0.3
+    else:  # 4-bit codes re-ranked by 8-bit rows of twice the width (different row size)
+        rb = np.repeat(base, 2, axis=1)
+        rq = np.repeat(q, 2, axis=1)
+    for bkw, L, k in [(dict(R=16, L=24, VL=60), 32, 10), (dict(R=16, L=20, VL=60, hier_beam=3, m_l=0.6), 40, 20)]:
+        g, pre, sp, _, _, _ = oracle_lib.build_hnsw(dtype, "l2", base, **bkw)
+        hb = bkw.get("hier_beam", 1)
+        for rf in (3, 100, 0):
+            a = oracle_lib.search_hnsw_rerank(dtype, "l2", base, rb, g, pre, sp, q, rq, L=L, k=k, rerank_factor=rf,
+                                              hier_beam=hb)
+            b = ref_lib.search_hnsw_rerank(dtype, "l2", base, rb, g, pre, sp, q, rq, L=L, k=k, rerank_factor=rf,
+                                           hier_beam=hb)
+            for i in (0, 2, 3, 4):
+                assert np.array_equal(a[i], b[i]), (hb, L, k, rf, i)
+            if rf:
+                assert not np.array_equal(a[0], oracle_lib.search_hnsw(dtype, "l2", base, g, pre, sp, q, L=L, k=k,
+                                                                       hier_beam=hb)[0])

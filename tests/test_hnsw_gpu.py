@@ -149,3 +149,65 @@ def test_search_with_repeated_start_points(gpu_lib, oracle_lib, kernel):
             ids, ds, cnt, vis, cm = oracle_lib.search("u8", "l2", b, g, q, L=L, k=k, start_points=sp)
             assert np.array_equal(r.ids, ids) and np.array_equal(r.count, cnt), (sp, L, k)
             assert np.array_equal(r.visited, vis) and np.array_equal(r.cmps, cm), (sp, L, k)
+
+
+@pytest.mark.parametrize("dtype,raw", [("u8", "f32"), ("u4", "u8"), ("i8", "f32")])
+def test_hnsw_rerank_matches_oracle(gpu_lib, oracle_lib, dtype, raw):
+    """Re-ranked HNSW queries (HNSW.cpp:93-124: --base_path raw rows, --rerank_factor): level 0 of
+    the GPU query re-ranks its frontier head (rerank_factor 3, 100) or filters its visited list (0)
+    by the raw rows of the nodes' vectors; ids, raw distances, counts, expansions and distance
+    counts equal the oracle's (which equals the reference's hier_qsearchAll through the harness)."""
+    from conftest import dataset
+    from nbpg_gb300.index import Index, QueryParams
+    base, q, _ = dataset(dtype, "l2", dims=16 if dtype == "u4" else 32)
+    base = base[:2000]
+    rng = np.random.default_rng(4)
+    if raw == "f32":
+        rb = base.astype(np.float32) + rng.normal(size=base.shape).astype(np.float32) * 0.3
+        rq = q.astype(np.float32) + rng.normal(size=q.shape).astype(np.float32) * 0.3
+    else:
+        rb, rq = np.repeat(base, 2, axis=1), np.repeat(q, 2, axis=1)
+    for bkw, L, k in [(dict(R=16, L=24, VL=60), 32, 10), (dict(R=16, L=20, VL=60, hier_beam=3, m_l=0.6), 40, 20)]:
+        hb = bkw.pop("hier_beam", 1)
+        R = bkw.pop("R")
+        idx = Index(base, dtype, "l2", max_degree=R)
+        idx.set_raw_points(rb)
+        h, _ = idx.build_hnsw(hier_beam=hb, **bkw)
+        g, pre = h.get()
+        for rf in (3, 100, 0):
+            r = h.search_rerank(q, rq, QueryParams(k=k, beamSize=L), rf, hier_beam=hb)
+            o = oracle_lib.search_hnsw_rerank(dtype, "l2", base, rb, g, pre, h.entry, q, rq, L=L, k=k,
+                                              rerank_factor=rf, hier_beam=hb)
+            assert np.array_equal(r.ids, o[0]), (hb, rf)
+            assert np.array_equal(r.dists.view(np.uint32), o[1].view(np.uint32)), (hb, rf)
+            assert np.array_equal(r.count, o[2]) and np.array_equal(r.visited, o[3]) and np.array_equal(r.cmps, o[4])
+        h.close()
+
+
+def test_hnsw_drop_in_reranks_with_raw_rows(gpu_lib, oracle_lib, tmp_path):
+    """nbpg_hnsw with --base_path/--query_path raw float rows beside the u8 rows (HNSW.cpp:255-281):
+    the query sweep runs re-ranked and reports recall over the raw rows, as the reference driver."""
+    import subprocess
+    from nbpg_gb300 import build_ext
+    z = np.load(os.path.join(G, "hnsw_default.npz"))
+    b, q = z["base"], z["queries"]
+    rng = np.random.default_rng(6)
+    rb = b.astype(np.float32) + rng.normal(size=b.shape).astype(np.float32) * 0.3
+    rq = q.astype(np.float32) + rng.normal(size=q.shape).astype(np.float32) * 0.3
+    paths = {x: str(tmp_path / x) for x in ("b.u8bin", "q.u8bin", "b.fbin", "q.fbin", "q.gt")}
+    formats.write_vectors(paths["b.u8bin"], b)
+    formats.write_vectors(paths["q.u8bin"], q)
+    formats.write_vectors(paths["b.fbin"], rb)
+    formats.write_vectors(paths["q.fbin"], rq)
+    d = ((rq[:, None, :].astype(np.float64) - rb[None, :, :]) ** 2).sum(-1)
+    gi = np.argsort(d, axis=1, kind="stable")[:, :10].astype(np.uint32)
+    formats.write_gt(paths["q.gt"], gi, np.take_along_axis(d, gi.astype(np.int64), 1).astype(np.float32))
+    ip = str(tmp_path / "idx")
+    exe = os.path.join(build_ext.OUT, "nbpg_hnsw")
+    r = subprocess.run([exe, "--quant_base_path", paths["b.u8bin"], "--index_path", ip, "--rebuild",
+                        *str(z["flags"]).split(), "--base_path", paths["b.fbin"], "--query_path", paths["q.fbin"],
+                        "--quant_query_path", paths["q.u8bin"], "--gt_path", paths["q.gt"], "--k", "10",
+                        "--rerank_factor", "4"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = [x for x in r.stdout.splitlines() if x.startswith("For 10@10 recall")]
+    assert lines and max(float(x.split("recall = ")[1].split(",")[0]) for x in lines) > 0.8
