@@ -610,7 +610,7 @@ def cpu_search_qps(base, g, q, L, threads, min_seconds=8.0):
             return reps * len(q) / el, reps
 
 
-def time_serving(idx, q, res_op, L_op, k, tuned, value, mixed_peak):
+def time_serving(idx, q, res_op, L_op, k, tuned, value, mixed_peak, gi=None, gd=None):
     """Continuous batching with Poisson arrivals (requests admitted as batch slots and the
     working-set budget free up): p50/p99 latency from each request's arrival to completion,
     at half the measured peak, at 500k QPS, and with the serving configuration's L/k mix."""
@@ -668,8 +668,15 @@ def time_serving(idx, q, res_op, L_op, k, tuned, value, mixed_peak):
     for frac, rate in [(None, 5e5)] + [(f, f * mixed_peak) for f in (0.25, 0.5, 0.75, 1.0)]:
         ids, ds, cnt, lat, el = srv.replay(qq, rate_qps=rate, Ls=Ls, ks=ks, seed=5)
         p50, p99 = np.percentile(lat, [50, 99])
-        points.append({"offered_fraction_of_peak": frac, "offered_qps": rate, "achieved_qps": len(qq) / el,
-                       "p50_ms": float(p50), "p99_ms": float(p99), "requests": len(qq)})
+        pt = {"offered_fraction_of_peak": frac, "offered_qps": rate, "achieved_qps": len(qq) / el,
+              "p50_ms": float(p50), "p99_ms": float(p99), "requests": len(qq)}
+        if gi is not None:
+            # recall@10 of the requests that asked for k >= 10 (request i is query i mod 10k)
+            from nbpg_gb300.recall import recall_at_k
+            sel = np.nonzero(ks >= 10)[0]
+            src = sel % len(q)
+            pt["recall@10_k>=10"] = round(recall_at_k(ids[sel, :10], gi[src], gd[src], 10), 4)
+        points.append(pt)
         log(f"[bench] serving mixed L/k at {rate:.3g} offered: achieved {len(qq) / el:.3g}, p50 {p50:.3f} ms, "
             f"p99 {p99:.3f} ms")
     half = [p for p in points if p["offered_fraction_of_peak"] is not None and p["offered_fraction_of_peak"] >= 0.5]
@@ -1090,7 +1097,7 @@ def main():
     serving = None
     if rank == 0:
         try:
-            serving = time_serving(idx, q, res_op, L_op, k, tuned, value, uneven["batched_qps"])
+            serving = time_serving(idx, q, res_op, L_op, k, tuned, value, uneven["batched_qps"], gi, gd)
         except Exception as exc:  # a secondary measurement: reported in the line, not fatal
             serving = {"error": str(exc)}
             log(f"[bench] serving failed: {exc}")
