@@ -354,9 +354,10 @@ nbpg_status nbpg_u8_to_u4(const uint8_t *rows, uint64_t n, uint32_t dims, uint8_
  * value returns NBPG_ERR_INVALID_ARG (the reference asserts). */
 nbpg_status nbpg_f32_to_u8(const float *rows, uint64_t n, uint32_t dims, uint8_t *out, int32_t device);
 
-/* Test hook for the failure path of the tensor engine: runs a small kNN whose base tiles
- * are withheld, so its bounded device waits (2 s) run out; returns NBPG_ERR_TIMEOUT when the
- * kernel recorded the timeout, tore down and returned with the context still usable. */
+/* TEST HOOK, not for applications: exercises the failure path of the tensor engine by running a
+ * small kNN whose base tiles are withheld, so its bounded device waits (2 s) run out; returns
+ * NBPG_ERR_TIMEOUT when the kernel recorded the timeout, tore down and returned with the context
+ * still usable.  No counterpart in the reference. */
 nbpg_status nbpg_test_gt_timeout(int32_t device);
 
 /* ---------------------------------------------------------------------------

@@ -21,7 +21,9 @@ ORACLE_SO = os.path.join(HERE, "_build", "libnbpg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnbpg_ref.so")
 REF_COMPGT = os.path.join(HERE, "_ref", "CompGT")
 REF_VAMANA = os.path.join(HERE, "_ref", "Vamana")
-# where the reference sources lie, on the machines that have them (the harness recipe reads them there)
+# where the reference sources are checked out, on the machines that have them (the harness recipe
+# reads them there); NBPG_REF_ROOT overrides the location, and a machine without them builds the
+# restatement only
 REF_ROOT = os.environ.get("NBPG_REF_ROOT", "/root/reference")
 
 DTYPES = {"u8": 0, "i8": 1, "u4": 2, "i4": 3, "f32": 4}
@@ -91,6 +93,10 @@ class CpuLib:
             f("max_angle_prune").restype = C.c_int
             f("max_angle_prune").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, C.c_uint32, _u32p,
                                              _f32p, _u32p, C.c_uint32, C.c_uint32, C.c_double, C.c_double, _u32p]
+        if hasattr(self.lib, prefix + "qsearch_all"):
+            f("qsearch_all").restype = C.c_double
+            f("qsearch_all").argtypes = [C.c_int, C.c_int, C.c_uint32, _u8p, C.c_uint64, _u32p, C.c_uint32, _u8p,
+                                         C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, C.c_uint32, _u32p, C.c_int]
         if hasattr(self.lib, prefix + "search_hnsw_rerank"):
             f("search_hnsw_rerank").restype = C.c_int
             f("search_hnsw_rerank").argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
@@ -282,6 +288,19 @@ class CpuLib:
         if rc != 0:
             raise ValueError("search_hnsw rejected its arguments")
         return ids, cnt, vis, cm
+
+    def qsearch_all(self, dtype, metric, base, graph, queries, L, k, cut=1.35, threads=0):
+        """The reference's qsearchAll itself (harness only): (ids, seconds of the call)."""
+        base, queries = np.ascontiguousarray(base), np.ascontiguousarray(queries)
+        graph = np.ascontiguousarray(graph, dtype=np.uint32)
+        nq = queries.shape[0]
+        ids = np.empty((nq, k), np.uint32)
+        sec = self._f("qsearch_all")(DTYPES[dtype], METRICS[metric], base.shape[1], base.ctypes.data, base.shape[0],
+                                     _p(graph, _u32p), graph.shape[1] - 1, queries.ctypes.data, nq, L, k, cut, k,
+                                     _p(ids, _u32p), threads)
+        if sec < 0:
+            raise ValueError("qsearch_all rejected its arguments")
+        return ids, sec
 
     def search_hnsw_rerank(self, dtype, metric, base, raw_base, graph, pre, sp, queries, raw_queries, L, k,
                            rerank_factor, cut=1.35, hier_beam=1, threads=0):

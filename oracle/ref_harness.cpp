@@ -6,6 +6,7 @@
 // without the reference sources.  Every exported function calls the reference's
 // templates directly and mirrors the signature of the matching nbpg_oracle_* call.
 #include <cstdint>
+#include <chrono>
 #include <cstring>
 #include <functional>
 #include <iostream>
@@ -76,6 +77,32 @@ int search_t(uint32_t dims, int metric, const void *base, uint64_t n, const uint
         if (out_cmps) out_cmps[i] = stats.distances[i];
     }
     return 0;
+}
+
+// The reference's own query driver, qsearchAll (beamSearch.h:257-303), as check_nn_recall.h:74-76
+// times it: one BeamSearchMemoryTable for all queries, start point {0}, uniform L and k, OpenMP over
+// the queries.  Returns the wall seconds of the call itself (scratch allocation included).
+template <typename T>
+double qsearch_all_t(uint32_t dims, int metric, const void *base, uint64_t n, const uint32_t *graph, uint32_t R,
+                     const void *queries, uint32_t nq, uint32_t L, uint32_t k, double cut, uint32_t k_stride,
+                     uint32_t *out_ids)
+{
+    auto B = make_points<T>(base, n, dims, metric);
+    auto Q = make_points<T>(queries, nq, dims, metric);
+    auto G = make_graph(graph, n, R);
+    QueryStatic stats(nq);
+    uint32_t sp0 = 0;
+    std::function<std::pair<uint32_t *, uint32_t>(uint32_t)> get_sp = [&](uint32_t) {
+        return std::make_pair(&sp0, uint32_t(1));
+    };
+    QueryParams QP(k, L, cut, n, R);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto res = qsearchAll<uint32_t>(Q, Q, G, B, B, stats, get_sp, QP);
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (uint32_t i = 0; i < nq; ++i)
+        for (uint32_t j = 0; j < k_stride; ++j)
+            out_ids[size_t(i) * k_stride + j] = j < res[i].size() ? res[i][j] : 0xFFFFFFFFu;
+    return sec;
 }
 
 // beam_search_rerank (beamSearch.h:183-247) with raw rows (Base_Points) of type TR beside
@@ -376,6 +403,19 @@ int nbpg_ref_search(int dtype, int metric, uint32_t dims, const void *base, uint
     default: return 1;
     }
 #undef NBPG_REF_SEARCH
+}
+
+double nbpg_ref_qsearch_all(int dtype, int metric, uint32_t dims, const void *base, uint64_t n,
+                            const uint32_t *graph, uint32_t R, const void *queries, uint32_t nq, uint32_t L,
+                            uint32_t k, double cut, uint32_t k_stride, uint32_t *out_ids, int threads)
+{
+    if (threads > 0) omp_set_num_threads(threads);
+    if (k > L || k > k_stride) return -1.0;
+    switch (dtype) {
+    case 0: return qsearch_all_t<uint8_t>(dims, metric, base, n, graph, R, queries, nq, L, k, cut, k_stride, out_ids);
+    case 1: return qsearch_all_t<int8_t>(dims, metric, base, n, graph, R, queries, nq, L, k, cut, k_stride, out_ids);
+    default: return -1.0;
+    }
 }
 
 int nbpg_ref_search_rerank(int dtype, int raw_dtype, int metric, uint32_t dims, uint32_t raw_dims, const void *base,
