@@ -293,7 +293,9 @@ __device__ __forceinline__ uint32_t pair_dists(const SearchArgs &a, const uint4 
         }
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
-            uint32_t acc = acc_row<DT, MET, VPL>(bv[p], pv);
+            uint32_t acc = 0;
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], pv[v], acc);
             for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
             if (lq == 0 && live[p]) {
                 ++cm;

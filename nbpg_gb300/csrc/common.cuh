@@ -164,23 +164,6 @@ __device__ __forceinline__ uint32_t acc_vec(uint4 b, uint4 q, uint32_t acc)
     return acc;
 }
 
-// The exact int32 sum over VPL 16-byte pieces of a row, in four independent accumulators (one
-// per 32-bit lane of the pieces) added at the end: a chain of VPL dependent DP4As instead of
-// 4 x VPL.  Integer sums, so the result equals the sequential one.
-template <int DT, int MET, int VPL>
-__device__ __forceinline__ uint32_t acc_row(const uint4 (&b)[VPL], const uint4 (&q)[VPL])
-{
-    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-#pragma unroll
-    for (int v = 0; v < VPL; ++v) {
-        s0 = acc_word<DT, MET>(b[v].x, q[v].x, s0);
-        s1 = acc_word<DT, MET>(b[v].y, q[v].y, s1);
-        s2 = acc_word<DT, MET>(b[v].z, q[v].z, s2);
-        s3 = acc_word<DT, MET>(b[v].w, q[v].w, s3);
-    }
-    return (s0 + s1) + (s2 + s3);
-}
-
 // int32 total -> the reference's float distance
 template <int DT, int MET>
 __device__ __forceinline__ float finish_dist(uint32_t acc)

@@ -120,7 +120,9 @@ __device__ __forceinline__ uint32_t warp_row_keys_impl(const SearchArgs &a, cons
 #pragma unroll
         for (int p = 0; p < P; ++p) {
             if (r0 + p * rows_per >= cnt) break;  // warp-uniform: no rows left in this pass
-            uint32_t acc = acc_row<DT, MET, VPL>(bv[p], qv);
+            uint32_t acc = 0;
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) acc = acc_vec<DT, MET>(bv[p][v], qv[v], acc);
             for (uint32_t o = lpr >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
             const uint32_t r = r0 + p * rows_per + grp;
             const uint64_t key = make_dist_key<MET>(finish_dist<DT, MET>(acc), id[p]);
@@ -405,11 +407,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
         const uint32_t ne = deg < a.degree_limit ? deg : a.degree_limit;
         adj += 1 + ne;
 
-        // visited filter, in neighbour order (beamSearch.h:71-83); the slots of every chunk are
-        // hashed first, off the chain of dependent shared-memory probes that follows
-        uint32_t slv[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) slv[c] = uint32_t(c * 32 + lane) < ne ? filter_slot(nbv[c], smask) : 0xFFFFFFFFu;
+        // visited filter, in neighbour order (beamSearch.h:71-83)
         uint32_t nf = 0;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -417,7 +415,7 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             const uint32_t i = c * 32 + lane;
             const bool act = i < ne;
             const uint32_t nb = nbv[c];
-            const uint32_t sl = slv[c];
+            const uint32_t sl = act ? filter_slot(nb, smask) : 0xFFFFFFFFu;
             const unsigned peers = __match_any_sync(kFull, sl);
             const unsigned earlier = peers & lanemask_lt();
             const int src = earlier ? 31 - __clz(earlier) : lane;
