@@ -113,6 +113,14 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+// plain bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on bar
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
 // K-major operand, 128-byte swizzle: rows of 128 B, 8-row groups 1024 B apart
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
 {
@@ -322,9 +330,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint8_t *sA = smem;
     uint8_t *sB = smem + tile_bytes;                                        // a.stages tiles
     uint8_t *win = sB + a.stages * tile_bytes;                              // [128][128] tree nodes
-    float *qv = reinterpret_cast<float *>(win + TC_M * TC_M);               // [TC_QUEUE][128] queued accumulators
+    float *qv = reinterpret_cast<float *>(win + TC_M * TC_M);               // [TC_QUEUE][128] queued t_j values
     uint32_t *qi = reinterpret_cast<uint32_t *>(qv + TC_QUEUE * TC_M);        // [TC_QUEUE][128] queued ids
-    uint64_t *bars = reinterpret_cast<uint64_t *>(qi + TC_QUEUE * TC_M);
+    float *nring = reinterpret_cast<float *>(qi + TC_QUEUE * TC_M);       // [TC_ACC][128] base norms
+    uint64_t *bars = reinterpret_cast<uint64_t *>(nring + TC_ACC * TC_M);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 24);
     float *tk_d = reinterpret_cast<float *>(tmem_slot + 4);                 // [k][128]
 
@@ -334,7 +343,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                    bar_tfull = smem_u32(bars + 2 * TC_MAX_STAGES),
                    bar_tempty = smem_u32(bars + 2 * TC_MAX_STAGES + TC_ACC),
                    bar_a = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC),
-                   bar_done = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 1);
+                   bar_done = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 1),
+                   bar_nfull = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 2);  // TC_ACC barriers
     if (tid == 0) {
         for (uint32_t s = 0; s < a.stages; ++s) {
             mbar_init(bar_full + 8 * s, 1);
@@ -344,6 +354,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(bar_tfull + 8 * s, 1);
             mbar_init(bar_tempty + 8 * s, TC_M);
         }
+        for (uint32_t s = 0; s < TC_ACC; ++s) mbar_init(bar_nfull + 8 * s, 1);
         mbar_init(bar_a, 1);
         mbar_init(bar_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -385,11 +396,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0) {
             const uint32_t idesc = tc_idesc(TC_M, TC_N);
             bool ok = mbar_wait(bar_a, 0, a.err);
-            uint32_t s = 0, ph = 0;
+            uint32_t s = 0, ph = 0, nissued = 0;
             for (uint32_t t = 0; ok && t < T; ++t) {
                 const uint32_t ts = t % TC_ACC, tph = (t / TC_ACC) & 1;  // TMEM accumulator
                 if (!mbar_wait(bar_full + 8 * s, ph, a.err)) break;
                 if (!mbar_wait(bar_tempty + 8 * ts, tph ^ 1, a.err)) break;
+                if constexpr (MET == M_L2) {
+                    // the tile's base norms beside its accumulator (the epilogue has released both),
+                    // so the epilogue reads them from shared memory with the copy long landed
+                    mbar_expect_tx(bar_nfull + 8 * ts, TC_N * 4);
+                    bulk_load(smem_u32(nring + ts * TC_M), a.bnorm + size_t(t) * TC_N, TC_N * 4, bar_nfull + 8 * ts);
+                    ++nissued;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t d = tmem + ts * TC_N;
                 const uint32_t aB = smem_u32(sA), bB = smem_u32(sB + s * tile_bytes);
@@ -401,9 +419,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 tc_commit(bar_tfull + 8 * ts);   // accumulator ts ready
                 if (++s == a.stages) { s = 0; ph ^= 1; }
             }
-            // all issued MMAs complete before teardown
+            // all issued MMAs complete, and the last norm copies landed, before teardown
             tc_commit(bar_done);
             mbar_wait(bar_done, 0, a.err);
+            for (uint32_t t = nissued > TC_ACC ? nissued - TC_ACC : 0; t < nissued; ++t)
+                mbar_wait(bar_nfull + 8 * (t % TC_ACC), (t / TC_ACC) & 1, a.err);
         }
         __syncwarp();
     } else {
@@ -430,16 +450,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // |q|^2 (L2).  A candidate can survive only if t_j < thr = B / scale - |q|^2.
         // Until the list holds k entries everything passes; padding queries never do.
         float thr = live ? kInf : -kInf;
-        float4 bn_next[8];
-        if constexpr (MET == M_L2) {
-            const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) bn_next[j] = __ldg(bp + j);
-        }
         for (uint32_t t = 0; t < T; ++t) {
             const uint32_t s = t % TC_ACC, ph = (t / TC_ACC) & 1;
             // warp-uniform wait so that the warp stays converged for tcgen05.ld
-            const bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
+            bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
+            if constexpr (MET == M_L2) ok = ok && __all_sync(kFull, mbar_wait(bar_nfull + 8 * s, ph, a.err));
             if (!ok) {
                 done = false;
                 break;
@@ -449,18 +464,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint64_t id0 = uint64_t(t) * TC_N + c * 32;
                 float bn[32];
                 if constexpr (MET == M_L2) {
+                    // this chunk's base norms from the tile's staged copy (one broadcast read per 16 B)
+                    const float4 *bp = reinterpret_cast<const float4 *>(nring + s * TC_M + c * 32);
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        bn[4 * j] = bn_next[j].x;
-                        bn[4 * j + 1] = bn_next[j].y;
-                        bn[4 * j + 2] = bn_next[j].z;
-                        bn[4 * j + 3] = bn_next[j].w;
+                        const float4 x = bp[j];
+                        bn[4 * j] = x.x;
+                        bn[4 * j + 1] = x.y;
+                        bn[4 * j + 2] = x.z;
+                        bn[4 * j + 3] = x.w;
                     }
-                    // the next chunk's norms (n_pad entries; the last chunk re-reads its own)
-                    const uint64_t nx = id0 + 32 < uint64_t(T) * TC_N ? id0 + 32 : id0;
-                    const float4 *bp = reinterpret_cast<const float4 *>(a.bnorm + nx);
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) bn_next[j] = __ldg(bp + j);
                 }
                 uint32_t v[32];
                 __syncwarp();
@@ -498,8 +511,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 // cost the warp about the largest per-thread count, not one round per chunk.
                 if (__any_sync(kFull, qlen + __popc(mask) > TC_QUEUE)) {
                     for (uint32_t e = 0; e < qlen; ++e) {
-                        const float tj = MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tid], a.bnorm[qi[e * TC_M + tid]])
-                                                     : -qv[e * TC_M + tid];
+                        const float tj = qv[e * TC_M + tid];
                         if (!(tj < thr)) continue;  // the bound fell since the chunk test
                         const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
                         thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
@@ -518,7 +530,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     while (mask) {
                         const uint32_t j = __ffs(mask) - 1;
                         mask &= mask - 1;
-                        qv[qlen * TC_M + tid] = __uint_as_float(pick32(v, j));
+                        const float acc = __uint_as_float(pick32(v, j));
+                        qv[qlen * TC_M + tid] = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
                         qi[qlen * TC_M + tid] = uint32_t(id0) + j;
                         ++qlen;
                     }
@@ -528,8 +541,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_arrive(bar_tempty + 8 * s);
         }
         for (uint32_t e = 0; e < qlen; ++e) {
-            const float tj =
-                MET == M_L2 ? fmaf(-2.0f, qv[e * TC_M + tid], a.bnorm[qi[e * TC_M + tid]]) : -qv[e * TC_M + tid];
+            const float tj = qv[e * TC_M + tid];
             if (!(tj < thr)) continue;
             const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
             thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
@@ -641,7 +653,7 @@ static bool make_map(CUtensorMap *m, void *base, uint64_t rows, uint32_t K)
 size_t gt_tc_smem(uint32_t katoms, uint32_t k, uint32_t stages)
 {
     const size_t need = 1024 + size_t(katoms) * TC_M * 128 * (1 + stages) + TC_M * TC_M + TC_QUEUE * TC_M * 8 +
-                        24 * 8 + 16 + size_t(k) * TC_M * 4;
+                        TC_ACC * TC_M * 4 + 24 * 8 + 16 + size_t(k) * TC_M * 4;
     return need > 120 * 1024 ? need : 120 * 1024;
 }
 
