@@ -200,11 +200,14 @@ nbpg_status nbpg_search_graph_destroy(nbpg_search_graph *g);
  * nbpg_search_device's.  The per-call scratch (work counters, queries re-run in exact
  * mode, start points) is a fixed static device array of about 260 KB held by every
  * device that loads the library until exit.  Limits: nq <= 65536, n_start <= 256,
- * L <= 181 (visited filter in shared memory), no per-query L/k arrays.  The first call
- * on a device looks up the array's address (cudaGetSymbolAddress): make that first
- * call before any stream capture.  All calls share the array, so calls that overlap
- * on the GPU race and must be serialised by the caller.  Runs on the current device
- * and on `stream` (a cudaStream_t; NULL = the legacy default stream). */
+ * L <= 181 (visited filter in shared memory), no per-query L/k arrays, strict mode only
+ * (FAST returns NBPG_ERR_UNSUPPORTED).  The first call on a device looks up the array's
+ * address (cudaGetSymbolAddress): make that first call before any stream capture; the
+ * address is looked up again when the device's context has changed (after
+ * cudaDeviceReset the array can move).  All calls share the array, so calls that overlap
+ * on the GPU race and must be serialised by the caller.  warps_per_cta = 0 picks the CTA
+ * size with the most resident warps per SM, as nbpg_search_device does.  Runs on the
+ * current device and on `stream` (a cudaStream_t; NULL = the legacy default stream). */
 nbpg_status nbpg_search_noalloc(uint32_t dtype, uint32_t metric, uint32_t dims, uint64_t n, uint32_t max_degree,
                                 const void *d_points, const uint32_t *d_graph, const void *d_queries, uint32_t nq,
                                 const nbpg_search_params *params, const uint32_t *start_points, uint32_t n_start,
