@@ -20,7 +20,12 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", f"-I{INCLUDE}"]
+# host code: no floating-point contraction, so that float expressions round as written on every host
+# (GCC contracts a * b + c into an FMA by default where the CPU has one, as the Grace host does; the
+# popularity-driven alpha of the build, minAlpha + cof * (maxAlpha - minAlpha), would then round
+# differently from the restatement it is checked against)
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off",
+         f"-I{INCLUDE}"]
 
 
 def _newest_dep() -> float:
@@ -78,7 +83,7 @@ def _build_cli() -> None:
                 LIB]
         if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
             continue
-        cmd = [cxx, "-O2", "-std=c++17", *defs, srcp, f"-I{INCLUDE}", f"-L{OUT}", "-lnbpg_gb300",
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", *defs, srcp, f"-I{INCLUDE}", f"-L{OUT}", "-lnbpg_gb300",
                "-Wl,-rpath,$ORIGIN", "-o", out]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
