@@ -266,6 +266,45 @@ __device__ __forceinline__ uint32_t sort_unique_minus(uint64_t *cand, uint32_t c
     return outc;
 }
 
+// sort_unique_minus fused with the candidates' side of the union: each kept candidate's rank in
+// the frontier comes from the same search that rejects frontier repeats, and the candidate is
+// placed at once at (its index among the kept) + (that rank) in the next frontier frn / fln when
+// that position is below L (the union is truncated to L).  Returns the count kept; cand[0, count)
+// holds them sorted, for the frontier's side of the union.
+__device__ __forceinline__ uint32_t sort_unique_place(uint64_t *cand, uint32_t cs, const uint64_t *fr, uint32_t fs,
+                                                      uint32_t L, uint64_t *frn, uint8_t *fln, int lane)
+{
+    sort_keys(cand, cs, lane);
+    uint32_t outc = 0;
+    uint64_t carry = kKeyMax;  // last element of the previous chunk, as read before compaction
+    for (uint32_t base = 0; base < cs; base += 32) {
+        const uint32_t i = base + lane;
+        const uint64_t v = i < cs ? cand[i] : kKeyMax;
+        uint64_t prev = __shfl_up_sync(kFull, v, 1);
+        if (lane == 0) prev = carry;
+        carry = __shfl_sync(kFull, v, 31);
+        uint32_t p = 0;
+        bool keep = i < cs && v != prev;
+        if (keep) {
+            p = lower_count(fr, fs, v);
+            keep = !(p < fs && fr[p] == v);
+        }
+        const unsigned m = __ballot_sync(kFull, keep);
+        __syncwarp();
+        const uint32_t j = outc + __popc(m & lanemask_lt());
+        if (keep) {
+            cand[j] = v;
+            if (j + p < L) {
+                frn[j + p] = v;
+                fln[j + p] = 0;
+            }
+        }
+        outc += __popc(m);
+        __syncwarp();
+    }
+    return outc;
+}
+
 // first index i in sorted s[0..n) with s[i] > key (std::upper_bound)
 __device__ __forceinline__ uint32_t warp_upper_bound(const uint64_t *s, uint32_t n, uint64_t key, int lane)
 {
@@ -492,11 +531,13 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             continue;
         }
 
-        // sort + unique candidates, set_union with the frontier, truncate to L (beamSearch.h:128-138)
-        const uint32_t cu = sort_unique_minus(cand, cst, frb, fs, lane);
+        // sort + unique candidates, set_union with the frontier, truncate to L (beamSearch.h:128-138):
+        // the candidates take their places in the next frontier during the dedupe, the frontier's
+        // entries theirs after it (positions below n0 = min(fs + cu, L) are exactly those below L)
         const int nb2 = b ^ 1;
         uint64_t *const frn = nb2 ? fr1 : fr0;
         uint8_t *const fln = nb2 ? fl1 : fl0;
+        const uint32_t cu = sort_unique_place(cand, cst, frb, fs, L, frn, fln, lane);
         const uint32_t U = fs + cu;
         const uint32_t n0 = U < L ? U : L;
         for (uint32_t i = lane; i < fs; i += 32) {
@@ -505,14 +546,6 @@ __device__ SearchState search_core(const SearchArgs &a, const uint8_t *qrow_byte
             if (p < n0) {
                 frn[p] = key;
                 fln[p] = flb[i];
-            }
-        }
-        for (uint32_t j = lane; j < cu; j += 32) {
-            const uint64_t key = cand[j];
-            const uint32_t p = j + lower_count(frb, fs, key);
-            if (p < n0) {
-                frn[p] = key;
-                fln[p] = 0;
             }
         }
         __syncwarp();
