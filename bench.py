@@ -648,7 +648,13 @@ def time_serving(idx, q, res_op, L_op, k, tuned, value, mixed_peak, gi=None, gd=
                                                              memory_budget_bytes=1 << 30), None),
                ("budget 1 GB, batch 2048, 8 in flight, FAST expand 2, 4096-slot hash",
                 dict(max_batch=2048, max_in_flight=8, memory_budget_bytes=1 << 30),
-                LaunchConfig(mode="fast", expand=2, hash_slots=4096))]
+                LaunchConfig(mode="fast", expand=2, hash_slots=4096)),
+               ("budget 1 GB, batch 1024, 16 in flight, FAST expand 2, 4096-slot hash",
+                dict(max_batch=1024, max_in_flight=16, memory_budget_bytes=1 << 30),
+                LaunchConfig(mode="fast", expand=2, hash_slots=4096)),
+               ("budget 1 GB, batch 1024, 8 in flight, FAST expand 4, 4096-slot hash",
+                dict(max_batch=1024, max_in_flight=8, memory_budget_bytes=1 << 30),
+                LaunchConfig(mode="fast", expand=4, hash_slots=4096))]
     tried = []
     for name, kw, lc in configs:
         srv = Server(idx, max_L=256, max_k=100, qp=qpm, launch=lc, **kw)
