@@ -161,7 +161,7 @@ __device__ void search_fast_query(const SearchArgs &a, uint32_t qi, uint8_t *slo
         uint8_t *const fln = nb2 ? fl1 : fl0;
         if (cst) {
             // sort + unique, union with the frontier truncated to L, cut rule (beamSearch.h:128-149)
-            const uint32_t cu = sort_unique_minus(cand, cst, frb, fs, lane);
+            const uint32_t cu = sort_unique_place(cand, cst, frb, fs, L, frn, fln, lane);
             const uint32_t U = fs + cu;
             const uint32_t n0 = U < L ? U : L;
             for (uint32_t i = lane; i < fs; i += 32) {
@@ -170,14 +170,6 @@ __device__ void search_fast_query(const SearchArgs &a, uint32_t qi, uint8_t *slo
                 if (p < n0) {
                     frn[p] = key;
                     fln[p] = flb[i];
-                }
-            }
-            for (uint32_t j = lane; j < cu; j += 32) {
-                const uint64_t key = cand[j];
-                const uint32_t p = j + lower_count(frb, fs, key);
-                if (p < n0) {
-                    frn[p] = key;
-                    fln[p] = 0;
                 }
             }
             __syncwarp();

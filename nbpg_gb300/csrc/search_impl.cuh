@@ -241,36 +241,12 @@ __device__ __forceinline__ bool unvisited_multi(const uint64_t *fr, uint32_t i, 
     return r >= c;
 }
 
-// Sort the candidates, drop repeats (std::unique after the sort, beamSearch.h:128-130)
-// and drop those already in the frontier (set_union keeps the frontier's copy,
-// beamSearch.h:132-135).  Returns the count of what is left, sorted in cand[].
-__device__ __forceinline__ uint32_t sort_unique_minus(uint64_t *cand, uint32_t cs, const uint64_t *fr, uint32_t fs,
-                                                      int lane)
-{
-    sort_keys(cand, cs, lane);
-    uint32_t outc = 0;
-    uint64_t carry = kKeyMax;  // last element of the previous chunk, as read before compaction
-    for (uint32_t base = 0; base < cs; base += 32) {
-        const uint32_t i = base + lane;
-        const uint64_t v = i < cs ? cand[i] : kKeyMax;
-        uint64_t prev = __shfl_up_sync(kFull, v, 1);
-        if (lane == 0) prev = carry;
-        carry = __shfl_sync(kFull, v, 31);
-        const bool keep = i < cs && v != prev && !contains(fr, fs, v);
-        const unsigned m = __ballot_sync(kFull, keep);
-        __syncwarp();
-        if (keep) cand[outc + __popc(m & lanemask_lt())] = v;
-        outc += __popc(m);
-        __syncwarp();
-    }
-    return outc;
-}
-
-// sort_unique_minus fused with the candidates' side of the union: each kept candidate's rank in
-// the frontier comes from the same search that rejects frontier repeats, and the candidate is
-// placed at once at (its index among the kept) + (that rank) in the next frontier frn / fln when
-// that position is below L (the union is truncated to L).  Returns the count kept; cand[0, count)
-// holds them sorted, for the frontier's side of the union.
+// Sort the candidates, drop repeats (std::unique after the sort, beamSearch.h:128-130) and drop
+// those already in the frontier (set_union keeps the frontier's copy, beamSearch.h:132-135), and
+// place the candidates' side of the union at once: a kept candidate's rank in the frontier comes
+// from the same search that rejects frontier repeats, and it goes to (its index among the kept) +
+// (that rank) in the next frontier frn / fln when that position is below L (the union is truncated
+// to L).  Returns the count kept; cand[0, count) holds them sorted, for the frontier's side.
 __device__ __forceinline__ uint32_t sort_unique_place(uint64_t *cand, uint32_t cs, const uint64_t *fr, uint32_t fs,
                                                       uint32_t L, uint64_t *frn, uint8_t *fln, int lane)
 {
