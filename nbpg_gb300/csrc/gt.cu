@@ -283,7 +283,7 @@ bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_opti
 nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t stride, const uint8_t *d_base,
                          uint64_t n, const uint8_t *d_q, uint32_t nq, uint32_t k, uint32_t mode, uint32_t *d_ids,
                          float *d_dists, void *ws, cudaStream_t st, bool withhold = false);
-size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq);
+size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq, uint32_t k);
 
 nbpg_status gt_device(uint32_t dtype, uint32_t metric, const GtArgs &a, cudaStream_t st, size_t smem_optin)
 {
@@ -407,7 +407,7 @@ extern "C" nbpg_status nbpg_gt_workspace_size(uint32_t dtype, uint32_t dims, uin
     uint32_t eng = 0;
     const nbpg_status s = resolve_engine(dtype, dims, k, engine, &eng);
     if (s != NBPG_OK) return s;
-    *bytes = eng == NBPG_GT_TENSOR ? gt_tc_workspace(dtype, dims, n, nq) : 0;
+    *bytes = eng == NBPG_GT_TENSOR ? gt_tc_workspace(dtype, dims, n, nq, k) : 0;
     return NBPG_OK;
 }
 
@@ -430,7 +430,7 @@ extern "C" nbpg_status nbpg_gt_device(uint32_t dtype, uint32_t metric, uint32_t 
     if (s != NBPG_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (eng == NBPG_GT_TENSOR) {
-        const size_t need = gt_tc_workspace(dtype, dims, n, nq);
+        const size_t need = gt_tc_workspace(dtype, dims, n, nq, k);
         NBPG_CHECK_ARG(!d_workspace || workspace_bytes >= need, "workspace smaller than nbpg_gt_workspace_size");
         return gt_tc_device(dtype, metric, dims, row_stride, static_cast<const uint8_t *>(d_base), n,
                             static_cast<const uint8_t *>(d_queries), nq, k, mode, d_ids, d_dists, d_workspace, st);

@@ -45,13 +45,68 @@ struct TcArgs {
     uint64_t n;
     uint32_t nq, k, exact, scale;  // scale: 1, or 256 for 4-bit codes
     uint32_t katoms;               // K / 64
-    uint32_t ntiles;
+    uint32_t T;                    // base tiles of one full scan
     uint32_t stages;               // depth of the base-tile ring
     uint32_t withhold;             // test hook: the producer issues no base tiles
-    uint32_t *out_ids;
+    uint32_t *out_ids;             // slot-order lists after the scan, (dist, id)-sorted after the merge
     float *out_dists;
     uint32_t *err;
+    // work split: the (query tile, base tile) steps of all listed query tiles, in order, cut
+    // into consecutive ranges [cuts[c], cuts[c + 1]), one per CTA
+    const uint64_t *cuts;
+    const uint2 *conts;         // per list entry: first CTA and count of the ranges that start inside its scan
+    const uint32_t *tile_list;  // query tile of each list entry, or null (entry i = query tile i)
+    uint4 *state;               // per query after its tile's first segment: cnt, toppos, topdist, list max
+    float *bound;               // per query: the survivor bound (t_j space) its first segment publishes
+    uint2 *lists;               // [CTA][cap][128] (dist bits, id): a CTA's candidates of a segment that
+    uint32_t *list_n;           // [CTA][128]      starts inside a query tile's scan, and their count
+    uint32_t cap;
+    uint32_t *ovf;              // per list entry: a continuation list overflowed (rerun unsplit)
 };
+
+// A CTA's range [pb, pe) in segments, one per query tile it touches: the scans that start in
+// the range (at fb, fb + T, ...) are processed first, the one the range joins in mid-scan (if
+// pb is inside a scan) last, so that by then that scan's first segment, in an earlier CTA, has
+// published its bound.
+struct TcRange {
+    uint64_t pb, pe, fb;
+    uint32_t npre, nseg;
+};
+
+struct TcSeg {
+    uint32_t li, b0, b1;  // list entry, base tiles [b0, b1)
+};
+
+__host__ __device__ __forceinline__ TcRange tc_range(uint64_t pb, uint64_t pe, uint32_t T)
+{
+    TcRange r;
+    r.pb = pb;
+    r.pe = pe;
+    r.fb = (pb + T - 1) / T * T;
+    r.npre = r.fb < pe ? uint32_t((pe - r.fb + T - 1) / T) : 0u;
+    r.nseg = r.npre + (pb < r.fb && pb < pe ? 1u : 0u);
+    return r;
+}
+
+__host__ __device__ __forceinline__ TcSeg tc_seg_at(const TcRange &r, uint32_t i, uint32_t T)
+{
+    uint64_t s, e;
+    if (i < r.npre) {
+        s = r.fb + uint64_t(i) * T;
+        e = s + T < r.pe ? s + T : r.pe;
+    } else {
+        s = r.pb;
+        e = r.fb < r.pe ? r.fb : r.pe;
+    }
+    TcSeg g;
+    g.li = uint32_t(s / T);
+    g.b0 = uint32_t(s % T);
+    g.b1 = uint32_t(g.b0 + (e - s));
+    return g;
+}
+
+__device__ __forceinline__ float ld_volatile(const float *p) { return *reinterpret_cast<const volatile float *>(p); }
+__device__ __forceinline__ void st_volatile(float *p, float v) { *reinterpret_cast<volatile float *>(p) = v; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
@@ -180,13 +235,58 @@ struct TkList {
 };
 
 // Running state of one query's list.  CompGT: CompGT's toppos/topdist and the list
-// maximum.  Exact: top = slot of the largest key, topdist = its distance.
+// maximum, and per group of 16 slots (slots 1.. k-1) its largest distance and that value's
+// first slot, in registers.  Exact: top = slot of the largest key, topdist = its distance.
+constexpr uint32_t TK_GROUP = 16;
+constexpr uint32_t TK_GROUPS = 7;  // (100 - 1 + 15) / 16
 struct TkState {
     uint32_t cnt, toppos;
     float topdist, lmax;
+    float gm[TK_GROUPS];
+    uint32_t ga[TK_GROUPS];
 };
 
 constexpr uint32_t kNoSlot = 0xFF;
+
+// Largest distance of group g (slots 1 + 16 g .. min(k, 1 + 16 g + 16) - 1) and its first slot:
+// sixteen independent shared-memory reads and a left-to-right scan with strict >.
+__device__ __forceinline__ void tk_group_scan(const TkList &L, uint32_t g, float &m, uint32_t &arg)
+{
+    const uint32_t s0 = 1 + g * TK_GROUP;
+    float v[TK_GROUP];
+#pragma unroll
+    for (uint32_t j = 0; j < TK_GROUP; ++j) v[j] = s0 + j < L.k ? L.d[(s0 + j) * TC_M + L.tid] : -3.402823466e38f;
+    m = v[0];
+    arg = s0;
+#pragma unroll
+    for (uint32_t j = 1; j < TK_GROUP; ++j)
+        if (v[j] > m) {
+            m = v[j];
+            arg = s0 + j;
+        }
+}
+
+// The first maximum over slots 1..k-1 from the group maxima (groups in slot order, strict >)
+__device__ __forceinline__ void tk_groups_max(const TkState &S, uint32_t ng, float &m, uint32_t &arg)
+{
+    m = -3.402823466e38f;
+    arg = kNoSlot;
+#pragma unroll
+    for (uint32_t g = 0; g < TK_GROUPS; ++g)
+        if (g < ng && (arg == kNoSlot || S.gm[g] > m)) {
+            m = S.gm[g];
+            arg = S.ga[g];
+        }
+}
+
+__device__ __forceinline__ void tk_groups_build(const TkList &L, TkState &S)
+{
+    const uint32_t ng = (L.k - 1 + TK_GROUP - 1) / TK_GROUP;
+#pragma unroll
+    for (uint32_t g = 0; g < TK_GROUPS; ++g)
+        if (g < ng) tk_group_scan(L, g, S.gm[g], S.ga[g]);
+}
+
 
 __device__ __forceinline__ uint32_t tt_node(const TkList &L, uint32_t x)
 {
@@ -268,20 +368,35 @@ __device__ __forceinline__ float tk_offer(const TkList &L, TkState &S, float dis
     const float kInf = __int_as_float(0x7f800000);
     if (!L.exact) {
         // CompGT.cpp:71-95
+        const uint32_t ng = (L.k - 1 + TK_GROUP - 1) / TK_GROUP;
         if (S.cnt < L.k) {
             if (dist > S.topdist) { S.topdist = dist; S.toppos = S.cnt; }
             S.lmax = fmaxf(S.lmax, dist);
             L.d[S.cnt * TC_M + t] = dist;
             L.id[S.cnt] = id;
-            if (++S.cnt == L.k) tt_build(L);
+            if (++S.cnt == L.k) tk_groups_build(L, S);
         } else if (dist < S.topdist) {
             // overwrite toppos; the rescan over slots 1..k-1 starts from topk[0] read before the write
             const float old0 = L.d[t];
             const uint32_t p = S.toppos;
             L.d[p * TC_M + t] = dist;
             L.id[p] = id;
-            const uint32_t r = p >= 1 ? tt_update(L, p, dist, id) : tt_root(L);
-            const float m1 = r == kNoSlot ? -kInf : L.d[r * TC_M + t];
+            if (p >= 1) {
+                const uint32_t gp = (p - 1) / TK_GROUP;
+                float m;
+                uint32_t arg;
+                tk_group_scan(L, gp, m, arg);
+#pragma unroll
+                for (uint32_t g = 0; g < TK_GROUPS; ++g)
+                    if (g == gp) {
+                        S.gm[g] = m;
+                        S.ga[g] = arg;
+                    }
+            }
+            float m1;
+            uint32_t r;
+            tk_groups_max(S, ng, m1, r);
+            if (r == kNoSlot) m1 = -kInf;
             if (m1 > old0) { S.topdist = m1; S.toppos = r; }
             else { S.topdist = old0; S.toppos = 0; }
             S.lmax = fmaxf(p == 0 ? dist : old0, m1);
@@ -344,7 +459,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                    bar_tempty = smem_u32(bars + 2 * TC_MAX_STAGES + TC_ACC),
                    bar_a = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC),
                    bar_done = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 1),
-                   bar_nfull = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 2);  // TC_ACC barriers
+                   bar_nfull = smem_u32(bars + 2 * TC_MAX_STAGES + 2 * TC_ACC + 2),  // TC_ACC barriers
+                   bar_aempty = smem_u32(bars + 2 * TC_MAX_STAGES + 3 * TC_ACC + 2);
     if (tid == 0) {
         for (uint32_t s = 0; s < a.stages; ++s) {
             mbar_init(bar_full + 8 * s, 1);
@@ -356,6 +472,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         for (uint32_t s = 0; s < TC_ACC; ++s) mbar_init(bar_nfull + 8 * s, 1);
         mbar_init(bar_a, 1);
+        mbar_init(bar_aempty, 1);
         mbar_init(bar_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -367,27 +484,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t q0 = blockIdx.x * TC_M;
-    const uint32_t T = a.ntiles;
+    const uint32_t T = a.T;
+    const TcRange rg = tc_range(a.cuts[blockIdx.x], a.cuts[blockIdx.x + 1], T);
 
     if (warp == 4) {
         if (lane == 0) {
-            // queries once, then base tiles through the ring
-            mbar_expect_tx(bar_a, tile_bytes);
-            for (uint32_t c = 0; c < a.katoms; ++c)
-                tma_load_2d(smem_u32(sA + c * atom_bytes), &tmA, int32_t(c * TC_KATOM), int32_t(q0), bar_a);
-            uint32_t issued = 0, s = 0, ph = 0;
-            for (uint32_t t = 0; t < (a.withhold ? 0u : T); ++t) {
-                if (!mbar_wait(bar_empty + 8 * s, ph ^ 1, a.err)) break;
-                mbar_expect_tx(bar_full + 8 * s, tile_bytes);
+            // per segment: its query tile (once the previous segment's MMAs are done with the
+            // last one), then its base tiles through the ring
+            uint32_t issued = 0, s = 0, ph = 0, aloads = 0;
+            bool ok = true;
+            for (uint32_t i = 0; ok && i < rg.nseg; ++i) {
+                const TcSeg g = tc_seg_at(rg, i, T);
+                const uint32_t qt = a.tile_list ? a.tile_list[g.li] : g.li;
+                if (aloads > 0 && !mbar_wait(bar_aempty, (aloads - 1) & 1, a.err)) break;
+                mbar_expect_tx(bar_a, tile_bytes);
                 for (uint32_t c = 0; c < a.katoms; ++c)
-                    tma_load_2d(smem_u32(sB + s * tile_bytes + c * atom_bytes), &tmB, int32_t(c * TC_KATOM),
-                                int32_t(t * TC_N), bar_full + 8 * s);
-                ++issued;
-                if (++s == a.stages) { s = 0; ph ^= 1; }
+                    tma_load_2d(smem_u32(sA + c * atom_bytes), &tmA, int32_t(c * TC_KATOM), int32_t(qt * TC_M), bar_a);
+                ++aloads;
+                for (uint32_t b = g.b0; b < (a.withhold ? g.b0 : g.b1); ++b) {
+                    if (!mbar_wait(bar_empty + 8 * s, ph ^ 1, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(bar_full + 8 * s, tile_bytes);
+                    for (uint32_t c = 0; c < a.katoms; ++c)
+                        tma_load_2d(smem_u32(sB + s * tile_bytes + c * atom_bytes), &tmB, int32_t(c * TC_KATOM),
+                                    int32_t(b * TC_N), bar_full + 8 * s);
+                    ++issued;
+                    if (++s == a.stages) { s = 0; ph ^= 1; }
+                }
             }
             // every copy this thread issued has landed before the CTA may exit
-            mbar_wait(bar_a, 0, a.err);
+            if (aloads > 0) mbar_wait(bar_a, (aloads - 1) & 1, a.err);
             for (uint32_t t = issued > a.stages ? issued - a.stages : 0; t < issued; ++t)
                 mbar_wait(bar_full + 8 * (t % a.stages), (t / a.stages) & 1, a.err);
         }
@@ -395,182 +523,200 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (warp == 5) {
         if (lane == 0) {
             const uint32_t idesc = tc_idesc(TC_M, TC_N);
-            bool ok = mbar_wait(bar_a, 0, a.err);
-            uint32_t s = 0, ph = 0, nissued = 0;
-            for (uint32_t t = 0; ok && t < T; ++t) {
-                const uint32_t ts = t % TC_ACC, tph = (t / TC_ACC) & 1;  // TMEM accumulator
-                if (!mbar_wait(bar_full + 8 * s, ph, a.err)) break;
-                if (!mbar_wait(bar_tempty + 8 * ts, tph ^ 1, a.err)) break;
-                if constexpr (MET == M_L2) {
-                    // the tile's base norms beside its accumulator (the epilogue has released both),
-                    // so the epilogue reads them from shared memory with the copy long landed
-                    mbar_expect_tx(bar_nfull + 8 * ts, TC_N * 4);
-                    bulk_load(smem_u32(nring + ts * TC_M), a.bnorm + size_t(t) * TC_N, TC_N * 4, bar_nfull + 8 * ts);
-                    ++nissued;
+            uint32_t s = 0, ph = 0, g = 0;
+            bool ok = true;
+            for (uint32_t seg = 0; ok && seg < rg.nseg; ++seg) {
+                const TcSeg sg = tc_seg_at(rg, seg, T);
+                if (!mbar_wait(bar_a, seg & 1, a.err)) break;
+                for (uint32_t b = sg.b0; b < sg.b1; ++b, ++g) {
+                    const uint32_t ts = g % TC_ACC, tph = (g / TC_ACC) & 1;  // TMEM accumulator
+                    if (!mbar_wait(bar_full + 8 * s, ph, a.err) || !mbar_wait(bar_tempty + 8 * ts, tph ^ 1, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    if constexpr (MET == M_L2) {
+                        // the tile's base norms beside its accumulator (the epilogue has released both),
+                        // so the epilogue reads them from shared memory with the copy long landed
+                        mbar_expect_tx(bar_nfull + 8 * ts, TC_N * 4);
+                        bulk_load(smem_u32(nring + ts * TC_M), a.bnorm + size_t(b) * TC_N, TC_N * 4,
+                                  bar_nfull + 8 * ts);
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t d = tmem + ts * TC_N;
+                    const uint32_t aB = smem_u32(sA), bB = smem_u32(sB + s * tile_bytes);
+                    for (uint32_t kk = 0; kk < a.katoms * (TC_KATOM / 16); ++kk) {
+                        const uint32_t off = (kk >> 2) * atom_bytes + (kk & 3) * 32;  // 16 bf16 = 32 B per step
+                        tc_mma(d, sw128_desc(aB + off), sw128_desc(bB + off), idesc, kk > 0 ? 1u : 0u);
+                    }
+                    tc_commit(bar_empty + 8 * s);    // operands of stage s consumed
+                    tc_commit(bar_tfull + 8 * ts);   // accumulator ts ready
+                    if (++s == a.stages) { s = 0; ph ^= 1; }
                 }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t d = tmem + ts * TC_N;
-                const uint32_t aB = smem_u32(sA), bB = smem_u32(sB + s * tile_bytes);
-                for (uint32_t kk = 0; kk < a.katoms * (TC_KATOM / 16); ++kk) {
-                    const uint32_t off = (kk >> 2) * atom_bytes + (kk & 3) * 32;  // 16 bf16 = 32 B per step
-                    tc_mma(d, sw128_desc(aB + off), sw128_desc(bB + off), idesc, kk > 0 ? 1u : 0u);
-                }
-                tc_commit(bar_empty + 8 * s);    // operands of stage s consumed
-                tc_commit(bar_tfull + 8 * ts);   // accumulator ts ready
-                if (++s == a.stages) { s = 0; ph ^= 1; }
+                tc_commit(bar_aempty);  // this segment's MMAs are done with the query tile
             }
             // all issued MMAs complete, and the last norm copies landed, before teardown
             tc_commit(bar_done);
             mbar_wait(bar_done, 0, a.err);
+            const uint32_t nissued = MET == M_L2 ? g : 0u;
             for (uint32_t t = nissued > TC_ACC ? nissued - TC_ACC : 0; t < nissued; ++t)
                 mbar_wait(bar_nfull + 8 * (t % TC_ACC), (t / TC_ACC) & 1, a.err);
         }
         __syncwarp();
     } else {
-        const uint32_t q = q0 + tid;
-        const bool live = q < a.nq;
-        const float qn = live ? a.qnorm[q] : 0.0f;
         const uint32_t k = a.k;
         const float scale = float(a.scale), inv_scale = 1.0f / float(a.scale);  // 1 or 256: exact
         const float kInf = __int_as_float(0x7f800000);
-        TkList L;
-        L.d = tk_d;
-        L.id = live ? a.out_ids + size_t(q) * k : nullptr;
-        L.win = win;
-        L.tid = tid;
-        L.k = k;
-        L.exact = a.exact;
-        L.lo = a.exact ? 0u : 1u;
-        L.P = 1;
-        while (L.P < k - L.lo) L.P <<= 1;
-        TkState S{0u, 0u, -3.402823466e38f, -3.402823466e38f};
-        uint32_t qlen = 0;  // queued flagged candidates, in id order
-        bool done = true;   // every tile consumed (false after a timed-out wait)
-        // t_j = |b|^2 - 2 q.b (L2) or -q.b (IP) per candidate: the distance / scale minus
-        // |q|^2 (L2).  A candidate can survive only if t_j < thr = B / scale - |q|^2.
-        // Until the list holds k entries everything passes; padding queries never do.
-        float thr = live ? kInf : -kInf;
-        for (uint32_t t = 0; t < T; ++t) {
-            const uint32_t s = t % TC_ACC, ph = (t / TC_ACC) & 1;
-            // warp-uniform wait so that the warp stays converged for tcgen05.ld
-            bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
-            if constexpr (MET == M_L2) ok = ok && __all_sync(kFull, mbar_wait(bar_nfull + 8 * s, ph, a.err));
-            if (!ok) {
-                done = false;
-                break;
+        bool done = true;  // every tile consumed (false after a timed-out wait)
+        uint32_t g = 0;    // tiles consumed by this CTA: the accumulator ring position
+        for (uint32_t seg = 0; done && seg < rg.nseg; ++seg) {
+            const TcSeg sg = tc_seg_at(rg, seg, T);
+            const uint32_t qt = a.tile_list ? a.tile_list[sg.li] : sg.li;
+            const uint32_t q = qt * TC_M + tid;
+            const bool live = q < a.nq;
+            // The segment that starts a query tile's scan replays the admission rule from an empty
+            // list and leaves the list for the merge; a segment that starts inside the scan (at
+            // most one per CTA, processed last) only records, in id order, the candidates below
+            // the bound the first segment publishes.  That bound never grows, and any later admission
+            // is below it at every moment, so the record holds every candidate the replay of the
+            // whole scan admits in this segment.
+            const bool first_seg = sg.b0 == 0;
+            const float qn = live ? a.qnorm[q] : 0.0f;
+            TkList L;
+            L.d = tk_d;
+            L.id = live ? a.out_ids + size_t(q) * k : nullptr;
+            L.win = win;
+            L.tid = tid;
+            L.k = k;
+            L.exact = a.exact;
+            L.lo = a.exact ? 0u : 1u;
+            L.P = 1;
+            while (L.P < k - L.lo) L.P <<= 1;
+            TkState S{0u, 0u, -3.402823466e38f, -3.402823466e38f, {}, {}};
+            uint32_t qlen = 0;  // queued flagged candidates, in id order
+            uint2 *const lst = a.lists + size_t(blockIdx.x) * a.cap * TC_M + tid;  // entry e at lst[e * 128]
+            uint32_t ln = 0;  // recorded candidates (beyond cap: counted only)
+            // t_j = |b|^2 - 2 q.b (L2) or -q.b (IP) per candidate: the distance / scale minus
+            // |q|^2 (L2).  A candidate can survive only if t_j < thr = B / scale - |q|^2.
+            // Until the list holds k entries everything passes; padding queries never do.
+            float thr = live ? kInf : -kInf;
+            for (uint32_t b = sg.b0; b < sg.b1; ++b, ++g) {
+                const uint32_t s = g % TC_ACC, ph = (g / TC_ACC) & 1;
+                // warp-uniform wait so that the warp stays converged for tcgen05.ld
+                bool ok = __all_sync(kFull, mbar_wait(bar_tfull + 8 * s, ph, a.err));
+                if constexpr (MET == M_L2) ok = ok && __all_sync(kFull, mbar_wait(bar_nfull + 8 * s, ph, a.err));
+                if (!ok) {
+                    done = false;
+                    break;
+                }
+                if (!first_seg && live) thr = fminf(thr, ld_volatile(a.bound + q));
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (uint32_t c = 0; c < TC_N / 32; ++c) {
+                    const uint64_t id0 = uint64_t(b) * TC_N + c * 32;
+                    float bn[32];
+                    if constexpr (MET == M_L2) {
+                        // this chunk's base norms from the tile's staged copy (one broadcast read per 16 B)
+                        const float4 *bp = reinterpret_cast<const float4 *>(nring + s * TC_M + c * 32);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const float4 x = bp[j];
+                            bn[4 * j] = x.x;
+                            bn[4 * j + 1] = x.y;
+                            bn[4 * j + 2] = x.z;
+                            bn[4 * j + 3] = x.w;
+                        }
+                    }
+                    uint32_t v[32];
+                    __syncwarp();
+                    tc_ld32(tmem + (uint32_t(warp * 32) << 16) + s * TC_N + c * 32, v);
+                    // chunk minimum of t_j by a tree (independent operations)
+                    float m[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        if constexpr (MET == M_L2)
+                            m[j] = fminf(fmaf(-2.0f, __uint_as_float(v[j]), bn[j]),
+                                         fmaf(-2.0f, __uint_as_float(v[j + 16]), bn[j + 16]));
+                        else
+                            m[j] = fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 16]));
+                    }
+#pragma unroll
+                    for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+                        for (int j = 0; j < w; ++j) m[j] = MET == M_L2 ? fminf(m[j], m[j + w]) : fmaxf(m[j], m[j + w]);
+                    const float tmin = MET == M_L2 ? m[0] : -m[0];
+                    // flagged candidates of this chunk; ids at or past n are zero padding rows of the last tile
+                    uint32_t mask = 0;
+                    if (tmin < thr) {
+                        if (id0 < a.n) mask = a.n - id0 >= 32 ? kFull : (1u << uint32_t(a.n - id0)) - 1u;
+                        uint32_t pass = 0;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const float tj =
+                                MET == M_L2 ? fmaf(-2.0f, __uint_as_float(v[j]), bn[j]) : -__uint_as_float(v[j]);
+                            pass |= uint32_t(tj < thr) << j;
+                        }
+                        mask &= pass;
+                    }
+                    if (!first_seg) {
+                        while (mask) {
+                            const uint32_t j = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            const float acc = __uint_as_float(pick32(v, j));
+                            const float tj = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
+                            const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+                            if (ln < a.cap) lst[size_t(ln) * TC_M] = make_uint2(__float_as_uint(dist), uint32_t(id0) + j);
+                            ++ln;
+                        }
+                        continue;
+                    }
+                    // Queue them; when some thread's queue would overflow, the warp drains every
+                    // queue (older ids first) and replays this chunk directly.  Admissions then
+                    // cost the warp about the largest per-thread count, not one round per chunk.
+                    if (__any_sync(kFull, qlen + __popc(mask) > TC_QUEUE)) {
+                        for (uint32_t e = 0; e < qlen; ++e) {
+                            const float tj = qv[e * TC_M + tid];
+                            if (!(tj < thr)) continue;  // the bound fell since the chunk test
+                            const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+                            thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
+                        }
+                        qlen = 0;
+                        while (mask) {
+                            const uint32_t j = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            const float acc = __uint_as_float(pick32(v, j));
+                            const float tj = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
+                            if (!(tj < thr)) continue;
+                            const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+                            thr = tk_offer(L, S, dist, uint32_t(id0) + j) * inv_scale - (MET == M_L2 ? qn : 0.0f);
+                        }
+                    } else {
+                        while (mask) {
+                            const uint32_t j = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            const float acc = __uint_as_float(pick32(v, j));
+                            qv[qlen * TC_M + tid] = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
+                            qi[qlen * TC_M + tid] = uint32_t(id0) + j;
+                            ++qlen;
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                mbar_arrive(bar_tempty + 8 * s);
+                if (first_seg && live && thr < kInf) st_volatile(a.bound + q, thr);
             }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (uint32_t c = 0; c < TC_N / 32; ++c) {
-                const uint64_t id0 = uint64_t(t) * TC_N + c * 32;
-                float bn[32];
-                if constexpr (MET == M_L2) {
-                    // this chunk's base norms from the tile's staged copy (one broadcast read per 16 B)
-                    const float4 *bp = reinterpret_cast<const float4 *>(nring + s * TC_M + c * 32);
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const float4 x = bp[j];
-                        bn[4 * j] = x.x;
-                        bn[4 * j + 1] = x.y;
-                        bn[4 * j + 2] = x.z;
-                        bn[4 * j + 3] = x.w;
-                    }
+            if (first_seg) {
+                for (uint32_t e = 0; e < qlen; ++e) {
+                    const float tj = qv[e * TC_M + tid];
+                    if (!(tj < thr)) continue;
+                    const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
+                    thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
                 }
-                uint32_t v[32];
-                __syncwarp();
-                tc_ld32(tmem + (uint32_t(warp * 32) << 16) + s * TC_N + c * 32, v);
-                // chunk minimum of t_j by a tree (independent operations)
-                float m[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    if constexpr (MET == M_L2)
-                        m[j] = fminf(fmaf(-2.0f, __uint_as_float(v[j]), bn[j]),
-                                     fmaf(-2.0f, __uint_as_float(v[j + 16]), bn[j + 16]));
-                    else
-                        m[j] = fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 16]));
+                // the list in slot order (ids are already in out_ids) and the replay state, for the merge
+                if (done && live) {
+                    for (uint32_t l = 0; l < S.cnt; ++l) a.out_dists[size_t(q) * k + l] = tk_d[l * TC_M + tid];
+                    a.state[q] = make_uint4(S.cnt, S.toppos, __float_as_uint(S.topdist), __float_as_uint(S.lmax));
                 }
-#pragma unroll
-                for (int w = 8; w > 0; w >>= 1)
-#pragma unroll
-                    for (int j = 0; j < w; ++j) m[j] = MET == M_L2 ? fminf(m[j], m[j + w]) : fmaxf(m[j], m[j + w]);
-                const float tmin = MET == M_L2 ? m[0] : -m[0];
-                // flagged candidates of this chunk; ids at or past n are zero padding rows of the last tile
-                uint32_t mask = 0;
-                if (tmin < thr) {
-                    if (id0 < a.n) mask = a.n - id0 >= 32 ? kFull : (1u << uint32_t(a.n - id0)) - 1u;
-                    uint32_t pass = 0;
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const float tj =
-                            MET == M_L2 ? fmaf(-2.0f, __uint_as_float(v[j]), bn[j]) : -__uint_as_float(v[j]);
-                        pass |= uint32_t(tj < thr) << j;
-                    }
-                    mask &= pass;
-                }
-                // Queue them; when some thread's queue would overflow, the warp drains every
-                // queue (older ids first) and replays this chunk directly.  Admissions then
-                // cost the warp about the largest per-thread count, not one round per chunk.
-                if (__any_sync(kFull, qlen + __popc(mask) > TC_QUEUE)) {
-                    for (uint32_t e = 0; e < qlen; ++e) {
-                        const float tj = qv[e * TC_M + tid];
-                        if (!(tj < thr)) continue;  // the bound fell since the chunk test
-                        const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
-                        thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
-                    }
-                    qlen = 0;
-                    while (mask) {
-                        const uint32_t j = __ffs(mask) - 1;
-                        mask &= mask - 1;
-                        const float acc = __uint_as_float(pick32(v, j));
-                        const float tj = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
-                        if (!(tj < thr)) continue;
-                        const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
-                        thr = tk_offer(L, S, dist, uint32_t(id0) + j) * inv_scale - (MET == M_L2 ? qn : 0.0f);
-                    }
-                } else {
-                    while (mask) {
-                        const uint32_t j = __ffs(mask) - 1;
-                        mask &= mask - 1;
-                        const float acc = __uint_as_float(pick32(v, j));
-                        qv[qlen * TC_M + tid] = MET == M_L2 ? fmaf(-2.0f, acc, pick32(bn, j)) : -acc;
-                        qi[qlen * TC_M + tid] = uint32_t(id0) + j;
-                        ++qlen;
-                    }
-                }
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            mbar_arrive(bar_tempty + 8 * s);
-        }
-        for (uint32_t e = 0; e < qlen; ++e) {
-            const float tj = qv[e * TC_M + tid];
-            if (!(tj < thr)) continue;
-            const float dist = (MET == M_L2 ? qn + tj : tj) * scale;
-            thr = tk_offer(L, S, dist, qi[e * TC_M + tid]) * inv_scale - (MET == M_L2 ? qn : 0.0f);
-        }
-        // output sorted by (dist, id) (CompGT.cpp:107-124).  Every tile has been through the
-        // MMA, so the operand area is free: the ids go there, [k][128] so that a thread's
-        // entries stride 128 words, and the insertion sort runs on shared memory only.
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        uint32_t *sid = reinterpret_cast<uint32_t *>(smem);
-        if (done && live && S.cnt == k) {
-            for (uint32_t l = 0; l < k; ++l) sid[l * TC_M + tid] = L.id[l];
-            for (uint32_t i = 1; i < k; ++i) {
-                const float dv = tk_d[i * TC_M + tid];
-                const uint32_t iv = sid[i * TC_M + tid];
-                int32_t j = int32_t(i) - 1;
-                while (j >= 0) {
-                    const float dj = tk_d[j * TC_M + tid];
-                    const uint32_t ij = sid[j * TC_M + tid];
-                    if (!(dj > dv || (dj == dv && ij > iv))) break;
-                    tk_d[(j + 1) * TC_M + tid] = dj;
-                    sid[(j + 1) * TC_M + tid] = ij;
-                    --j;
-                }
-                tk_d[(j + 1) * TC_M + tid] = dv;
-                sid[(j + 1) * TC_M + tid] = iv;
-            }
-            for (uint32_t l = 0; l < k; ++l) {
-                L.id[l] = sid[l * TC_M + tid];
-                a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
+            } else if (live) {
+                a.list_n[size_t(blockIdx.x) * TC_M + tid] = ln;
             }
         }
     }
@@ -581,6 +727,91 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
     }
 }
+
+// Merge of one query tile (thread t = query t): the list its first segment left (slot order,
+// with the replay state), then the candidates recorded by the segments that continue its scan,
+// in id order, through the same admission rule; then the output sorted by (dist, id)
+// (CompGT.cpp:107-124).  Shared memory: the list [k][128], the ids for the sort [k][128] and the
+// tournament tree [128][128].
+template <int MET>
+__global__ void __launch_bounds__(TC_M) gt_tc_merge_kernel(TcArgs a)
+{
+    extern __shared__ __align__(16) uint8_t msmem[];
+    const uint32_t k = a.k;
+    float *tk_d = reinterpret_cast<float *>(msmem);
+    uint32_t *sid = reinterpret_cast<uint32_t *>(tk_d + size_t(k) * TC_M);
+    uint8_t *win = reinterpret_cast<uint8_t *>(sid + size_t(k) * TC_M);
+    const int tid = threadIdx.x;
+    const uint32_t li = blockIdx.x;
+    const uint32_t qt = a.tile_list ? a.tile_list[li] : li;
+    const uint32_t q = qt * TC_M + tid;
+    if (q >= a.nq || *a.err) return;  // padding query, or the scan did not finish
+    TkList L;
+    L.d = tk_d;
+    L.id = a.out_ids + size_t(q) * k;
+    L.win = win;
+    L.tid = tid;
+    L.k = k;
+    L.exact = a.exact;
+    L.lo = a.exact ? 0u : 1u;
+    L.P = 1;
+    while (L.P < k - L.lo) L.P <<= 1;
+    const uint4 st = a.state[q];
+    TkState S{st.x < k ? st.x : k, st.y, __uint_as_float(st.z), __uint_as_float(st.w), {}, {}};
+    for (uint32_t l = 0; l < S.cnt; ++l) tk_d[l * TC_M + tid] = a.out_dists[size_t(q) * k + l];
+    if (S.cnt == k) {
+        if (a.exact) tt_build(L);
+        else tk_groups_build(L, S);
+    }
+    // the CTAs whose ranges start inside this tile's scan, in order
+    const uint2 cr = a.conts[li];
+    for (uint32_t c = cr.x; c < cr.x + cr.y; ++c) {
+        const uint32_t n = a.list_n[size_t(c) * TC_M + tid];
+        if (n > a.cap) {
+            atomicExch(a.ovf + li, 1u);  // recorded candidates lost: the host reruns this tile unsplit
+            return;
+        }
+        // entry-major lists: the warp's threads read one 256-byte line per entry index; the
+        // next 16 entries load while the current 16 are replayed
+        const uint2 *lst = a.lists + size_t(c) * a.cap * TC_M + tid;
+        uint2 x[16], y[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) x[j] = uint32_t(j) < n ? lst[size_t(j) * TC_M] : make_uint2(0, 0);
+        for (uint32_t e0 = 0; e0 < n; e0 += 16) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                y[j] = e0 + 16 + j < n ? lst[size_t(e0 + 16 + j) * TC_M] : make_uint2(0, 0);
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (e0 + j < n) tk_offer(L, S, __uint_as_float(x[j].x), x[j].y);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) x[j] = y[j];
+        }
+    }
+    if (S.cnt != k) return;  // n >= k is checked by the caller
+    for (uint32_t l = 0; l < k; ++l) sid[l * TC_M + tid] = L.id[l];
+    for (uint32_t i = 1; i < k; ++i) {
+        const float dv = tk_d[i * TC_M + tid];
+        const uint32_t iv = sid[i * TC_M + tid];
+        int32_t j = int32_t(i) - 1;
+        while (j >= 0) {
+            const float dj = tk_d[j * TC_M + tid];
+            const uint32_t ij = sid[j * TC_M + tid];
+            if (!(dj > dv || (dj == dv && ij > iv))) break;
+            tk_d[(j + 1) * TC_M + tid] = dj;
+            sid[(j + 1) * TC_M + tid] = ij;
+            --j;
+        }
+        tk_d[(j + 1) * TC_M + tid] = dv;
+        sid[(j + 1) * TC_M + tid] = iv;
+    }
+    for (uint32_t l = 0; l < k; ++l) {
+        L.id[l] = sid[l * TC_M + tid];
+        a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
+    }
+}
+
+static size_t gt_tc_merge_smem(uint32_t k) { return size_t(k) * TC_M * 8 + TC_M * TC_M; }
 
 // u8/i8/u4 rows -> bf16 K-major rows (K = padded element count) and int32 squared norms
 template <int DT>
@@ -657,14 +888,12 @@ size_t gt_tc_smem(uint32_t katoms, uint32_t k, uint32_t stages)
     return need > 120 * 1024 ? need : 120 * 1024;
 }
 
-// deepest ring that fits, 0 if even two stages do not; the final sort reuses the operand
-// area (query tile + ring) for the ids, so it must hold k x 128 of them
+// deepest ring that fits, 0 if even two stages do not (or the merge's lists do not)
 static uint32_t gt_tc_stages(uint32_t katoms, uint32_t k, size_t smem_optin)
 {
+    if (gt_tc_merge_smem(k) > smem_optin) return 0;
     for (uint32_t st = TC_MAX_STAGES; st >= 2; --st)
-        if (gt_tc_smem(katoms, k, st) <= smem_optin &&
-            size_t(katoms) * TC_M * 128 * (1 + st) >= size_t(k) * TC_M * 4)
-            return st;
+        if (gt_tc_smem(katoms, k, st) <= smem_optin) return st;
     return 0;
 }
 
@@ -678,15 +907,78 @@ bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_opti
     return gt_tc_stages(katoms, k, smem_optin) != 0;
 }
 
+// Work split: the QT query tiles' scans, QT x T (query tile, base tile) steps in order, cut into
+// ranges of about W steps, one per CTA, with about one CTA per SM.  A range may end inside one
+// tile's scan and continue into the next; each range that starts inside a scan records that
+// segment's candidates in a list of `cap` entries per query.  The candidates recorded are those
+// below the bound of the scan's first segment, so cuts are moved off the first W/4 tiles of a
+// scan (ranges then differ from W by at most W/8).
+struct TcSplit {
+    uint64_t W, total;
+    uint32_t ctas, cap;
+};
+
+static void tc_cuts(const TcSplit &sp, uint32_t T, uint32_t qtiles, std::vector<uint64_t> &cuts,
+                    std::vector<uint2> &conts)
+{
+    cuts.assign(sp.ctas + 1, 0);
+    const uint64_t pmin = std::max<uint64_t>(1, std::min<uint64_t>(sp.W / 4, T / 2));
+    for (uint32_t c = 1; c < sp.ctas; ++c) {
+        uint64_t x = uint64_t(c) * sp.W;
+        const uint64_t r = x % T;
+        if (sp.W >= 4ull * T) x = r * 2 < T ? x - r : x - r + T;  // ranges of whole scans
+        else if (r != 0 && r < pmin) x = r * 2 < pmin ? x - r : x - r + pmin;
+        cuts[c] = x;
+    }
+    cuts[sp.ctas] = sp.total;
+    conts.assign(qtiles, make_uint2(0, 0));
+    for (uint32_t c = 1; c < sp.ctas; ++c) {
+        if (cuts[c] % T == 0) continue;
+        const uint64_t li = cuts[c] / T;
+        if (conts[li].y == 0) conts[li].x = c;
+        ++conts[li].y;
+    }
+}
+
+static TcSplit tc_split(uint64_t qtiles, uint64_t T, uint32_t k, uint32_t sms)
+{
+    TcSplit sp;
+    sp.total = qtiles * T;
+    const uint64_t per = (sp.total + sms - 1) / sms;
+    const uint64_t floor_w = T < 64 ? T : 64;  // no segment much shorter than 64 tiles (8192 rows)
+    sp.W = per > floor_w ? per : floor_w;
+    sp.ctas = uint32_t((sp.total + sp.W - 1) / sp.W);
+    // A continuation records about k x (its rows / the first segment's rows) candidates once the
+    // first segment is done, and more while it runs: on clustered rows, where a tile's first
+    // segment holds fewer than k rows of a query's cluster, several thousand at k = 100.
+    uint32_t cap = 2048;
+    while (cap < 160 * k) cap <<= 1;
+    sp.cap = cap;
+    return sp;
+}
+
+static uint32_t device_sms()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || sms <= 0)
+        return 1;
+    return uint32_t(sms);
+}
+
 // Workspace of the tensor engine: bf16 rows of base and queries (K = codes rounded up to
-// 64), fp32 squared norms, and the error flag; regions 256-byte aligned.
+// 64), fp32 squared norms, the error flag, and the split's merge state (per query: replay
+// state and published bound; per CTA: continuation lists and counts; per query tile: overflow
+// flag, then the rerun tile list); regions 256-byte aligned.
 struct TcLayout {
     uint32_t K, katoms;
     uint64_t n_pad, nq_pad;
-    size_t off_bq, off_bn, off_qn, off_err, bytes;
+    TcSplit sp;
+    size_t off_bq, off_bn, off_qn, off_err, off_state, off_bound, off_listn, off_lists, off_ovf, off_tl, off_cuts,
+        off_conts, bytes;
 };
 
-static TcLayout tc_layout(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq)
+static TcLayout tc_layout(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq, uint32_t k, uint32_t sms)
 {
     TcLayout l;
     const uint32_t elems = (dtype == NBPG_U4 || dtype == NBPG_I4) ? 2 * dims : dims;
@@ -694,18 +986,28 @@ static TcLayout tc_layout(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq
     l.katoms = l.K / TC_KATOM;
     l.n_pad = (n + TC_N - 1) / TC_N * TC_N;
     l.nq_pad = (uint64_t(nq) + TC_M - 1) / TC_M * TC_M;
+    const uint64_t qtiles = l.nq_pad / TC_M;
+    l.sp = tc_split(qtiles, l.n_pad / TC_N, k, sms);
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     l.off_bq = up(l.n_pad * l.K * 2);
     l.off_bn = l.off_bq + up(l.nq_pad * l.K * 2);
     l.off_qn = l.off_bn + up(l.n_pad * 4);
     l.off_err = l.off_qn + up(l.nq_pad * 4);
-    l.bytes = l.off_err + 256;
+    l.off_state = l.off_err + 256;
+    l.off_bound = l.off_state + up(l.nq_pad * 16);
+    l.off_listn = l.off_bound + up(l.nq_pad * 4);
+    l.off_lists = l.off_listn + up(size_t(l.sp.ctas) * TC_M * 4);
+    l.off_ovf = l.off_lists + up(size_t(l.sp.ctas) * TC_M * l.sp.cap * 8);
+    l.off_tl = l.off_ovf + up(qtiles * 4);
+    l.off_cuts = l.off_tl + up(qtiles * 4);
+    l.off_conts = l.off_cuts + up((std::max<uint64_t>(l.sp.ctas, qtiles) + 1) * 8);
+    l.bytes = l.off_conts + up(qtiles * 8);
     return l;
 }
 
-size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq)
+size_t gt_tc_workspace(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq, uint32_t k)
 {
-    return tc_layout(dtype, dims, n, nq).bytes;
+    return tc_layout(dtype, dims, n, nq, k, device_sms()).bytes;
 }
 
 // Device-resident inputs (rows of dims bytes, stride bytes apart); outputs device arrays
@@ -716,7 +1018,7 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
                          float *d_dists, void *ws, cudaStream_t st, bool withhold = false)
 {
     const bool nib = dtype == NBPG_U4 || dtype == NBPG_I4;
-    const TcLayout l = tc_layout(dtype, dims, n, nq);
+    const TcLayout l = tc_layout(dtype, dims, n, nq, k, device_sms());
     const uint32_t K = l.K;
     const uint64_t n_pad = l.n_pad, nq_pad = l.nq_pad;
     void *owned = nullptr;
@@ -734,8 +1036,14 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
     __nv_bfloat16 *bQ = reinterpret_cast<__nv_bfloat16 *>(w + l.off_bq);
     float *bn = reinterpret_cast<float *>(w + l.off_bn), *qn = reinterpret_cast<float *>(w + l.off_qn);
     uint32_t *err = reinterpret_cast<uint32_t *>(w + l.off_err);
+    const uint32_t qtiles = uint32_t(nq_pad / TC_M);
+    uint32_t *ovf = reinterpret_cast<uint32_t *>(w + l.off_ovf);
     nbpg_status s = NBPG_OK;
     e = cudaMemsetAsync(err, 0, 4, st);
+    // bounds start far above any distance (0x7f7f7f7f = 3.4e38): until a tile's first segment
+    // publishes, a continuation records every candidate
+    if (e == cudaSuccess) e = cudaMemsetAsync(w + l.off_bound, 0x7f, l.nq_pad * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ovf, 0, size_t(qtiles) * 4, st);
     if (e == cudaSuccess) {
         const uint32_t thr = 128;
         switch (dtype) {
@@ -767,19 +1075,84 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
         s = NBPG_ERR_UNSUPPORTED;
     }
     const size_t smem = gt_tc_smem(l.katoms, k, stages ? stages : 2);
+    const size_t msmem = gt_tc_merge_smem(k);
     if (e == cudaSuccess && s == NBPG_OK)
         e = cudaFuncSetAttribute(metric == NBPG_L2 ? gt_tc_kernel<M_L2> : gt_tc_kernel<M_IP>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e == cudaSuccess && s == NBPG_OK) {
-        TcArgs a{qn, bn, n, nq, k, mode == NBPG_GT_EXACT ? 1u : 0u, nib ? 256u : 1u, l.katoms,
-                 uint32_t(n_pad / TC_N), stages, withhold ? 1u : 0u, d_ids, d_dists, err};
-        if (metric == NBPG_L2) gt_tc_kernel<M_L2><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
-        else gt_tc_kernel<M_IP><<<uint32_t(nq_pad / TC_M), TC_THREADS, smem, st>>>(mA, mB, a);
-        e = cudaGetLastError();
-    }
+    if (e == cudaSuccess && s == NBPG_OK)
+        e = cudaFuncSetAttribute(metric == NBPG_L2 ? gt_tc_merge_kernel<M_L2> : gt_tc_merge_kernel<M_IP>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(msmem));
+    TcArgs a{};
+    a.qnorm = qn;
+    a.bnorm = bn;
+    a.n = n;
+    a.nq = nq;
+    a.k = k;
+    a.exact = mode == NBPG_GT_EXACT ? 1u : 0u;
+    a.scale = nib ? 256u : 1u;
+    a.katoms = l.katoms;
+    a.T = uint32_t(n_pad / TC_N);
+    a.stages = stages;
+    a.withhold = withhold ? 1u : 0u;
+    a.out_ids = d_ids;
+    a.out_dists = d_dists;
+    a.err = err;
+    uint64_t *d_cuts = reinterpret_cast<uint64_t *>(w + l.off_cuts);
+    uint2 *d_conts = reinterpret_cast<uint2 *>(w + l.off_conts);
+    std::vector<uint64_t> cuts;
+    std::vector<uint2> conts;
+    tc_cuts(l.sp, uint32_t(n_pad / TC_N), qtiles, cuts, conts);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_cuts, cuts.data(), cuts.size() * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_conts, conts.data(), conts.size() * 8, cudaMemcpyHostToDevice, st);
+    a.cuts = d_cuts;
+    a.conts = d_conts;
+    a.tile_list = nullptr;
+    a.state = reinterpret_cast<uint4 *>(w + l.off_state);
+    a.bound = reinterpret_cast<float *>(w + l.off_bound);
+    a.lists = reinterpret_cast<uint2 *>(w + l.off_lists);
+    a.list_n = reinterpret_cast<uint32_t *>(w + l.off_listn);
+    a.cap = l.sp.cap;
+    a.ovf = ovf;
+    auto launch = [&](const TcArgs &x, uint32_t ctas, uint32_t tiles) {
+        if (metric == NBPG_L2) {
+            gt_tc_kernel<M_L2><<<ctas, TC_THREADS, smem, st>>>(mA, mB, x);
+            gt_tc_merge_kernel<M_L2><<<tiles, TC_M, msmem, st>>>(x);
+        } else {
+            gt_tc_kernel<M_IP><<<ctas, TC_THREADS, smem, st>>>(mA, mB, x);
+            gt_tc_merge_kernel<M_IP><<<tiles, TC_M, msmem, st>>>(x);
+        }
+        return cudaGetLastError();
+    };
+    if (e == cudaSuccess && s == NBPG_OK) e = launch(a, l.sp.ctas, qtiles);
     uint32_t herr = 0;
+    std::vector<uint32_t> hovf(qtiles, 0);
     if (e == cudaSuccess && s == NBPG_OK) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && s == NBPG_OK)
+        e = cudaMemcpyAsync(hovf.data(), ovf, size_t(qtiles) * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && s == NBPG_OK && !herr) {
+        // query tiles whose continuation lists overflowed: rerun them with one CTA per whole scan
+        std::vector<uint32_t> rerun;
+        for (uint32_t i = 0; i < qtiles; ++i)
+            if (hovf[i]) rerun.push_back(i);
+        if (!rerun.empty()) {
+            uint32_t *tl = reinterpret_cast<uint32_t *>(w + l.off_tl);
+            TcArgs b = a;
+            b.tile_list = tl;
+            cuts.resize(rerun.size() + 1);
+            for (size_t i = 0; i <= rerun.size(); ++i) cuts[i] = uint64_t(i) * a.T;
+            conts.assign(rerun.size(), make_uint2(0, 0));
+            e = cudaMemcpyAsync(tl, rerun.data(), rerun.size() * 4, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d_cuts, cuts.data(), cuts.size() * 8, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_conts, conts.data(), conts.size() * 8, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = launch(b, uint32_t(rerun.size()), uint32_t(rerun.size()));
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        }
+    }
     if (e != cudaSuccess && s == NBPG_OK) {
         set_error(std::string("nbpg_gt (tensor path): ") + cudaGetErrorString(e));
         s = NBPG_ERR_CUDA;

@@ -88,6 +88,39 @@ def test_gt_tensor_limits(gpu_lib, oracle_lib):
         ground_truth(w, w[:9], "u8", "l2", k=10, engine="tensor")
 
 
+def test_gt_tensor_split_scan(gpu_lib, oracle_lib):
+    """The tensor engine cuts the (query tile, base tile) steps into one range per SM, so a
+    query tile's scan spans several CTAs: the first replays the admission rule, the others
+    record the candidates below the bound it publishes, and a merge replays them in id order.
+    200k rows give each 128-query tile about a dozen segments of 64 base tiles."""
+    from nbpg_gb300 import synth
+    from nbpg_gb300.index import ground_truth
+    b, q = synth.u8_mixture(200000, 300, dim=32, n_centres=64)
+    for metric in ("l2", "ip"):
+        for exact in (False, True):
+            for k in (10, 100):
+                ids, ds = ground_truth(b, q, "u8", metric, k=k, exact=exact, engine="tensor")
+                oi, od = oracle_lib.gt("u8", metric, b, q, k=k, exact=exact)
+                assert np.array_equal(ids, oi), (metric, exact, k)
+                assert np.array_equal(ds.view(np.uint32), od.view(np.uint32)), (metric, exact, k)
+
+
+def test_gt_tensor_split_overflow(gpu_lib, oracle_lib):
+    """Base rows in decreasing distance from every query: each new row is admitted, so every
+    segment after the first records all of its rows, more than its list holds; the engine
+    reruns those query tiles with one CTA per whole scan and the results stay exact."""
+    from nbpg_gb300.index import ground_truth
+    r = np.random.default_rng(4)
+    b = r.integers(0, 256, (100000, 16)).astype(np.uint8)
+    b = b[np.argsort(-(b.astype(np.int64) ** 2).sum(1), kind="stable")]
+    q = np.zeros((140, 16), np.uint8)
+    q[::2] = 1
+    for exact in (False, True):
+        ids, ds = ground_truth(b, q, "u8", "l2", k=10, exact=exact, engine="tensor")
+        oi, od = oracle_lib.gt("u8", "l2", b, q, k=10, exact=exact)
+        assert np.array_equal(ids, oi) and np.array_equal(ds, od), exact
+
+
 @pytest.mark.parametrize("engine", ["dp4a", "tensor"])
 def test_gt_device_entry(gpu_lib, oracle_lib, engine):
     """nbpg_gt_device on device buffers with padded rows, caller workspace and internal allocation."""
