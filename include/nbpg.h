@@ -292,7 +292,11 @@ nbpg_status nbpg_gt_with_engine(uint32_t dtype, uint32_t metric, uint32_t dims, 
  * legacy default stream).  Rows are row_stride bytes apart (a multiple of 16, >= dims;
  * bytes past dims must be zero), both arrays 16-byte aligned.  The tensor engine needs
  * nbpg_gt_workspace_size() bytes of device workspace (0 for DP4A); d_workspace NULL
- * makes the call allocate it.  Returns after the work has finished on `stream`. */
+ * makes the call allocate it.  The size depends on the current device's SM count: the
+ * tensor engine cuts the scans into one range per SM and keeps, per range and query, a list
+ * of up to max(2048, 80 k rounded up to a power of two) candidates (1.5 GB on 152 SMs at
+ * k = 100, besides the bf16 copies of base and queries).  Returns after the work has
+ * finished on `stream`. */
 nbpg_status nbpg_gt_workspace_size(uint32_t dtype, uint32_t dims, uint64_t n, uint32_t nq, uint32_t k,
                                    uint32_t engine, size_t *bytes);
 nbpg_status nbpg_gt_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_t row_stride, const void *d_base,

@@ -557,9 +557,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // all issued MMAs complete, and the last norm copies landed, before teardown
             tc_commit(bar_done);
             mbar_wait(bar_done, 0, a.err);
-            const uint32_t nissued = MET == M_L2 ? g : 0u;
-            for (uint32_t t = nissued > TC_ACC ? nissued - TC_ACC : 0; t < nissued; ++t)
-                mbar_wait(bar_nfull + 8 * (t % TC_ACC), (t / TC_ACC) & 1, a.err);
+            if constexpr (MET == M_L2)
+                for (uint32_t t = g > TC_ACC ? g - TC_ACC : 0; t < g; ++t)
+                    mbar_wait(bar_nfull + 8 * (t % TC_ACC), (t / TC_ACC) & 1, a.err);
         }
         __syncwarp();
     } else {
@@ -813,38 +813,43 @@ __global__ void __launch_bounds__(TC_M) gt_tc_merge_kernel(TcArgs a)
 
 static size_t gt_tc_merge_smem(uint32_t k) { return size_t(k) * TC_M * 8 + TC_M * TC_M; }
 
-// u8/i8/u4 rows -> bf16 K-major rows (K = padded element count) and int32 squared norms
+// u8/i8/u4 rows -> bf16 K-major rows (K = padded element count, 64 or 128) and int32 squared
+// norms.  One thread per 8 elements: one 16-byte store each, the row's norm summed over its
+// K / 8 lanes by shuffles (rows_pad x K / 8 is a multiple of 1024, so every warp is full).
 template <int DT>
-__global__ void to_bf16_kernel(const uint8_t *src, uint32_t row_bytes, uint32_t stride, uint64_t rows,
-                               uint64_t rows_pad, uint32_t K, __nv_bfloat16 *dst, float *norm)
+__global__ void __launch_bounds__(256) to_bf16_kernel(const uint8_t *src, uint32_t row_bytes, uint32_t stride,
+                                                      uint64_t rows, uint64_t rows_pad, uint32_t K,
+                                                      __nv_bfloat16 *dst, float *norm)
 {
-    const uint64_t r = blockIdx.x;
-    if (r >= rows_pad) return;
+    const uint32_t gpr = K / 8;  // lanes per row: 8 or 16
+    const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t r = t / gpr;
+    const uint32_t g = uint32_t(t % gpr);
     int32_t acc = 0;
-    for (uint32_t e = threadIdx.x; e < K; e += blockDim.x) {
-        int32_t v = 0;
-        if (r < rows) {
-            if constexpr (DT == DT_U8) { if (e < row_bytes) v = src[r * stride + e]; }
-            else if constexpr (DT == DT_I8) { if (e < row_bytes) v = int8_t(src[r * stride + e]); }
-            else {
-                if (e / 2 < row_bytes) {
-                    const uint8_t b = src[r * stride + e / 2];
-                    v = (e & 1) ? (b & 0x0F) : (b >> 4);  // nibble values; distances scaled by 256 later
+    uint32_t packed[4] = {0, 0, 0, 0};
+    if (r < rows_pad) {
+#pragma unroll
+        for (uint32_t j = 0; j < 8; ++j) {
+            const uint32_t e = g * 8 + j;
+            int32_t v = 0;
+            if (r < rows) {
+                if constexpr (DT == DT_U8) { if (e < row_bytes) v = src[r * stride + e]; }
+                else if constexpr (DT == DT_I8) { if (e < row_bytes) v = int8_t(src[r * stride + e]); }
+                else {
+                    if (e / 2 < row_bytes) {
+                        const uint8_t b = src[r * stride + e / 2];
+                        v = (e & 1) ? (b & 0x0F) : (b >> 4);  // nibble values; distances scaled by 256 later
+                    }
                 }
             }
+            acc += v * v;
+            const uint32_t h = __bfloat16_as_ushort(__int2bfloat16_rn(v));
+            packed[j / 2] |= h << (16 * (j & 1));
         }
-        dst[r * K + e] = __int2bfloat16_rn(v);
-        acc += v * v;
+        *reinterpret_cast<uint4 *>(dst + r * K + g * 8) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-    __shared__ int32_t part[32];
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int32_t s = 0;
-        for (uint32_t w = 0; w < (blockDim.x + 31) / 32; ++w) s += part[w];
-        norm[r] = float(s);  // at most 128 * 255^2 < 2^24: exact
-    }
+    for (uint32_t o = gpr / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if (r < rows_pad && g == 0) norm[r] = float(acc);  // at most 128 * 255^2 < 2^24: exact
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -950,9 +955,9 @@ static TcSplit tc_split(uint64_t qtiles, uint64_t T, uint32_t k, uint32_t sms)
     sp.ctas = uint32_t((sp.total + sp.W - 1) / sp.W);
     // A continuation records about k x (its rows / the first segment's rows) candidates once the
     // first segment is done, and more while it runs: on clustered rows, where a tile's first
-    // segment holds fewer than k rows of a query's cluster, several thousand at k = 100.
+    // segment holds fewer than k rows of a query's cluster, up to about 5,500 at k = 100.
     uint32_t cap = 2048;
-    while (cap < 160 * k) cap <<= 1;
+    while (cap < 80 * k) cap <<= 1;
     sp.cap = cap;
     return sp;
 }
@@ -1045,19 +1050,19 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
     if (e == cudaSuccess) e = cudaMemsetAsync(w + l.off_bound, 0x7f, l.nq_pad * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(ovf, 0, size_t(qtiles) * 4, st);
     if (e == cudaSuccess) {
-        const uint32_t thr = 128;
+        const uint32_t cb = uint32_t(n_pad * (K / 8) / 256), cq = uint32_t(nq_pad * (K / 8) / 256);
         switch (dtype) {
         case NBPG_U8:
-            to_bf16_kernel<DT_U8><<<uint32_t(n_pad), thr, 0, st>>>(d_base, dims, stride, n, n_pad, K, bB, bn);
-            to_bf16_kernel<DT_U8><<<uint32_t(nq_pad), thr, 0, st>>>(d_q, dims, stride, nq, nq_pad, K, bQ, qn);
+            to_bf16_kernel<DT_U8><<<cb, 256, 0, st>>>(d_base, dims, stride, n, n_pad, K, bB, bn);
+            to_bf16_kernel<DT_U8><<<cq, 256, 0, st>>>(d_q, dims, stride, nq, nq_pad, K, bQ, qn);
             break;
         case NBPG_I8:
-            to_bf16_kernel<DT_I8><<<uint32_t(n_pad), thr, 0, st>>>(d_base, dims, stride, n, n_pad, K, bB, bn);
-            to_bf16_kernel<DT_I8><<<uint32_t(nq_pad), thr, 0, st>>>(d_q, dims, stride, nq, nq_pad, K, bQ, qn);
+            to_bf16_kernel<DT_I8><<<cb, 256, 0, st>>>(d_base, dims, stride, n, n_pad, K, bB, bn);
+            to_bf16_kernel<DT_I8><<<cq, 256, 0, st>>>(d_q, dims, stride, nq, nq_pad, K, bQ, qn);
             break;
         default:
-            to_bf16_kernel<DT_U4><<<uint32_t(n_pad), thr, 0, st>>>(d_base, dims, stride, n, n_pad, K, bB, bn);
-            to_bf16_kernel<DT_U4><<<uint32_t(nq_pad), thr, 0, st>>>(d_q, dims, stride, nq, nq_pad, K, bQ, qn);
+            to_bf16_kernel<DT_U4><<<cb, 256, 0, st>>>(d_base, dims, stride, n, n_pad, K, bB, bn);
+            to_bf16_kernel<DT_U4><<<cq, 256, 0, st>>>(d_q, dims, stride, nq, nq_pad, K, bQ, qn);
         }
         e = cudaGetLastError();
     }
