@@ -227,11 +227,12 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32])
 // slots 1..k-1 in the tree (its rescan is seeded with slot 0, CompGT.cpp:82-90); the
 // exact mode keeps all k slots and orders ties by id (the larger id is the larger key).
 struct TkList {
-    float *d;        // [k][128] in shared memory
+    float *d;        // [k][st] in shared memory
     uint32_t *id;    // k ids: this query's row of the output (written on admission, read on ties)
-    uint8_t *win;    // [128 nodes][128]
+    uint8_t *win;    // [128 nodes][st]
     int tid;
     uint32_t k, lo, P, exact;
+    uint32_t st;  // entries of one slot (threads sharing the arrays): 128 in the scan, 32 in the merge
 };
 
 // Running state of one query's list.  CompGT: CompGT's toppos/topdist and the list
@@ -255,7 +256,7 @@ __device__ __forceinline__ void tk_group_scan(const TkList &L, uint32_t g, float
     const uint32_t s0 = 1 + g * TK_GROUP;
     float v[TK_GROUP];
 #pragma unroll
-    for (uint32_t j = 0; j < TK_GROUP; ++j) v[j] = s0 + j < L.k ? L.d[(s0 + j) * TC_M + L.tid] : -3.402823466e38f;
+    for (uint32_t j = 0; j < TK_GROUP; ++j) v[j] = s0 + j < L.k ? L.d[(s0 + j) * L.st + L.tid] : -3.402823466e38f;
     m = v[0];
     arg = s0;
 #pragma unroll
@@ -294,27 +295,27 @@ __device__ __forceinline__ uint32_t tt_node(const TkList &L, uint32_t x)
         const uint32_t slot = L.lo + (x - L.P);
         return slot < L.k ? slot : kNoSlot;
     }
-    return L.win[x * TC_M + L.tid];
+    return L.win[x * L.st + L.tid];
 }
 
 __device__ __forceinline__ uint32_t tt_pick(const TkList &L, uint32_t a, uint32_t b)
 {
     if (b == kNoSlot) return a;
     if (a == kNoSlot) return b;
-    const float da = L.d[a * TC_M + L.tid], db = L.d[b * TC_M + L.tid];
+    const float da = L.d[a * L.st + L.tid], db = L.d[b * L.st + L.tid];
     if (db != da) return db > da ? b : a;
     return (L.exact && L.id[b] > L.id[a]) ? b : a;
 }
 
 __device__ __forceinline__ uint32_t tt_root(const TkList &L)
 {
-    return L.P > 1 ? uint32_t(L.win[TC_M + L.tid]) : (L.lo < L.k ? L.lo : kNoSlot);
+    return L.P > 1 ? uint32_t(L.win[L.st + L.tid]) : (L.lo < L.k ? L.lo : kNoSlot);
 }
 
 __device__ __noinline__ void tt_build(const TkList &L)
 {
     for (uint32_t x = L.P - 1; x >= 1; --x)
-        L.win[x * TC_M + L.tid] = uint8_t(tt_pick(L, tt_node(L, 2 * x), tt_node(L, 2 * x + 1)));
+        L.win[x * L.st + L.tid] = uint8_t(tt_pick(L, tt_node(L, 2 * x), tt_node(L, 2 * x + 1)));
 }
 
 // Slot `slot` now holds (dv, iv): replay the matches on its path to the root, carrying
@@ -328,7 +329,7 @@ __device__ __forceinline__ uint32_t tt_update(const TkList &L, uint32_t slot, fl
         const uint32_t sib = cur ^ 1u;
         const uint32_t ws = tt_node(L, sib);
         if (ws != kNoSlot) {
-            const float ds = L.d[ws * TC_M + t];
+            const float ds = L.d[ws * L.st + t];
             bool sw;
             if (ds != wd) sw = ds > wd;
             else sw = L.exact ? L.id[ws] > wi : sib < cur;  // CompGT: the lower slot
@@ -339,7 +340,7 @@ __device__ __forceinline__ uint32_t tt_update(const TkList &L, uint32_t slot, fl
             }
         }
         cur >>= 1;
-        L.win[cur * TC_M + t] = uint8_t(w);
+        L.win[cur * L.st + t] = uint8_t(w);
     }
     return w;
 }
@@ -372,14 +373,14 @@ __device__ __forceinline__ float tk_offer(const TkList &L, TkState &S, float dis
         if (S.cnt < L.k) {
             if (dist > S.topdist) { S.topdist = dist; S.toppos = S.cnt; }
             S.lmax = fmaxf(S.lmax, dist);
-            L.d[S.cnt * TC_M + t] = dist;
+            L.d[S.cnt * L.st + t] = dist;
             L.id[S.cnt] = id;
             if (++S.cnt == L.k) tk_groups_build(L, S);
         } else if (dist < S.topdist) {
             // overwrite toppos; the rescan over slots 1..k-1 starts from topk[0] read before the write
             const float old0 = L.d[t];
             const uint32_t p = S.toppos;
-            L.d[p * TC_M + t] = dist;
+            L.d[p * L.st + t] = dist;
             L.id[p] = id;
             if (p >= 1) {
                 const uint32_t gp = (p - 1) / TK_GROUP;
@@ -405,19 +406,19 @@ __device__ __forceinline__ float tk_offer(const TkList &L, TkState &S, float dis
     }
     // exact: replace the largest key; a later id never wins a tie
     if (S.cnt < L.k) {
-        L.d[S.cnt * TC_M + t] = dist;
+        L.d[S.cnt * L.st + t] = dist;
         L.id[S.cnt] = id;
         if (++S.cnt == L.k) {
             tt_build(L);
             S.toppos = tt_root(L);
-            S.topdist = L.d[S.toppos * TC_M + t];
+            S.topdist = L.d[S.toppos * L.st + t];
         }
     } else if (dist < S.topdist) {
         const uint32_t r = S.toppos;
-        L.d[r * TC_M + t] = dist;
+        L.d[r * L.st + t] = dist;
         L.id[r] = id;
         S.toppos = tt_update(L, r, dist, id);
-        S.topdist = L.d[S.toppos * TC_M + t];
+        S.topdist = L.d[S.toppos * L.st + t];
     }
     return S.cnt < L.k ? kInf : S.topdist;
 }
@@ -591,6 +592,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             L.lo = a.exact ? 0u : 1u;
             L.P = 1;
             while (L.P < k - L.lo) L.P <<= 1;
+            L.st = TC_M;
             TkState S{0u, 0u, -3.402823466e38f, -3.402823466e38f, {}, {}};
             uint32_t qlen = 0;  // queued flagged candidates, in id order
             uint2 *const lst = a.lists + size_t(blockIdx.x) * a.cap * TC_M + tid;  // entry e at lst[e * 128]
@@ -728,23 +730,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// Merge of one query tile (thread t = query t): the list its first segment left (slot order,
-// with the replay state), then the candidates recorded by the segments that continue its scan,
-// in id order, through the same admission rule; then the output sorted by (dist, id)
-// (CompGT.cpp:107-124).  Shared memory: the list [k][128], the ids for the sort [k][128] and the
-// tournament tree [128][128].
+// Merge, one block of 32 queries (a quarter of a query tile; thread t = one query): the list
+// the tile's first segment left (slot order, with the replay state), then the candidates
+// recorded by the segments that continue its scan, in id order, through the same admission
+// rule; then the output sorted by (dist, id) (CompGT.cpp:107-124).  Shared memory: the list
+// [k][32], the ids for the sort [k][32] and the tournament tree [128][32].
+constexpr uint32_t TC_MB = 32;
 template <int MET>
-__global__ void __launch_bounds__(TC_M) gt_tc_merge_kernel(TcArgs a)
+__global__ void __launch_bounds__(TC_MB) gt_tc_merge_kernel(TcArgs a)
 {
     extern __shared__ __align__(16) uint8_t msmem[];
     const uint32_t k = a.k;
     float *tk_d = reinterpret_cast<float *>(msmem);
-    uint32_t *sid = reinterpret_cast<uint32_t *>(tk_d + size_t(k) * TC_M);
-    uint8_t *win = reinterpret_cast<uint8_t *>(sid + size_t(k) * TC_M);
+    uint32_t *sid = reinterpret_cast<uint32_t *>(tk_d + size_t(k) * TC_MB);
+    uint8_t *win = reinterpret_cast<uint8_t *>(sid + size_t(k) * TC_MB);
     const int tid = threadIdx.x;
-    const uint32_t li = blockIdx.x;
+    const uint32_t li = blockIdx.x / (TC_M / TC_MB);
+    const uint32_t r = (blockIdx.x % (TC_M / TC_MB)) * TC_MB + tid;  // the query's row in its tile
     const uint32_t qt = a.tile_list ? a.tile_list[li] : li;
-    const uint32_t q = qt * TC_M + tid;
+    const uint32_t q = qt * TC_M + r;
     if (q >= a.nq || *a.err) return;  // padding query, or the scan did not finish
     TkList L;
     L.d = tk_d;
@@ -756,9 +760,10 @@ __global__ void __launch_bounds__(TC_M) gt_tc_merge_kernel(TcArgs a)
     L.lo = a.exact ? 0u : 1u;
     L.P = 1;
     while (L.P < k - L.lo) L.P <<= 1;
+    L.st = TC_MB;
     const uint4 st = a.state[q];
     TkState S{st.x < k ? st.x : k, st.y, __uint_as_float(st.z), __uint_as_float(st.w), {}, {}};
-    for (uint32_t l = 0; l < S.cnt; ++l) tk_d[l * TC_M + tid] = a.out_dists[size_t(q) * k + l];
+    for (uint32_t l = 0; l < S.cnt; ++l) tk_d[l * TC_MB + tid] = a.out_dists[size_t(q) * k + l];
     if (S.cnt == k) {
         if (a.exact) tt_build(L);
         else tk_groups_build(L, S);
@@ -766,14 +771,14 @@ __global__ void __launch_bounds__(TC_M) gt_tc_merge_kernel(TcArgs a)
     // the CTAs whose ranges start inside this tile's scan, in order
     const uint2 cr = a.conts[li];
     for (uint32_t c = cr.x; c < cr.x + cr.y; ++c) {
-        const uint32_t n = a.list_n[size_t(c) * TC_M + tid];
+        const uint32_t n = a.list_n[size_t(c) * TC_M + r];
         if (n > a.cap) {
             atomicExch(a.ovf + li, 1u);  // recorded candidates lost: the host reruns this tile unsplit
             return;
         }
-        // entry-major lists: the warp's threads read one 256-byte line per entry index; the
-        // next 16 entries load while the current 16 are replayed
-        const uint2 *lst = a.lists + size_t(c) * a.cap * TC_M + tid;
+        // entry-major lists: the warp reads one 256-byte span per entry index; the next 16
+        // entries load while the current 16 are replayed
+        const uint2 *lst = a.lists + size_t(c) * a.cap * TC_M + r;
         uint2 x[16], y[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) x[j] = uint32_t(j) < n ? lst[size_t(j) * TC_M] : make_uint2(0, 0);
@@ -789,29 +794,29 @@ __global__ void __launch_bounds__(TC_M) gt_tc_merge_kernel(TcArgs a)
         }
     }
     if (S.cnt != k) return;  // n >= k is checked by the caller
-    for (uint32_t l = 0; l < k; ++l) sid[l * TC_M + tid] = L.id[l];
+    for (uint32_t l = 0; l < k; ++l) sid[l * TC_MB + tid] = L.id[l];
     for (uint32_t i = 1; i < k; ++i) {
-        const float dv = tk_d[i * TC_M + tid];
-        const uint32_t iv = sid[i * TC_M + tid];
+        const float dv = tk_d[i * TC_MB + tid];
+        const uint32_t iv = sid[i * TC_MB + tid];
         int32_t j = int32_t(i) - 1;
         while (j >= 0) {
-            const float dj = tk_d[j * TC_M + tid];
-            const uint32_t ij = sid[j * TC_M + tid];
+            const float dj = tk_d[j * TC_MB + tid];
+            const uint32_t ij = sid[j * TC_MB + tid];
             if (!(dj > dv || (dj == dv && ij > iv))) break;
-            tk_d[(j + 1) * TC_M + tid] = dj;
-            sid[(j + 1) * TC_M + tid] = ij;
+            tk_d[(j + 1) * TC_MB + tid] = dj;
+            sid[(j + 1) * TC_MB + tid] = ij;
             --j;
         }
-        tk_d[(j + 1) * TC_M + tid] = dv;
-        sid[(j + 1) * TC_M + tid] = iv;
+        tk_d[(j + 1) * TC_MB + tid] = dv;
+        sid[(j + 1) * TC_MB + tid] = iv;
     }
     for (uint32_t l = 0; l < k; ++l) {
-        L.id[l] = sid[l * TC_M + tid];
-        a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_M + tid]);
+        L.id[l] = sid[l * TC_MB + tid];
+        a.out_dists[size_t(q) * k + l] = output_dist<MET>(tk_d[l * TC_MB + tid]);
     }
 }
 
-static size_t gt_tc_merge_smem(uint32_t k) { return size_t(k) * TC_M * 8 + TC_M * TC_M; }
+static size_t gt_tc_merge_smem(uint32_t k) { return size_t(k) * TC_MB * 8 + TC_M * TC_MB; }
 
 // u8/i8/u4 rows -> bf16 K-major rows (K = padded element count, 64 or 128) and int32 squared
 // norms.  One thread per 8 elements: one 16-byte store each, the row's norm summed over its
@@ -1123,10 +1128,10 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
     auto launch = [&](const TcArgs &x, uint32_t ctas, uint32_t tiles) {
         if (metric == NBPG_L2) {
             gt_tc_kernel<M_L2><<<ctas, TC_THREADS, smem, st>>>(mA, mB, x);
-            gt_tc_merge_kernel<M_L2><<<tiles, TC_M, msmem, st>>>(x);
+            gt_tc_merge_kernel<M_L2><<<tiles * (TC_M / TC_MB), TC_MB, msmem, st>>>(x);
         } else {
             gt_tc_kernel<M_IP><<<ctas, TC_THREADS, smem, st>>>(mA, mB, x);
-            gt_tc_merge_kernel<M_IP><<<tiles, TC_M, msmem, st>>>(x);
+            gt_tc_merge_kernel<M_IP><<<tiles * (TC_M / TC_MB), TC_MB, msmem, st>>>(x);
         }
         return cudaGetLastError();
     };
