@@ -10,13 +10,17 @@
 // tcgen05.mma .kind::i8 for sm_103a ("Feature '.kind::i8' not supported on .target 'sm_103a'"),
 // so the bf16 form is the exact tensor path on this part.
 //
-// One CTA owns 128 queries (the MMA's M = the 128 TMEM lanes) and walks the base in
-// id order in tiles of 128 rows (N).  Warp 4 loads tiles with TMA (128-byte swizzle)
-// into a ring of 2-4 stages; warp 5 issues tcgen05.mma into one of four TMEM accumulators;
-// warps 0-3 are the epilogue: thread t reads lane t (query t) of the accumulator with
-// tcgen05.ld and replays the admission rule for its query over the tile's ids in order
-// (CompGT's replace-max with its stale read, or an exact sorted top-k).  All waits on
-// mbarriers are bounded; on a timeout the kernel records an error and tears down.
+// A CTA works on 128 queries at a time (the MMA's M = the 128 TMEM lanes) and walks base
+// tiles of 128 rows (N) in id order.  Warp 4 loads tiles with TMA (128-byte swizzle) into a
+// ring of 2-4 stages; warp 5 issues tcgen05.mma into one of four TMEM accumulators; warps
+// 0-3 are the epilogue: thread t reads lane t (query t) of the accumulator with tcgen05.ld
+// and replays the admission rule for its query over the tile's ids in order (CompGT's
+// replace-max with its stale read, or an exact sorted top-k).  The (query tile, base tile)
+// steps are cut into one range per SM, so a tile's scan can span CTAs: the CTA holding its
+// start replays and publishes its survivor bound, the others record the candidates below
+// that bound, and gt_tc_merge_kernel replays the records in id order after the first
+// segment's list.  All waits on mbarriers are bounded; on a timeout the kernel records an
+// error and tears down.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
