@@ -129,7 +129,9 @@ typedef struct nbpg_search_params {
  *
  * nbpg_search: host buffers; copies in and out on the index stream and returns when done.
  * nbpg_search_device: device buffers (start_points stays a host array); enqueued on
- *   `stream` (a cudaStream_t, NULL = the index stream); returns after enqueueing. */
+ *   `stream` (a cudaStream_t, NULL = the index stream); returns after enqueueing.  Calls on
+ *   different streams keep separate work counters and scratch (up to 16 streams per index), so
+ *   they may run on the device at the same time. */
 nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *params,
                         const uint32_t *Ls, const uint32_t *ks, const uint32_t *start_points, uint32_t n_start,
                         uint32_t k_stride, uint32_t *out_ids, float *out_dists, uint32_t *out_count,
@@ -138,6 +140,23 @@ nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t 
                                const uint32_t *d_Ls, const uint32_t *d_ks, const uint32_t *start_points,
                                uint32_t n_start, uint32_t k_stride, uint32_t *d_out_ids, float *d_out_dists,
                                uint32_t *d_out_count, uint32_t *d_out_visited, uint32_t *d_out_cmps, void *stream);
+
+/* Asynchronous host call: as nbpg_search with uniform L and k and every host buffer pinned
+ * (cudaHostAlloc / cudaHostRegister; NBPG_ERR_INVALID_ARG otherwise), enqueued on `stream`
+ * (NULL = the index stream) and returning before the work is done: the results are in the
+ * caller's buffers once the stream gets there (cudaStreamSynchronize, an event).  The kernels
+ * read the query rows from, and write the results into, the pinned buffers through their
+ * device mappings where the rows need no padding, else staging copies run in the same stream
+ * order.  out_status (pinned, may be NULL) receives 1 when a query was rejected on the device,
+ * 0 otherwise.  Each distinct call (buffers, parameters, start points) is captured once as a
+ * CUDA graph with its own staging and scratch (the first call runs synchronously), so calls
+ * with different buffers may be in flight on different streams at the same time; calls that
+ * share buffers belong on one stream.  Up to 8 distinct calls are kept per index.  No
+ * counterpart in the reference. */
+nbpg_status nbpg_search_async(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *params,
+                              const uint32_t *start_points, uint32_t n_start, uint32_t k_stride, uint32_t *out_ids,
+                              float *out_dists, uint32_t *out_count, uint32_t *out_visited, uint32_t *out_cmps,
+                              uint32_t *out_status, void *stream);
 
 /* As nbpg_search_device (uniform L and k), plus d_out_adj_words (nq entries, may be NULL): per
  * query, the 32-bit adjacency words the search read, 1 + the neighbours scanned for every node it

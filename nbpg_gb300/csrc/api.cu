@@ -66,6 +66,10 @@ extern "C" nbpg_status nbpg_index_destroy(nbpg_index *idx)
     idx->scratch.release();
     host_call_release(idx->host_call);
     idx->host_call = nullptr;
+    for (nbpg::HostCall *c : idx->async_calls) host_call_release(c);
+    idx->async_calls.clear();
+    for (auto &e : idx->stream_scratch) e.second->release();
+    idx->stream_scratch.clear();
     for (DevBuf *b : {&idx->qbuf, &idx->obuf, &idx->ghash, &idx->order_buf}) b->release();
     if (idx->stream) cudaStreamDestroy(idx->stream);
     delete idx;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -142,7 +143,11 @@ struct nbpg_index {
     size_t smem_optin = 0;
     // scratch
     nbpg::SearchScratch scratch;  // used by the index's own search calls
+    // device-buffer searches, one scratch per caller stream, so that calls on different streams
+    // may run on the device at the same time (the index stream's calls use `scratch`)
+    std::vector<std::pair<cudaStream_t, std::unique_ptr<nbpg::SearchScratch>>> stream_scratch;
     nbpg::DevBuf qbuf, obuf, ghash, order_buf;  // host-API staging; build-time visited filters
     nbpg::HostCall *host_call = nullptr;        // the last pinned-buffer host call, as a CUDA graph
+    std::vector<nbpg::HostCall *> async_calls;  // nbpg_search_async's graphs, one per distinct call
     std::mutex mu;
 };

@@ -475,6 +475,30 @@ nbpg_status search_device_impl(nbpg_index *idx, SearchScratch &sc, const void *d
 
 using namespace nbpg;
 
+namespace nbpg {
+
+// The scratch of device-buffer searches on stream st (NULL: the index stream).  Calls on one
+// stream run in order and share it; calls on different streams get their own, so their launches
+// may overlap on the device.  Streams are told apart by handle only: a destroyed stream's entry
+// passes to a later stream with the same handle, which cannot overlap with the destroyed one.
+static SearchScratch &scratch_for(nbpg_index *idx, cudaStream_t st)
+{
+    if (!st || st == idx->stream) return idx->scratch;
+    for (auto &e : idx->stream_scratch)
+        if (e.first == st) return *e.second;
+    constexpr size_t kMaxStreams = 16;
+    if (idx->stream_scratch.size() >= kMaxStreams) {
+        // drop the oldest entry once nothing can still be using it
+        cudaDeviceSynchronize();
+        idx->stream_scratch.front().second->release();
+        idx->stream_scratch.erase(idx->stream_scratch.begin());
+    }
+    idx->stream_scratch.emplace_back(st, std::make_unique<SearchScratch>());
+    return *idx->stream_scratch.back().second;
+}
+
+}  // namespace nbpg
+
 extern "C" nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries, uint32_t nq,
                                           const nbpg_search_params *params, const uint32_t *d_Ls,
                                           const uint32_t *d_ks, const uint32_t *start_points, uint32_t n_start,
@@ -485,9 +509,9 @@ extern "C" nbpg_status nbpg_search_device(nbpg_index *idx, const void *d_queries
     if (!idx) { set_error("null index"); return NBPG_ERR_INVALID_ARG; }
     std::lock_guard<std::mutex> g(idx->mu);
     cudaSetDevice(idx->desc.device);
-    return search_device_impl(idx, idx->scratch, d_queries, nq, params, d_Ls, d_ks, start_points, n_start, k_stride,
-                              d_out_ids,
-                              d_out_dists, d_out_count, d_out_visited, d_out_cmps, static_cast<cudaStream_t>(stream));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return search_device_impl(idx, scratch_for(idx, st), d_queries, nq, params, d_Ls, d_ks, start_points, n_start,
+                              k_stride, d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps, st);
 }
 
 extern "C" nbpg_status nbpg_search_device_adj(nbpg_index *idx, const void *d_queries, uint32_t nq,
@@ -501,9 +525,10 @@ extern "C" nbpg_status nbpg_search_device_adj(nbpg_index *idx, const void *d_que
     cudaSetDevice(idx->desc.device);
     SearchEmit em;
     em.d_adj = d_out_adj_words;
-    return search_device_impl(idx, idx->scratch, d_queries, nq, params, nullptr, nullptr, start_points, n_start,
-                              k_stride, d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps,
-                              static_cast<cudaStream_t>(stream), &em);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return search_device_impl(idx, scratch_for(idx, st), d_queries, nq, params, nullptr, nullptr, start_points,
+                              n_start, k_stride, d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps, st,
+                              &em);
 }
 
 extern "C" nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_queries, uint32_t nq,
@@ -518,9 +543,9 @@ extern "C" nbpg_status nbpg_search_device_sp(nbpg_index *idx, const void *d_quer
     SearchTarget tgt;
     tgt.d_sp = d_start_points;
     tgt.sp_stride = sp_stride;
-    return search_device_impl(idx, idx->scratch, d_queries, nq, params, nullptr, nullptr, nullptr, 0, k_stride,
-                              d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps,
-                              static_cast<cudaStream_t>(stream), nullptr, &tgt);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return search_device_impl(idx, scratch_for(idx, st), d_queries, nq, params, nullptr, nullptr, nullptr, 0, k_stride,
+                              d_out_ids, d_out_dists, d_out_count, d_out_visited, d_out_cmps, st, nullptr, &tgt);
 }
 
 namespace nbpg {
@@ -542,6 +567,7 @@ struct HostCall {
     SearchScratch sc;
     DevBuf qbuf, obuf;
     uint32_t *err_host = nullptr;  // pinned
+    uint32_t *status = nullptr;    // nbpg_search_async: the caller's pinned error word (or null)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     // zero-copy form: the kernels read the queries from, and write the results into, the
@@ -612,6 +638,8 @@ static nbpg_status enqueue_host_call(nbpg_index *idx, HostCall *hc, cudaStream_t
                                                  hc->dev_dists, hc->dev_cnt, hc->dev_vis, hc->dev_cmps, st);
         if (s != NBPG_OK) return s;
         NBPG_CUDA_TRY(cudaMemcpyAsync(hc->err_host, hc->sc.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+        if (hc->status)
+            NBPG_CUDA_TRY(cudaMemcpyAsync(hc->status, hc->sc.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
         return NBPG_OK;
     }
     uint8_t *dq = hc->qbuf.as<uint8_t>();
@@ -632,6 +660,80 @@ static nbpg_status enqueue_host_call(nbpg_index *idx, HostCall *hc, cudaStream_t
     if (hc->vis) NBPG_CUDA_TRY(cudaMemcpyAsync(hc->vis, d_v, nq * 4, cudaMemcpyDeviceToHost, st));
     if (hc->cmps) NBPG_CUDA_TRY(cudaMemcpyAsync(hc->cmps, d_m, nq * 4, cudaMemcpyDeviceToHost, st));
     NBPG_CUDA_TRY(cudaMemcpyAsync(hc->err_host, hc->sc.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+    if (hc->status)
+        NBPG_CUDA_TRY(cudaMemcpyAsync(hc->status, hc->sc.queue.as<uint32_t>() + 2, 4, cudaMemcpyDeviceToHost, st));
+    return NBPG_OK;
+}
+
+// Whether hc was captured for exactly this call: the same arguments and, for the zero-copy
+// form, the same device mappings of the buffers.
+static bool host_call_matches(const HostCall *hc, const void *queries, uint32_t nq, const nbpg_search_params &P,
+                              const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *ids, float *dists,
+                              uint32_t *cnt, uint32_t *vis, uint32_t *cmps)
+{
+    if (!hc || !hc->exec || !hc->same(queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps)) return false;
+    if (!hc->direct) return true;
+    const void *dq = nullptr;
+    uint32_t *di = nullptr, *dc = nullptr, *dv = nullptr, *dm = nullptr;
+    float *dd = nullptr;
+    return mapped(queries, &dq) && mapped(ids, &di) && mapped(dists, &dd) && mapped(cnt, &dc) && mapped(vis, &dv) &&
+           mapped(cmps, &dm) && dq == hc->dev_queries && di == hc->dev_ids && dd == hc->dev_dists &&
+           dc == hc->dev_cnt && dv == hc->dev_vis && dm == hc->dev_cmps;
+}
+
+// A new HostCall for this call, its buffers checked for the zero-copy form, staging sized
+static nbpg_status host_call_new(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params &P,
+                                 const uint32_t *sp, uint32_t nsp, uint32_t k_stride, uint32_t *ids, float *dists,
+                                 uint32_t *cnt, uint32_t *vis, uint32_t *cmps, HostCall **out)
+{
+    auto *hc = new HostCall();
+    *out = hc;
+    hc->queries = queries;
+    hc->nq = nq;
+    hc->k_stride = k_stride;
+    hc->P = P;
+    hc->sp.assign(sp, sp + nsp);
+    hc->ids = ids;
+    hc->dists = dists;
+    hc->cnt = cnt;
+    hc->vis = vis;
+    hc->cmps = cmps;
+    nbpg_status s;
+    hc->direct = idx->row_bytes == idx->row_stride && mapped(queries, &hc->dev_queries) && mapped(ids, &hc->dev_ids) &&
+                 mapped(dists, &hc->dev_dists) && mapped(cnt, &hc->dev_cnt) && mapped(vis, &hc->dev_vis) &&
+                 mapped(cmps, &hc->dev_cmps);
+    if (!hc->direct && ((s = hc->qbuf.ensure(size_t(nq) * idx->row_stride)) != NBPG_OK ||
+                        (s = hc->obuf.ensure(size_t(nq) * (size_t(k_stride) * 8 + 12) + 64)) != NBPG_OK))
+        return s;
+    NBPG_CUDA_TRY(cudaHostAlloc(&hc->err_host, 4, cudaHostAllocDefault));
+    *hc->err_host = 0;
+    return NBPG_OK;
+}
+
+// Runs the call once on the index stream (its results are the call's), then captures the same
+// work as a graph for the calls that repeat it.  *err: the call's rejection word.  A failed
+// capture leaves hc without a graph.
+static nbpg_status host_call_first(nbpg_index *idx, HostCall *hc, uint32_t *err)
+{
+    cudaStream_t st = idx->stream;
+    nbpg_status s;
+    if ((s = enqueue_host_call(idx, hc, st)) != NBPG_OK) return s;
+    NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+    *err = *hc->err_host;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        s = enqueue_host_call(idx, hc, st);
+        cudaError_t e2 = cudaStreamEndCapture(st, &hc->graph);
+        if (e2 != cudaSuccess) e = e2;
+    }
+    if (s == NBPG_OK && e == cudaSuccess) e = cudaGraphInstantiate(&hc->exec, hc->graph, 0);
+    if (s != NBPG_OK || e != cudaSuccess) {
+        cudaGetLastError();
+        if (hc->exec) cudaGraphExecDestroy(hc->exec);
+        if (hc->graph) cudaGraphDestroy(hc->graph);
+        hc->exec = nullptr;
+        hc->graph = nullptr;
+    }
     return NBPG_OK;
 }
 
@@ -643,56 +745,19 @@ static nbpg_status host_call_graphed(nbpg_index *idx, const void *queries, uint3
 {
     cudaStream_t st = idx->stream;
     HostCall *hc = idx->host_call;
-    bool reuse = hc && hc->exec && hc->same(queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps);
-    if (reuse && hc->direct) {
-        // the buffers' device mappings are the ones the graph was captured with
-        const void *dq = nullptr;
-        uint32_t *di = nullptr, *dc = nullptr, *dv = nullptr, *dm = nullptr;
-        float *dd = nullptr;
-        reuse = mapped(queries, &dq) && mapped(ids, &di) && mapped(dists, &dd) && mapped(cnt, &dc) &&
-                mapped(vis, &dv) && mapped(cmps, &dm) && dq == hc->dev_queries && di == hc->dev_ids &&
-                dd == hc->dev_dists && dc == hc->dev_cnt && dv == hc->dev_vis && dm == hc->dev_cmps;
-    }
-    if (!reuse) {
+    if (!host_call_matches(hc, queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps)) {
         host_call_release(hc);
-        idx->host_call = hc = new HostCall();
-        hc->queries = queries;
-        hc->nq = nq;
-        hc->k_stride = k_stride;
-        hc->P = P;
-        hc->sp.assign(sp, sp + nsp);
-        hc->ids = ids;
-        hc->dists = dists;
-        hc->cnt = cnt;
-        hc->vis = vis;
-        hc->cmps = cmps;
-        nbpg_status s;
-        hc->direct = idx->row_bytes == idx->row_stride && mapped(queries, &hc->dev_queries) &&
-                     mapped(ids, &hc->dev_ids) && mapped(dists, &hc->dev_dists) && mapped(cnt, &hc->dev_cnt) &&
-                     mapped(vis, &hc->dev_vis) && mapped(cmps, &hc->dev_cmps);
-        if (!hc->direct &&
-            ((s = hc->qbuf.ensure(size_t(nq) * idx->row_stride)) != NBPG_OK ||
-             (s = hc->obuf.ensure(size_t(nq) * (size_t(k_stride) * 8 + 12) + 64)) != NBPG_OK))
-            return s;
-        NBPG_CUDA_TRY(cudaHostAlloc(&hc->err_host, 4, cudaHostAllocDefault));
-        *hc->err_host = 0;
-        // this call, uncaptured (sizes the scratch, stages the start points, plans the launches)
-        if ((s = enqueue_host_call(idx, hc, st)) != NBPG_OK) return s;
-        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
-        const uint32_t err = *hc->err_host;
-        // the same work captured for the calls that repeat it
-        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            s = enqueue_host_call(idx, hc, st);
-            cudaError_t e2 = cudaStreamEndCapture(st, &hc->graph);
-            if (e2 != cudaSuccess) e = e2;
-        }
-        if (s == NBPG_OK && e == cudaSuccess) e = cudaGraphInstantiate(&hc->exec, hc->graph, 0);
-        if (s != NBPG_OK || e != cudaSuccess) {  // no graph: later calls take the plain path
-            cudaGetLastError();
+        idx->host_call = nullptr;
+        nbpg_status s = host_call_new(idx, queries, nq, P, sp, nsp, k_stride, ids, dists, cnt, vis, cmps, &hc);
+        if (s != NBPG_OK) {
             host_call_release(hc);
-            idx->host_call = nullptr;
+            return s;
         }
+        uint32_t err = 0;
+        s = host_call_first(idx, hc, &err);
+        if (s != NBPG_OK || !hc->exec) host_call_release(hc);  // no graph: later calls take the plain path
+        else idx->host_call = hc;
+        if (s != NBPG_OK) return s;
         if (err) {
             set_error("a query was rejected on the device (k > L or L above the planned maximum)");
             return NBPG_ERR_INVALID_ARG;
@@ -710,6 +775,70 @@ static nbpg_status host_call_graphed(nbpg_index *idx, const void *queries, uint3
 }
 
 }  // namespace nbpg
+
+// Asynchronous pinned-buffer search: each distinct call (buffers, parameters, start points) has
+// its own graph, staging and scratch, kept in a small per-index cache, so calls with different
+// buffers may be in flight on different streams at the same time.
+extern "C" nbpg_status nbpg_search_async(nbpg_index *idx, const void *queries, uint32_t nq,
+                                         const nbpg_search_params *P, const uint32_t *start_points, uint32_t n_start,
+                                         uint32_t k_stride, uint32_t *out_ids, float *out_dists, uint32_t *out_count,
+                                         uint32_t *out_visited, uint32_t *out_cmps, uint32_t *out_status,
+                                         void *stream)
+{
+    using namespace nbpg;
+    if (!idx || !P || !queries || !out_ids || !start_points) { set_error("null argument"); return NBPG_ERR_INVALID_ARG; }
+    NBPG_CHECK_ARG(n_start >= 1 && n_start <= 256, "need 1..256 start points");
+    std::lock_guard<std::mutex> g(idx->mu);
+    NBPG_CUDA_TRY(cudaSetDevice(idx->desc.device));
+    if (nq == 0) return NBPG_OK;
+    NBPG_CHECK_ARG(pinned(queries) && pinned(out_ids) && pinned(out_dists) && pinned(out_count) &&
+                       pinned(out_visited) && pinned(out_cmps) && pinned(out_status),
+                   "nbpg_search_async needs pinned host buffers (cudaHostAlloc or cudaHostRegister)");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : idx->stream;
+    HostCall *hc = nullptr;
+    for (HostCall *c : idx->async_calls)
+        if (c->status == out_status && host_call_matches(c, queries, nq, *P, start_points, n_start, k_stride, out_ids,
+                                                         out_dists, out_count, out_visited, out_cmps)) {
+            hc = c;
+            break;
+        }
+    if (!hc) {
+        // a new call: set up once the caller's stream has drained, run it once on the index stream
+        // (its results are this call's, ready before the caller's stream gets to them), capture it
+        NBPG_CUDA_TRY(cudaStreamSynchronize(st));
+        constexpr size_t kMaxCalls = 8;
+        if (idx->async_calls.size() >= kMaxCalls) {
+            cudaDeviceSynchronize();  // the oldest call's graph may still be in flight on some stream
+            host_call_release(idx->async_calls.front());
+            idx->async_calls.erase(idx->async_calls.begin());
+        }
+        nbpg_status s = host_call_new(idx, queries, nq, *P, start_points, n_start, k_stride, out_ids, out_dists,
+                                      out_count, out_visited, out_cmps, &hc);
+        if (s != NBPG_OK) {
+            host_call_release(hc);
+            return s;
+        }
+        hc->status = out_status;
+        uint32_t err = 0;
+        s = host_call_first(idx, hc, &err);
+        if (s != NBPG_OK || !hc->exec) {
+            host_call_release(hc);
+            if (s == NBPG_OK) {
+                set_error("nbpg_search_async: the call could not be captured as a graph");
+                s = NBPG_ERR_CUDA;
+            }
+            return s;
+        }
+        idx->async_calls.push_back(hc);
+        if (err) {
+            set_error("a query was rejected on the device (k > L or L above the planned maximum)");
+            return NBPG_ERR_INVALID_ARG;
+        }
+        return NBPG_OK;
+    }
+    NBPG_CUDA_TRY(cudaGraphLaunch(hc->exec, st));
+    return NBPG_OK;
+}
 
 extern "C" nbpg_status nbpg_search(nbpg_index *idx, const void *queries, uint32_t nq, const nbpg_search_params *P,
                                    const uint32_t *Ls, const uint32_t *ks, const uint32_t *start_points,
