@@ -13,9 +13,12 @@ A step = one strict search of all 10k queries at that L (k=10, cut=1.35, start
 point 0) with the launch nbpg_search_autotune picks (the plain one-query-per-block
 kernel or the persistent kernel pulling queries from a device queue, their lane
 widths and CTA sizes; every candidate returns identical results).
-`value` is device-resident QPS over the timed steps (CUDA events on the launching
-stream); `e2e` is the same search through the C ABI (nbpg_search) from pinned host
-queries to host results.  With N ranks (torchrun), each rank searches its own replica
+`value` is device-resident QPS over the timed steps with two requests in flight
+(`--in-flight`; step i on stream i mod 2 with that stream's own output buffers, CUDA
+events from the first step's start to the last step's end); `e2e` is the same search
+through the C ABI (nbpg_search_async, two requests in flight) from pinned host queries
+to pinned host results.  The one-in-flight rates (the steps back to back on one stream;
+synchronous nbpg_search calls) are reported beside them.  With N ranks (torchrun), each rank searches its own replica
 of the index, the job's time is the slowest rank's, and rank 0 prints the line.  The index (128 MB vectors + 272 MB graph) is larger than
 L2, so no flush is needed between steps.
 
@@ -777,6 +780,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--in-flight", type=int, default=2,
+                    help="search requests in flight in the timed steps (one stream and buffer set each)")
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
@@ -941,30 +946,68 @@ def main():
     # parity of the timed path with the host-API result at the operating point
     assert np.array_equal(o_ids.cpu().numpy().view(np.uint32), res_op.ids), "device-path results differ"
 
+    # one request in flight: the steps back to back on one stream, each timed by its own events
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    for e0, e1 in evs:
+        e0.record(stream)
+        dev_search()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    one_total_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / 1e3, dist)
+    value_one = job_rate(nq * args.steps, world, one_total_s)
+
+    # `value`: args.in_flight requests in flight, step i on stream i mod in_flight with that
+    # stream's own output buffers (the library keeps separate scratch per stream), so one
+    # request's launch tail and the next request's launch overlap on the device
+    F = max(1, args.in_flight)
+    streams = [stream] + [torch.cuda.Stream() for _ in range(F - 1)]
+    outs = [(o_ids, o_d, o_c, o_v, o_m)] + [tuple(torch.empty_like(t) for t in (o_ids, o_d, o_c, o_v, o_m))
+                                            for _ in range(F - 1)]
+
+    def dev_search_on(i):
+        oi, od, oc, ov, om = outs[i]
+        idx.search_device(qdev.data_ptr(), nq, qp, oi.data_ptr(), k, od.data_ptr(), oc.data_ptr(), ov.data_ptr(),
+                          om.data_ptr(), launch=tuned, stream=streams[i].cuda_stream)
+
+    for _ in range(args.warmup):
+        for i in range(F):
+            dev_search_on(i)
+    torch.cuda.synchronize()
+    for i in range(F):
+        assert np.array_equal(outs[i][0].cpu().numpy().view(np.uint32), res_op.ids), "in-flight results differ"
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(F)]
     with Clocks(local) as clk:
         clk.wait_ready()
         t0 = time.perf_counter()
-        for e0, e1 in evs:
-            e0.record(stream)
-            dev_search()
-            e1.record(stream)
+        start.record(streams[0])
+        for st_ in streams[1:]:
+            st_.wait_event(start)
+        for i in range(args.steps):
+            dev_search_on(i % F)
+        for e, st_ in zip(ends, streams):
+            e.record(st_)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         # the timed steps last milliseconds, shorter than the sampling period: keep the same search
         # running for half a second more (untimed) so the clock record covers this load
         t1 = time.perf_counter()
         while time.perf_counter() - t1 < 0.5:
-            for _ in range(20):
-                dev_search()
+            for i in range(20):
+                dev_search_on(i % F)
             torch.cuda.synchronize()
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_s = max_over_ranks(sum(step_ms) / 1e3, dist)
+    total_s = max_over_ranks(max(start.elapsed_time(e) for e in ends) / 1e3, dist)
+    for i in range(F):
+        assert np.array_equal(outs[i][0].cpu().numpy().view(np.uint32), res_op.ids), "in-flight results differ"
     value = job_rate(nq * args.steps, world, total_s)
     ms_step = 1e3 * total_s / args.steps
+    log(f"[bench] search: {value / 1e6:.2f} M queries/s with {F} requests in flight, {value_one / 1e6:.2f} M with one")
 
     # the two kernel forms at the same L: plain (one query per block, default launch) and
     # the batched persistent kernel with its default launch
@@ -1016,7 +1059,7 @@ def main():
     # FAST mode (exact visited hash, several expansions per step): QPS at the same recall target
     try:
         fast = time_fast(idx, q, qdev, gi, gd, gei, ged, k, stream)
-        fast["over_strict_tuned"] = fast["qps"] / value
+        fast["over_strict_tuned"] = fast["qps"] / value_one
         log(f"[bench] FAST mode: L={fast['L']} recall {fast['recall@10']} {fast['qps']:.3g} QPS "
             f"({fast['over_strict_tuned']:.2f}x strict), launch {fast['launch']}")
     except Exception as exc:  # a secondary measurement: reported in the line, not fatal
@@ -1046,9 +1089,43 @@ def main():
     t = time.perf_counter()
     for _ in range(args.steps):
         host_search()
+    e2e_one_s = max_over_ranks(time.perf_counter() - t, dist)
+    e2e_one_qps = job_rate(nq * args.steps, world, e2e_one_s)
+    assert np.array_equal(oh_ids.numpy().view(np.uint32), res_op.ids), "e2e results differ"
+
+    # e2e with args.in_flight requests in flight: nbpg_search_async on pinned buffers, one set of
+    # query and result buffers and one stream per request in flight; every step's kernels read its
+    # query rows from pinned host memory and write its results into pinned host memory
+    hbufs = []
+    for i in range(F):
+        hq = torch.from_numpy(q).pin_memory()
+        hb = (hq, torch.empty((nq, k), dtype=torch.int32).pin_memory(),
+              torch.empty((nq, k), dtype=torch.float32).pin_memory(),
+              *(torch.empty(nq, dtype=torch.int32).pin_memory() for _ in range(3)),
+              torch.zeros(1, dtype=torch.int32).pin_memory())
+        hbufs.append(hb)
+
+    def host_search_async(i):
+        hq, hi, hd, hc, hv, hm, hs = hbufs[i]
+        _lib.check(L.nbpg_search_async(idx.handle, hq.data_ptr(), nq, C.byref(prm), sp, 1, k, hi.data_ptr(),
+                                       hd.data_ptr(), hc.data_ptr(), hv.data_ptr(), hm.data_ptr(), hs.data_ptr(),
+                                       C.c_void_p(streams[i].cuda_stream)))
+
+    for _ in range(args.warmup):
+        for i in range(F):
+            host_search_async(i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t = time.perf_counter()
+    for i in range(args.steps):
+        host_search_async(i % F)
+    for st_ in streams:
+        st_.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t, dist)
     e2e_qps = job_rate(nq * args.steps, world, e2e_s)
-    assert np.array_equal(oh_ids.numpy().view(np.uint32), res_op.ids), "e2e results differ"
+    for hq, hi, hd, hc, hv, hm, hs in hbufs:
+        assert int(hs[0]) == 0 and np.array_equal(hi.numpy().view(np.uint32), res_op.ids), "async e2e results differ"
     h2d = nq * CFG["dim"]
     d2h = nq * k * 8 + nq * 12 + 4
 
@@ -1103,7 +1180,7 @@ def main():
     serving = None
     if rank == 0:
         try:
-            serving = time_serving(idx, q, res_op, L_op, k, tuned, value, uneven["batched_qps"], gi, gd)
+            serving = time_serving(idx, q, res_op, L_op, k, tuned, value_one, uneven["batched_qps"], gi, gd)
         except Exception as exc:  # a secondary measurement: reported in the line, not fatal
             serving = {"error": str(exc)}
             log(f"[bench] serving failed: {exc}")
@@ -1122,6 +1199,7 @@ def main():
     alg_bytes_avg_deg = float((res_op.visited.astype(np.float64) * 4.0 * (1.0 + avg_deg) + cmps * row + row).sum())
     peak, peak_src = measured_peaks()
     achieved = alg_bytes / (total_s / args.steps) / 1e9
+    achieved_one = alg_bytes / (one_total_s / args.steps) / 1e9
     tpq = traffic_per_query()
 
     # CPU baseline (rank 0, N=1): the reference algorithm on the host cores
@@ -1147,8 +1225,13 @@ def main():
                        "launch": {"kernel": tuned.kernel, "warps_per_cta": tuned.warps_per_cta,
                                   "lane_width": tuned.lane_width, "prefetch": tuned.prefetch,
                                   "chosen_by": "nbpg_search_autotune"},
+                       "in_flight": F, "one_in_flight_qps": value_one, "e2e_one_in_flight_qps": e2e_one_qps,
+                       "in_flight_note": "value and e2e: steps alternate over in_flight streams, each with its own "
+                                         "buffers (and the library's per-stream scratch), so one request's launch "
+                                         "tail overlaps the next; one_in_flight: the same steps back to back on one "
+                                         "stream (device) / synchronous nbpg_search calls (e2e)",
                        "plain_kernel_qps": plain_qps, "batched_default_qps": batched_default_qps,
-                       "tuned_over_plain": value / plain_qps, "cuda_graph_qps": graph_qps,
+                       "tuned_over_plain": value_one / plain_qps, "cuda_graph_qps": graph_qps,
                        "uneven_L_k_batch": uneven, "fast_mode": fast,
                        "build_s": None if build_s is None else round(build_s, 3), "gt_s": round(gt_s, 3), "avg_degree": round(avg_deg, 2),
                        "L_sweep": sweep, "parallelism": f"replicas x{world}"},
@@ -1161,6 +1244,9 @@ def main():
                                                    "scanned per expansion, the kernel's own counter) + 128 B x "
                                                    "(distances + 1)",
                          "algorithmic_bytes_with_graph_avg_degree": alg_bytes_avg_deg,
+                         "achieved_rule": f"algorithmic bytes of all timed launches / the timed region ({F} requests "
+                                          "in flight, CUDA events from the first launch's start to the last's end)",
+                         "achieved_one_in_flight": achieved_one, "frac_one_in_flight": achieved_one / peak,
                          "traffic": None if tpq is None else tpq * nq},
             "cpu_baseline": cpu, "clocks": clocks,
             "latency_ms": None if not serving or "at_half_peak" not in serving else {
