@@ -24,10 +24,13 @@ def test_device_searches_on_two_streams(gpu_lib, kernel):
     base, q, g = dataset("u8", "l2", dims=32)
     idx = _index(base, g)
     _, rs, _, _ = idx.device_info()
-    half = len(q) // 2
-    sets = [(q[:half], QueryParams(k=10, beamSize=48)), (q[half:], QueryParams(k=5, beamSize=16))]
+    third = len(q) // 3
+    # the third set caps the visited list at L, so most of its queries overflow it and go through
+    # the exact LIST re-run, whose taint list and work counter are per-stream scratch too
+    sets = [(q[:third], QueryParams(k=10, beamSize=48)), (q[third:2 * third], QueryParams(k=5, beamSize=16)),
+            (q[2 * third:], QueryParams(k=10, beamSize=24, visited_factor=1))]
     refs = [idx.search(qq, qp) for qq, qp in sets]
-    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    streams = [torch.cuda.Stream() for _ in sets]
     bufs = []
     for qq, qp in sets:
         qd = torch.zeros((len(qq), rs), dtype=torch.uint8, device="cuda")
