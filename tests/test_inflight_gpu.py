@@ -129,3 +129,27 @@ def test_search_async_cache_and_pageable_buffers(gpu_lib):
     s = L.nbpg_search_async(idx.handle, pq.ctypes.data, len(pq), C.byref(prm), sp, 1, qp.k, pi.ctypes.data,
                             None, None, None, None, None, None)
     assert s == 1, (s, L.nbpg_last_error())  # NBPG_ERR_INVALID_ARG
+
+
+def test_search_async_padded_rows(gpu_lib):
+    """Rows of 100 bytes are padded to 112 on the device, so the async call stages its queries and
+    results with copies inside its graph instead of reading the pinned buffers in place."""
+    import torch
+    from nbpg_gb300 import _lib
+    from nbpg_gb300.index import QueryParams
+    base, q, g = dataset("u8", "l2", dims=100)
+    idx = _index(base, g)
+    L = _lib.lib()
+    qp = QueryParams(k=10, beamSize=32)
+    parts = np.array_split(q, 2)
+    refs = [idx.search(p, qp) for p in parts]
+    bufs = [_async_bufs(p, qp.k) for p in parts]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    for rep in range(4):
+        for i, b in enumerate(bufs):
+            _lib.check(_async_call(L, idx, b, qp, streams[i].cuda_stream))
+    torch.cuda.synchronize()
+    for r, (hq, hi, hd, hc, hv, hm, hs) in zip(refs, bufs):
+        assert int(hs[0]) == 0
+        assert np.array_equal(hi.numpy().view(np.uint32), r.ids) and np.array_equal(hd.numpy(), r.dists)
+        assert np.array_equal(hm.numpy().view(np.uint32), r.cmps)
