@@ -203,6 +203,21 @@ class Index:
         check(_lib.lib().nbpg_search_device(self._h, d_queries, nq, C.byref(prm), d_Ls, d_ks, _p(sp), len(sp),
                                             k_stride, d_out_ids, d_out_dists, d_count, d_visited, d_cmps, stream))
 
+    def search_async(self, h_queries: int, nq: int, qp: QueryParams, h_out_ids: int, k_stride: int,
+                     h_out_dists: int | None = None, h_count: int | None = None, h_visited: int | None = None,
+                     h_cmps: int | None = None, h_status: int | None = None, start_points=(0,), stream: int = 0,
+                     launch: "LaunchConfig | None" = None) -> None:
+        """Enqueue a search on pinned host buffers (raw pointers; query rows of the index's row bytes)
+        on `stream` and return: the results are in the buffers once the stream gets there.  Each
+        distinct set of buffers keeps its own captured graph and scratch, so calls with different
+        buffers may be in flight on different streams (nbpg_search_async)."""
+        sp = np.ascontiguousarray(np.asarray(start_points, dtype=np.uint32))
+        launch = launch or LaunchConfig()
+        prm = launch.params(qp)
+        check(_lib.lib().nbpg_search_async(self._h, h_queries, nq, C.byref(prm), _p(sp), len(sp), k_stride,
+                                           h_out_ids, h_out_dists, h_count, h_visited, h_cmps, h_status,
+                                           C.c_void_p(stream)))
+
     def search_device_adj(self, d_queries: int, nq: int, qp: QueryParams, d_out_ids: int, k_stride: int,
                           d_out_adj: int, d_visited: int | None = None, d_cmps: int | None = None,
                           start_points=(0,), stream: int = 0, launch: "LaunchConfig | None" = None) -> None:

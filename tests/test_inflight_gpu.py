@@ -63,14 +63,12 @@ def _async_bufs(qq, k):
 
 
 def _async_call(L, idx, b, qp, stream):
-    from nbpg_gb300 import _lib
+    """One call through Index.search_async (nbpg_search_async); returns the status 0 or raises."""
     from nbpg_gb300.index import LaunchConfig
-    prm = LaunchConfig(kernel="batched").params(qp)
-    sp = (C.c_uint32 * 1)(0)
     hq, hi, hd, hc, hv, hm, hs = b
-    return L.nbpg_search_async(idx.handle, hq.data_ptr(), len(hq), C.byref(prm), sp, 1, qp.k, hi.data_ptr(),
-                               hd.data_ptr(), hc.data_ptr(), hv.data_ptr(), hm.data_ptr(), hs.data_ptr(),
-                               C.c_void_p(stream))
+    idx.search_async(hq.data_ptr(), len(hq), qp, hi.data_ptr(), qp.k, hd.data_ptr(), hc.data_ptr(), hv.data_ptr(),
+                     hm.data_ptr(), hs.data_ptr(), stream=stream, launch=LaunchConfig(kernel="batched"))
+    return 0
 
 
 def test_search_async_in_flight(gpu_lib):
