@@ -925,8 +925,9 @@ bool gt_tc_supported(uint32_t dtype, uint32_t dims, uint32_t k, size_t smem_opti
 // ranges of about W steps, one per CTA, with about one CTA per SM.  A range may end inside one
 // tile's scan and continue into the next; each range that starts inside a scan records that
 // segment's candidates in a list of `cap` entries per query.  The candidates recorded are those
-// below the bound of the scan's first segment, so cuts are moved off the first W/4 tiles of a
-// scan (ranges then differ from W by at most W/8).
+// below the bound of the scan's first segment, so cuts are moved off the first W/3 tiles of a
+// scan (ranges then differ from W by at most W/6; measured on 10k x 1M: floors of W/16, W/8,
+// W/4, W/3 and W/2 ran in 11.85, 10.65, 9.86, 9.65 and 9.94 ms).
 struct TcSplit {
     uint64_t W, total;
     uint32_t ctas, cap;
@@ -936,7 +937,7 @@ static void tc_cuts(const TcSplit &sp, uint32_t T, uint32_t qtiles, std::vector<
                     std::vector<uint2> &conts)
 {
     cuts.assign(sp.ctas + 1, 0);
-    const uint64_t pmin = std::max<uint64_t>(1, std::min<uint64_t>(sp.W / 4, T / 2));
+    const uint64_t pmin = std::max<uint64_t>(1, std::min<uint64_t>(sp.W / 3, T / 2));
     for (uint32_t c = 1; c < sp.ctas; ++c) {
         uint64_t x = uint64_t(c) * sp.W;
         const uint64_t r = x % T;
