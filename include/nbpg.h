@@ -386,6 +386,15 @@ nbpg_status nbpg_f32_to_u8(const float *rows, uint64_t n, uint32_t dims, uint8_t
  * still usable.  No counterpart in the reference. */
 nbpg_status nbpg_test_gt_timeout(int32_t device);
 
+/* TEST HOOK, not for applications: the tensor engine's work split on the host, no device work.
+ * For qtiles query tiles of T base tiles each, k neighbours and sms SMs: *ctas (the ranges),
+ * cuts[0 .. ctas] (range c = steps [cuts[c], cuts[c + 1]) of the qtiles x T steps in order) and
+ * conts[2 * li], conts[2 * li + 1] (first CTA and count of the ranges that start inside query
+ * tile li's scan); cuts must hold sms + 1 entries and conts 2 * qtiles.  *cap receives the
+ * per-query record capacity. */
+nbpg_status nbpg_test_gt_split(uint32_t qtiles, uint32_t T, uint32_t k, uint32_t sms, uint32_t *ctas, uint64_t *cuts,
+                               uint32_t *conts, uint32_t *cap);
+
 /* ---------------------------------------------------------------------------
  * Build.  Replaces build_vamana (algorithms/nsw.h:547-663) with NSWIndex::batch_insert
  * (nsw.h:110-286), RobustPrune (algorithms/utils/Graph/prune.h:159-209), reverse-edge

@@ -92,6 +92,8 @@ def lib() -> C.CDLL:
                               C.c_uint32, _u32p, _f32p, _u32p, _u32p, _u32p]
     L.nbpg_search_device.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _vp, _vp, _u32p, C.c_uint32,
                                      C.c_uint32, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.nbpg_test_gt_split.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p,
+                                     C.POINTER(C.c_uint64), _u32p, _u32p]
     L.nbpg_search_async.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _u32p, C.c_uint32, C.c_uint32,
                                     _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.nbpg_search_device_adj.argtypes = [_vp, _vp, C.c_uint32, C.POINTER(SearchParams), _u32p, C.c_uint32,

@@ -1185,6 +1185,27 @@ nbpg_status gt_tc_device(uint32_t dtype, uint32_t metric, uint32_t dims, uint32_
 
 }  // namespace nbpg
 
+// Test hook: the work split on the host (the same functions the engine calls), no device work
+extern "C" nbpg_status nbpg_test_gt_split(uint32_t qtiles, uint32_t T, uint32_t k, uint32_t sms, uint32_t *ctas,
+                                          uint64_t *cuts, uint32_t *conts, uint32_t *cap)
+{
+    using namespace nbpg;
+    NBPG_CHECK_ARG(ctas && cuts && conts && cap && qtiles >= 1 && T >= 1 && sms >= 1 && k >= 1, "bad argument");
+    const TcSplit sp = tc_split(qtiles, T, k, sms);
+    NBPG_CHECK_ARG(sp.ctas <= sms, "more ranges than SMs");
+    std::vector<uint64_t> c;
+    std::vector<uint2> ct;
+    tc_cuts(sp, T, qtiles, c, ct);
+    *ctas = sp.ctas;
+    *cap = sp.cap;
+    std::copy(c.begin(), c.end(), cuts);
+    for (uint32_t i = 0; i < qtiles; ++i) {
+        conts[2 * i] = ct[i].x;
+        conts[2 * i + 1] = ct[i].y;
+    }
+    return NBPG_OK;
+}
+
 // Test hook for the failure path: the tensor kNN on a small problem with its base tiles
 // withheld, so the MMA and epilogue waits run out (nothing ever arrives on those barriers);
 // the kernel must record the timeout, tear down (final commit, TMEM freed) and return, and

@@ -90,3 +90,35 @@ def test_compgt_bound_can_exceed_the_next_order_statistic():
         seen.append(d)
     b = compgt_bound(st, 2)
     assert b == 2 and sum(v < b for v in seen) == 3  # more than k = 2 seen values below B
+
+
+def test_engine_split_covers_every_step_once():
+    """The engine's own cut computation (nbpg_test_gt_split, host code, no device work): every
+    (query tile, base tile) step in exactly one range, no more ranges than SMs, every scan's first
+    segment at least min(W/3, T/2) tiles long when the scan continues in other ranges, and the
+    continuation list of each tile naming exactly the ranges that start inside its scan, in order."""
+    import ctypes as C
+    import os
+    from nbpg_gb300 import _lib, build_ext
+    if not os.path.exists(_lib.LIB_PATH):
+        build_ext.build()
+    L = _lib.lib()
+    for qtiles, T, k, sms in [(79, 7813, 100, 152), (1, 7813, 100, 152), (3, 157, 10, 152), (782, 7813, 10, 152),
+                              (2, 5, 10, 148), (153, 64, 50, 152), (40, 781, 100, 16)]:
+        n_ctas, cap = C.c_uint32(), C.c_uint32()
+        cuts = (C.c_uint64 * (sms + 1))()
+        conts = (C.c_uint32 * (2 * qtiles))()
+        _lib.check(L.nbpg_test_gt_split(qtiles, T, k, sms, C.byref(n_ctas), cuts, conts, C.byref(cap)))
+        ctas = n_ctas.value
+        assert 1 <= ctas <= sms and cap.value >= 2048
+        cs = [cuts[i] for i in range(ctas + 1)]
+        assert cs[0] == 0 and cs[-1] == qtiles * T and all(a < b for a, b in zip(cs, cs[1:])), (qtiles, T)
+        per = -(-qtiles * T // sms)
+        W = max(per, min(T, 64))
+        pmin = max(1, min(W // 3, T // 2))
+        for li in range(qtiles):
+            s0, s1 = li * T, (li + 1) * T
+            inside = [c for c in range(1, ctas) if s0 < cs[c] < s1]
+            assert [conts[2 * li] + j for j in range(conts[2 * li + 1])] == inside, (qtiles, T, li)
+            if inside:
+                assert cs[inside[0]] - s0 >= min(pmin, T), (qtiles, T, li)
